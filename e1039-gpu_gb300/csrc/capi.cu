@@ -1,0 +1,261 @@
+// capi.cu -- the C ABI of the library (include/or_gb300.h): context,
+// argument checks, stage launches, error reporting.
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/or_gb300.h"
+#include "or_device.cuh"
+
+namespace orgpu {
+cudaError_t launch_event_reduce(or_hits_view_t, uint8_t *, int, uint32_t *, cudaStream_t, int);
+cudaError_t launch_xz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, int32_t *, uint8_t *, int, cudaStream_t,
+                      int);
+cudaError_t launch_yz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
+                      cudaStream_t, int);
+cudaError_t launch_back_clean(or_tracks_view_t, const uint8_t *, int, cudaStream_t, int);
+cudaError_t launch_global(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
+                          cudaStream_t, int);
+cudaError_t launch_pack(const or_hit_record_t *, const int64_t *, int, const float *, or_hits_view_t, cudaStream_t,
+                        int);
+}  // namespace orgpu
+
+struct or_ctx {
+    int device;
+    int sm_count;
+    or_plane_t *d_plane;
+    bool has_geom;
+    uint32_t *d_errw;
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+int fail(int status, const std::string &msg) {
+    g_last_error = msg;
+    return status;
+}
+int cuda_fail(cudaError_t e, const char *where) {
+    return fail(OR_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+inline cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+int check_ctx(or_ctx_t *ctx, bool need_geom) {
+    if (!ctx) return fail(OR_ERR_ARG, "null context");
+    if (need_geom && !ctx->has_geom) return fail(OR_ERR_NOGEOM, "no geometry set (or_set_geometry)");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(OR_ERR_CUDA, "cudaSetDevice failed");
+    return OR_OK;
+}
+int check_hits(const or_hits_view_t &h) {
+    if (!h.nhits_cham || !h.hits_cham || !h.nhits_hodo || !h.hits_hodo || !h.nhits_prop || !h.hits_prop)
+        return fail(OR_ERR_ARG, "null pointer in hits view");
+    // slot images are fetched with 16-byte bulk copies
+    if (!aligned16(h.hits_cham) || !aligned16(h.hits_hodo) || !aligned16(h.hits_prop))
+        return fail(OR_ERR_ARG, "hit arrays must be 16-byte aligned");
+    return OR_OK;
+}
+int check_tracks(const or_tracks_view_t &t) {
+    if (!t.ntracks || !t.tracks) return fail(OR_ERR_ARG, "null pointer in tracks view");
+    return OR_OK;
+}
+}  // namespace
+
+extern "C" {
+
+const char *or_version(void) { return "e1039-gb300 0.1 (sm_103a)"; }
+const char *or_last_error(void) { return g_last_error.c_str(); }
+const char *or_status_string(int s) {
+    switch (s) {
+    case OR_OK: return "ok";
+    case OR_ERR_ARG: return "invalid argument";
+    case OR_ERR_CUDA: return "CUDA error";
+    case OR_ERR_IO: return "I/O error";
+    case OR_ERR_NOMEM: return "out of device memory";
+    case OR_ERR_CAPACITY: return "capacity exceeded";
+    case OR_ERR_TIMEOUT: return "device wait timed out";
+    case OR_ERR_NOGEOM: return "no geometry";
+    default: return "unknown status";
+    }
+}
+
+int or_create(int device, or_ctx_t **out) {
+    if (!out) return fail(OR_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+    if (device < 0 || device >= ndev) return fail(OR_ERR_ARG, "device index out of range");
+    if ((e = cudaSetDevice(device)) != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    or_ctx_t *c = new or_ctx_t();
+    c->device = device;
+    c->has_geom = false;
+    if ((e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "cudaDeviceGetAttribute");
+    }
+    if ((e = cudaMalloc(&c->d_plane, sizeof(or_plane_t))) != cudaSuccess) {
+        delete c;
+        return fail(OR_ERR_NOMEM, "cudaMalloc geometry");
+    }
+    if ((e = cudaMalloc(&c->d_errw, sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMemset(c->d_errw, 0, sizeof(uint32_t))) != cudaSuccess) {
+        cudaFree(c->d_plane);
+        delete c;
+        return fail(OR_ERR_NOMEM, "cudaMalloc error word");
+    }
+    *out = c;
+    return OR_OK;
+}
+
+int or_destroy(or_ctx_t *ctx) {
+    if (!ctx) return OR_OK;
+    cudaSetDevice(ctx->device);
+    cudaFree(ctx->d_plane);
+    cudaFree(ctx->d_errw);
+    delete ctx;
+    return OR_OK;
+}
+
+int or_set_geometry(or_ctx_t *ctx, const or_plane_t *plane) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (!plane) return fail(OR_ERR_ARG, "null geometry");
+    cudaError_t e = cudaMemcpy(ctx->d_plane, plane, sizeof(or_plane_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "copy geometry");
+    ctx->has_geom = true;
+    return OR_OK;
+}
+
+int or_stream_sync(or_ctx_t *ctx, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    cudaError_t e = cudaStreamSynchronize(S(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    uint32_t w = 0;
+    if ((e = cudaMemcpy(&w, ctx->d_errw, sizeof(w), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_fail(e, "read error word");
+    if (w) {
+        cudaMemset(ctx->d_errw, 0, sizeof(uint32_t));
+        if (w & orgpu::ERRW_TMA_TIMEOUT) return fail(OR_ERR_TIMEOUT, "a bounded bulk-copy wait gave up");
+        if (w & orgpu::ERRW_CAPACITY)
+            return fail(OR_ERR_CAPACITY, "a hit-pair window exceeded its capacity (128 pairs); tracklet skipped");
+    }
+    return OR_OK;
+}
+
+int or_event_reduce(or_ctx_t *ctx, or_hits_view_t hits, uint8_t *toomany, int n_events, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
+    if ((rc = check_hits(hits))) return rc;
+    cudaError_t e = orgpu::launch_event_reduce(hits, toomany, n_events, ctx->d_errw, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "event reducer launch");
+}
+
+int or_xz(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, int32_t *ntracklets, uint8_t *toomany,
+          int n_events, void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany || !ntracklets) return fail(OR_ERR_ARG, "bad event count or output arrays");
+    if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
+    cudaError_t e =
+        orgpu::launch_xz(ctx->d_plane, hits, tracks, ntracklets, toomany, n_events, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "XZ launch");
+}
+
+int or_yz(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany, int n_events,
+          void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
+    if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
+    cudaError_t e =
+        orgpu::launch_yz(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "YZ launch");
+}
+
+int or_back_clean(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
+    if ((rc = check_tracks(tracks))) return rc;
+    cudaError_t e = orgpu::launch_back_clean(tracks, toomany, n_events, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "cleaning launch");
+}
+
+int or_global(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany, int n_events,
+              void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
+    if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
+    cudaError_t e =
+        orgpu::launch_global(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "global tracking launch");
+}
+
+int or_run_batch(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, int32_t *ntracklets,
+                 uint8_t *toomany, int n_events, void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany || !ntracklets) return fail(OR_ERR_ARG, "bad event count or output arrays");
+    if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
+    cudaError_t e = cudaMemsetAsync(ntracklets, 0, sizeof(int32_t) * (size_t)n_events, S(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "clear tracklet counts");
+    if ((rc = or_event_reduce(ctx, hits, toomany, n_events, stream))) return rc;
+    if ((rc = or_xz(ctx, hits, tracks, ntracklets, toomany, n_events, stream))) return rc;
+    if ((rc = or_yz(ctx, hits, tracks, toomany, n_events, stream))) return rc;
+    if ((rc = or_back_clean(ctx, tracks, toomany, n_events, stream))) return rc;
+    return or_global(ctx, hits, tracks, toomany, n_events, stream);
+}
+
+or_hits_view_t or_hits_view_from_collection(void *coll) {
+    // gEventHitCollections, reconstruction_classes.cuh:76-87 (4-byte members,
+    // no padding)
+    or_hits_view_t v;
+    char *b = static_cast<char *>(coll);
+    const size_t E = OR_REF_EVTMAX;
+    v.nhits_cham = reinterpret_cast<uint32_t *>(b);
+    b += sizeof(uint32_t) * E * OR_NCHAM;
+    v.hits_cham = reinterpret_cast<float *>(b);
+    b += sizeof(float) * E * OR_EVT_CHAM_FLOATS;
+    v.nhits_hodo = reinterpret_cast<uint32_t *>(b);
+    b += sizeof(uint32_t) * E * OR_NHODO;
+    v.hits_hodo = reinterpret_cast<float *>(b);
+    b += sizeof(float) * E * OR_EVT_HODO_FLOATS;
+    v.nhits_prop = reinterpret_cast<uint32_t *>(b);
+    b += sizeof(uint32_t) * E * OR_NPROP;
+    v.hits_prop = reinterpret_cast<float *>(b);
+    return v;
+}
+
+or_tracks_view_t or_tracks_view_from_collection(void *coll) {
+    // gEventTrackCollection, reconstruction_classes.cuh:542-544
+    or_tracks_view_t v;
+    char *b = static_cast<char *>(coll);
+    v.ntracks = reinterpret_cast<uint16_t *>(b);
+    v.tracks = reinterpret_cast<float *>(b + sizeof(uint16_t) * (size_t)OR_REF_EVTMAX * OR_NSLOTS);
+    return v;
+}
+
+size_t or_hits_view_bytes(int n) {
+    return (size_t)n * (sizeof(uint32_t) * (OR_NCHAM + OR_NHODO + OR_NPROP) +
+                        sizeof(float) * (OR_EVT_CHAM_FLOATS + OR_EVT_HODO_FLOATS + OR_EVT_PROP_FLOATS));
+}
+size_t or_tracks_view_bytes(int n) {
+    return (size_t)n * (sizeof(uint16_t) * OR_NSLOTS + sizeof(float) * OR_EVT_TRK_FLOATS);
+}
+
+int or_pack_hits(or_ctx_t *ctx, const or_hit_record_t *records, const int64_t *rec_offsets, int n_events,
+                 const float *wire_pos_f, or_hits_view_t hits, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n_events < 0 || !rec_offsets || !wire_pos_f) return fail(OR_ERR_ARG, "bad packer arguments");
+    if ((rc = check_hits(hits))) return rc;
+    cudaError_t e =
+        orgpu::launch_pack(records, rec_offsets, n_events, wire_pos_f, hits, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "packer launch");
+}
+
+}  // extern "C"

@@ -1,0 +1,255 @@
+// er_kernel.cu -- event reducer (hit filtering, declustering, per-channel
+// de-duplication, in-place compaction, station-multiplicity reject).
+//
+// Replaces gkernel_eR<<<N,8>>> (OnlineReconstruction/reconstruction_kernels
+// .cuh:8-172) and event_reduction() (reconstruction_helper.cuh:168-361).
+//
+// Layout on the GPU: one warp per event.  An elected lane stages the
+// occupied part of each plane slot (5*n floats, rounded up to 16 bytes --
+// slot capacities are multiples of 16 bytes, so the round-up stays inside the
+// slot) into shared memory with 1-D TMA bulk copies completing on an
+// mbarrier; planes are taken in batches that fit the warp's buffer.  Each
+// lane then runs the reference's per-plane state machine on one plane out of
+// shared memory, and the warp writes the survivors back coalesced, with the
+// new SoA stride, into the same slot.  Bytes beyond the survivors are left as
+// they were, as the reference leaves them.
+#include "or_device.cuh"
+
+namespace orgpu {
+
+constexpr int ER_WARPS = 4;
+constexpr int ER_BUF_FLOATS = 2048;                 // 8 KB staging buffer per warp
+constexpr int ER_MAX_STAGED_HITS = ER_BUF_FLOATS / 5 + 8;
+constexpr int ER_NPLANES = 48;
+constexpr uint32_t ER_WAIT_LIMIT = 1u << 26;        // bounded mbarrier wait
+
+// the 48 planes the reducer touches: the 24 chambers of the E1039 set
+// (reconstruction_constants.h:60), 16 hodoscopes, 8 prop tubes (K:25-57)
+__device__ __constant__ unsigned char c_er_det[ER_NPLANES] = {
+    1,  2,  3,  4,  5,  6,  13, 14, 15, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30,
+    31, 32, 33, 34, 35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 45, 46, 47, 48, 49, 50, 51, 52, 53, 54};
+
+struct __align__(16) ErWarp {
+    float buf[ER_BUF_FLOATS];
+    uint64_t bar;
+    int n[ER_NPLANES];
+    int kept[ER_NPLANES];
+    int soff[ER_NPLANES];
+    int hoff[ER_NPLANES];
+    uint8_t keep[ER_MAX_STAGED_HITS];
+    uint16_t surv[ER_MAX_STAGED_HITS];
+    uint32_t seen[32][8];  // per-lane channel bitmap, 202 channels
+};
+
+struct PlaneRef {
+    float *slot;
+    uint32_t *count;
+    int cap;
+};
+
+__device__ __forceinline__ PlaneRef er_plane(const or_hits_view_t &hv, long e, int det) {
+    PlaneRef r;
+    if (det <= OR_NCHAM) {
+        r.slot = hv.hits_cham + e * OR_EVT_CHAM_FLOATS + (long)OR_NHITSPARAM * OR_MAXHITS_CHAM * (det - 1);
+        r.count = hv.nhits_cham + e * OR_NCHAM + det - 1;
+        r.cap = OR_MAXHITS_CHAM;
+    } else if (det <= OR_NCHAM + OR_NHODO) {
+        const int k = det - OR_NCHAM - 1;
+        r.slot = hv.hits_hodo + e * OR_EVT_HODO_FLOATS + (long)OR_NHITSPARAM * OR_MAXHITS_HODO * k;
+        r.count = hv.nhits_hodo + e * OR_NHODO + k;
+        r.cap = OR_MAXHITS_HODO;
+    } else {
+        const int k = det - OR_NCHAM - OR_NHODO - 1;
+        r.slot = hv.hits_prop + e * OR_EVT_PROP_FLOATS + (long)OR_NHITSPARAM * OR_MAXHITS_PROP * k;
+        r.count = hv.nhits_prop + e * OR_NPROP + k;
+        r.cap = OR_MAXHITS_PROP;
+    }
+    return r;
+}
+
+// event_reduction() on one staged plane (reconstruction_helper.cuh:168-361).
+// Returns the survivor count; keep[] gets 1/0 per hit, surv[] the survivor
+// indices in order.
+static __device__ int er_reduce_plane(const float *h, int n, int det, uint8_t *keep, uint16_t *surv, uint32_t *seen) {
+    auto chan = [&](int i) { return h[i]; };
+    auto pos = [&](int i) { return h[n + i]; };
+    auto tdc = [&](int i) { return h[2 * n + i]; };
+    auto intime = [&](int i) { return (((int)h[3 * n + i]) & 2) != 0; };
+    auto drift = [&](int i) { return h[4 * n + i]; };
+
+    int cl_first = 0, cl_last = 0, cls = 0;
+    for (int i = 0; i < n; ++i) {
+        keep[i] = 1;
+        if (!intime(i)) {  // H:198
+            keep[i] = 0;
+            continue;
+        }
+        // H:204-230 never changes a flag: uniqueID_curr is reset every hit.
+        if (det > OR_NCHAM) continue;
+        if (cls == 0) {  // H:241-243
+            cl_first = cl_last = i;
+            cls = 1;
+            continue;
+        }
+        const float dc = fabsf(chan(i) - chan(cl_last));
+        if (dc > 1 || i == n - 1) {  // H:258
+            if (i == n - 1 && dc <= 1) {
+                cl_last = i;
+                ++cls;
+            }
+            if (cls == 2) {  // H:267-295
+                const int a = cl_first, b = cl_last;
+                const float w_max = (float)(0.9 * 0.5 * (double)(pos(b) - pos(a)));
+                const float w_min = (float)(4.0 / 9.0 * (double)w_max);
+                if ((drift(a) > w_max && drift(b) > w_min) || (drift(a) > w_min && drift(b) > w_max)) {
+                    if (drift(a) > drift(b))
+                        keep[a] = 0;
+                    else
+                        keep[b] = 0;
+                } else {
+                    const float dt = tdc(a) - tdc(b);
+                    if ((((double)dt >= 0.0 && (double)dt < 8.0) || ((double)dt <= 0.0 && (double)dt > -8.0)) &&
+                        (det >= 19 && det <= 24)) {
+                        keep[a] = 0;
+                        keep[b] = 0;
+                    }
+                }
+            }
+            if (cls >= 3) {  // H:297-318: members are the in-time hits in [first, last]
+                float dt_mean = 0.0f;
+                int prev = cl_first;
+                for (int m = cl_first + 1; m <= cl_last; ++m) {
+                    if (!intime(m)) continue;
+                    const float d = tdc(m) - tdc(prev);
+                    dt_mean += ((double)d > 0.0 ? d : (tdc(prev) - tdc(m)));
+                    prev = m;
+                }
+                dt_mean = dt_mean / (float)(cls - 1);
+                const bool all = (double)dt_mean < 10.0;
+                for (int m = cl_first; m <= cl_last; ++m) {
+                    if (!intime(m)) continue;
+                    if (all || m != cl_first) keep[m] = 0;
+                }
+            }
+            cls = 0;
+        } else {
+            cl_last = i;
+            ++cls;
+        }
+    }
+    // H:334-349, first survivor per channel wins
+#pragma unroll
+    for (int w = 0; w < 8; ++w) seen[w] = 0u;
+    int nred = 0;
+    for (int i = 0; i < n; ++i) {
+        if (!keep[i]) continue;
+        const int c = (short)chan(i);
+        if (c >= 0 && c < 202) {
+            const uint32_t bit = 1u << (c & 31);
+            if (seen[c >> 5] & bit) {
+                keep[i] = 0;
+                continue;
+            }
+            seen[c >> 5] |= bit;
+        }
+        surv[nred++] = (uint16_t)i;
+    }
+    return nred;
+}
+
+__global__ void __launch_bounds__(ER_WARPS * 32) er_kernel(or_hits_view_t hv, uint8_t *__restrict__ toomany,
+                                                           int n_events, uint32_t *__restrict__ errw) {
+    __shared__ ErWarp sm[ER_WARPS];
+    const int w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    ErWarp &S = sm[w];
+    if (lane == 0) mbar_init(&S.bar, 1);
+    __syncwarp();
+    uint32_t phase = 0;
+
+    for (long e = (long)blockIdx.x * ER_WARPS + w; e < n_events; e += (long)gridDim.x * ER_WARPS) {
+        for (int p = lane; p < ER_NPLANES; p += 32) {
+            const PlaneRef r = er_plane(hv, e, c_er_det[p]);
+            const int n = (int)*r.count;
+            S.n[p] = n < r.cap ? n : r.cap;
+        }
+        __syncwarp();
+        int p0 = 0;
+        while (p0 < ER_NPLANES) {
+            // batch [p0, p1): planes whose staged images fit the buffer
+            int p1 = p0, off = 0, hits = 0;
+            while (p1 < ER_NPLANES) {
+                const int sz = (5 * S.n[p1] + 3) & ~3;
+                if (off + sz > ER_BUF_FLOATS) break;
+                if (lane == 0) {
+                    S.soff[p1] = off;
+                    S.hoff[p1] = hits;
+                }
+                off += sz;
+                hits += S.n[p1];
+                ++p1;
+            }
+            __syncwarp();
+            if (off > 0) {
+                if (lane == 0) {
+                    fence_proxy_async_smem();  // buffer was read by the generic proxy
+                    mbar_arrive_expect_tx(&S.bar, (uint32_t)off * 4u);
+                    for (int p = p0; p < p1; ++p) {
+                        const int sz = (5 * S.n[p] + 3) & ~3;
+                        if (sz == 0) continue;
+                        const PlaneRef r = er_plane(hv, e, c_er_det[p]);
+                        tma_load_1d(S.buf + S.soff[p], r.slot, (uint32_t)sz * 4u, &S.bar);
+                    }
+                }
+                if (!mbar_wait_bounded(&S.bar, phase, ER_WAIT_LIMIT)) {
+                    if (lane == 0) atomicOr(errw, ERRW_TMA_TIMEOUT);
+                    return;
+                }
+                phase ^= 1u;
+            }
+            for (int p = p0 + lane; p < p1; p += 32) {
+                S.kept[p] = er_reduce_plane(S.buf + S.soff[p], S.n[p], c_er_det[p], S.keep + S.hoff[p],
+                                            S.surv + S.hoff[p], S.seen[lane]);
+            }
+            __syncwarp();
+            for (int p = p0; p < p1; ++p) {
+                const int n = S.n[p], nk = S.kept[p];
+                const PlaneRef r = er_plane(hv, e, c_er_det[p]);
+                const float *src = S.buf + S.soff[p];
+                const uint16_t *sv = S.surv + S.hoff[p];
+                for (int i = lane; i < 5 * nk; i += 32) {
+                    const int f = i / nk;
+                    const int k = i - f * nk;
+                    r.slot[i] = src[f * n + sv[k]];
+                }
+                if (lane == 0) *r.count = (uint32_t)nk;
+            }
+            __syncwarp();
+            p0 = p1;
+        }
+        // K:128-139: station sums of the reduced chamber counts
+        if (lane == 0) {
+            int m[4] = {0, 0, 0, 0};
+            for (int p = 0; p < 24; ++p) {
+                const int d = c_er_det[p];
+                const int st = d <= 12 ? 0 : (d - 7) / 6;
+                m[st] += S.kept[p];
+            }
+            toomany[e] = (uint8_t)((m[0] > MAXD0) || (m[1] > MAXD2) || (m[2] > MAXD3) || (m[3] > MAXD3));
+        }
+        __syncwarp();
+    }
+}
+
+// Host launcher.
+cudaError_t launch_event_reduce(or_hits_view_t hv, uint8_t *toomany, int n_events, uint32_t *errw,
+                                cudaStream_t stream, int sm_count) {
+    if (n_events <= 0) return cudaSuccess;
+    long blocks = (n_events + ER_WARPS - 1) / ER_WARPS;
+    const long cap = (long)sm_count * 12;
+    if (blocks > cap) blocks = cap;
+    er_kernel<<<(unsigned)blocks, ER_WARPS * 32, 0, stream>>>(hv, toomany, n_events, errw);
+    return cudaGetLastError();
+}
+
+}  // namespace orgpu

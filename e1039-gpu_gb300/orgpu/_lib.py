@@ -1,0 +1,83 @@
+"""ctypes binding of liborgpu.so (include/or_gb300.h).
+
+The library is the product: there is no Python or CPU fallback.  If the
+shared object is missing or cannot be loaded, every entry point raises.
+"""
+import ctypes as C
+import os
+
+from . import layout as L
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "liborgpu.so")
+
+OR_OK, OR_ERR_ARG, OR_ERR_CUDA, OR_ERR_IO, OR_ERR_NOMEM, OR_ERR_CAPACITY, OR_ERR_TIMEOUT, OR_ERR_NOGEOM = range(8)
+
+# every symbol include/or_gb300.h declares
+EXPORTS = ("or_version", "or_last_error", "or_status_string", "or_geometry_load", "or_create", "or_destroy",
+           "or_set_geometry", "or_stream_sync", "or_event_reduce", "or_xz", "or_yz", "or_back_clean", "or_global",
+           "or_run_batch", "or_hits_view_from_collection", "or_tracks_view_from_collection", "or_hits_view_bytes",
+           "or_tracks_view_bytes", "or_pack_hits")
+
+
+class OrError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """Load liborgpu.so (built by build_lib.build()); raise if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OrError(-1, f"liborgpu.so not built at {LIB_PATH}; run __graft_entry__.build()")
+    lb = C.CDLL(LIB_PATH)
+    P = C.POINTER
+    vp = C.c_void_p
+    lb.or_version.restype = C.c_char_p
+    lb.or_last_error.restype = C.c_char_p
+    lb.or_status_string.restype = C.c_char_p
+    lb.or_status_string.argtypes = [C.c_int]
+    lb.or_geometry_load.argtypes = [C.c_char_p, P(L.OrPlane), vp]
+    lb.or_create.argtypes = [C.c_int, P(vp)]
+    lb.or_destroy.argtypes = [vp]
+    lb.or_set_geometry.argtypes = [vp, P(L.OrPlane)]
+    lb.or_stream_sync.argtypes = [vp, vp]
+    lb.or_event_reduce.argtypes = [vp, L.OrHitsView, vp, C.c_int, vp]
+    lb.or_xz.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, vp, C.c_int, vp]
+    lb.or_yz.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, C.c_int, vp]
+    lb.or_back_clean.argtypes = [vp, L.OrTracksView, vp, C.c_int, vp]
+    lb.or_global.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, C.c_int, vp]
+    lb.or_run_batch.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, vp, C.c_int, vp]
+    lb.or_hits_view_from_collection.argtypes = [vp]
+    lb.or_hits_view_from_collection.restype = L.OrHitsView
+    lb.or_tracks_view_from_collection.argtypes = [vp]
+    lb.or_tracks_view_from_collection.restype = L.OrTracksView
+    lb.or_hits_view_bytes.argtypes = [C.c_int]
+    lb.or_hits_view_bytes.restype = C.c_size_t
+    lb.or_tracks_view_bytes.argtypes = [C.c_int]
+    lb.or_tracks_view_bytes.restype = C.c_size_t
+    lb.or_pack_hits.argtypes = [vp, vp, vp, C.c_int, vp, L.OrHitsView, vp]
+    for name in EXPORTS:
+        getattr(lb, name)
+    _lib = lb
+    return _lib
+
+
+def check(rc, what="call"):
+    if rc != OR_OK:
+        raise OrError(rc, f"{what} failed: {lib().or_status_string(rc).decode()}: {lib().or_last_error().decode()}")
+
+
+def geometry_load(path):
+    """Parse a geometry table with the library's loader -> (OrPlane, wire_pos[55,400])."""
+    import numpy as np
+    p = L.OrPlane()
+    wp = np.zeros(L.NDET * L.WIREPOS_STRIDE, np.float64)
+    check(lib().or_geometry_load(str(path).encode(), C.byref(p), wp.ctypes.data), "or_geometry_load")
+    return p, wp.reshape(L.NDET, L.WIREPOS_STRIDE)

@@ -1,0 +1,165 @@
+"""Host-side mirror of the reference's launch chain
+(OnlineReconstruction/online_reconstruction.cu:738-1033) on top of the C ABI.
+
+`Reconstruction` owns a library context on one device; `DeviceBatch` owns the
+device buffers of a batch of events in the reference layout (hit
+collections, track collections, HasTooManyHits, nTracklets).  The stage
+methods keep the reference kernel names' meaning and order:
+
+    gkernel_eR                  -> Reconstruction.event_reduce
+    gKernel_XZ_tracking         -> Reconstruction.xz_tracking
+    gKernel_YZ_tracking         -> Reconstruction.yz_tracking
+    gKernel_BackTrackCleaning*  -> Reconstruction.back_track_cleaning
+    gKernel_Global_tracking     -> Reconstruction.global_tracking
+
+PyTorch is used for device memory and streams only; all work runs in the
+library's sm_103a kernels.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from . import layout as L
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise _lib.OrError(_lib.OR_ERR_CUDA, "no CUDA device: the reconstruction path runs on the GPU only")
+    return torch
+
+
+class DeviceBatch:
+    """Device buffers of n events in the reference layout."""
+
+    def __init__(self, n_events, device=0, with_tracks=True):
+        torch = _torch()
+        self.n = int(n_events)
+        dev = torch.device("cuda", device)
+        u32, f32 = torch.int32, torch.float32
+        n = self.n
+        self.nhits_cham = torch.zeros(n * L.NCHAM, dtype=u32, device=dev)
+        self.hits_cham = torch.empty(n * L.EVT_CHAM_FLOATS, dtype=f32, device=dev)
+        self.nhits_hodo = torch.zeros(n * L.NHODO, dtype=u32, device=dev)
+        self.hits_hodo = torch.empty(n * L.EVT_HODO_FLOATS, dtype=f32, device=dev)
+        self.nhits_prop = torch.zeros(n * L.NPROP, dtype=u32, device=dev)
+        self.hits_prop = torch.empty(n * L.EVT_PROP_FLOATS, dtype=f32, device=dev)
+        self.toomany = torch.zeros(n, dtype=torch.uint8, device=dev)
+        self.ntracklets = torch.zeros(n, dtype=torch.int32, device=dev)
+        if with_tracks:
+            self.ntracks = torch.zeros(n * L.NSLOTS, dtype=torch.int16, device=dev)
+            self.tracks = torch.zeros(n * L.EVT_TRK_FLOATS, dtype=f32, device=dev)
+        else:
+            self.ntracks = self.tracks = None
+
+    def hits_view(self):
+        v = L.OrHitsView()
+        (v.nhits_cham, v.hits_cham, v.nhits_hodo, v.hits_hodo, v.nhits_prop,
+         v.hits_prop) = (t.data_ptr() for t in (self.nhits_cham, self.hits_cham, self.nhits_hodo, self.hits_hodo,
+                                                 self.nhits_prop, self.hits_prop))
+        return v
+
+    def tracks_view(self):
+        v = L.OrTracksView()
+        v.ntracks = self.ntracks.data_ptr()
+        v.tracks = self.tracks.data_ptr()
+        return v
+
+    # -- host <-> device ----------------------------------------------------
+    def upload_hits(self, h):
+        """Copy a layout.HostHits (numpy) of the same size to the device."""
+        torch = _torch()
+        assert h.n == self.n
+        for dst, src in zip((self.nhits_cham, self.hits_cham, self.nhits_hodo, self.hits_hodo, self.nhits_prop,
+                             self.hits_prop), h.arrays()):
+            dst.copy_(torch.from_numpy(src.view(np.int32) if src.dtype == np.uint32 else src))
+
+    def upload_tracks(self, t):
+        torch = _torch()
+        self.ntracks.copy_(torch.from_numpy(t.ntracks.view(np.int16)))
+        self.tracks.copy_(torch.from_numpy(t.tracks))
+
+    def download_hits(self):
+        h = L.HostHits.__new__(L.HostHits)
+        h.n = self.n
+        h.nhits_cham = self.nhits_cham.cpu().numpy().view(np.uint32)
+        h.hits_cham = self.hits_cham.cpu().numpy()
+        h.nhits_hodo = self.nhits_hodo.cpu().numpy().view(np.uint32)
+        h.hits_hodo = self.hits_hodo.cpu().numpy()
+        h.nhits_prop = self.nhits_prop.cpu().numpy().view(np.uint32)
+        h.hits_prop = self.hits_prop.cpu().numpy()
+        return h
+
+    def download_tracks(self):
+        t = L.HostTracks.__new__(L.HostTracks)
+        t.n = self.n
+        t.ntracks = self.ntracks.cpu().numpy().view(np.uint16)
+        t.tracks = self.tracks.cpu().numpy()
+        return t
+
+
+class Reconstruction:
+    """One library context (one device) with its geometry."""
+
+    def __init__(self, plane, device=0):
+        torch = _torch()
+        self.device = device
+        self.lib = _lib.lib()
+        self.ctx = C.c_void_p()
+        _lib.check(self.lib.or_create(device, C.byref(self.ctx)), "or_create")
+        self.plane = plane
+        _lib.check(self.lib.or_set_geometry(self.ctx, C.byref(plane)), "or_set_geometry")
+        self._torch = torch
+
+    def close(self):
+        if self.ctx:
+            self.lib.or_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _stream(self, stream):
+        if stream is None:
+            stream = self._torch.cuda.current_stream(self.device)
+        return C.c_void_p(stream.cuda_stream)
+
+    # stage entry points (online_reconstruction.cu:776-894)
+    def event_reduce(self, b, stream=None):
+        _lib.check(self.lib.or_event_reduce(self.ctx, b.hits_view(), b.toomany.data_ptr(), b.n,
+                                            self._stream(stream)), "or_event_reduce")
+
+    def xz_tracking(self, b, stream=None):
+        _lib.check(self.lib.or_xz(self.ctx, b.hits_view(), b.tracks_view(), b.ntracklets.data_ptr(),
+                                  b.toomany.data_ptr(), b.n, self._stream(stream)), "or_xz")
+
+    def yz_tracking(self, b, stream=None):
+        _lib.check(self.lib.or_yz(self.ctx, b.hits_view(), b.tracks_view(), b.toomany.data_ptr(), b.n,
+                                  self._stream(stream)), "or_yz")
+
+    def back_track_cleaning(self, b, stream=None):
+        _lib.check(self.lib.or_back_clean(self.ctx, b.tracks_view(), b.toomany.data_ptr(), b.n,
+                                          self._stream(stream)), "or_back_clean")
+
+    def global_tracking(self, b, stream=None):
+        _lib.check(self.lib.or_global(self.ctx, b.hits_view(), b.tracks_view(), b.toomany.data_ptr(), b.n,
+                                      self._stream(stream)), "or_global")
+
+    def run_batch(self, b, stream=None):
+        _lib.check(self.lib.or_run_batch(self.ctx, b.hits_view(), b.tracks_view(), b.ntracklets.data_ptr(),
+                                         b.toomany.data_ptr(), b.n, self._stream(stream)), "or_run_batch")
+
+    def pack(self, b, d_records, d_offsets, d_wire_pos_f, stream=None):
+        """Device packer: compact records (device uint8 tensor of HIT_RECORD_DTYPE
+        bytes) + int64 offsets -> b's hit collections."""
+        _lib.check(self.lib.or_pack_hits(self.ctx, d_records.data_ptr(), d_offsets.data_ptr(), b.n,
+                                          d_wire_pos_f.data_ptr(), b.hits_view(), self._stream(stream)),
+                   "or_pack_hits")
+
+    def sync(self, stream=None):
+        """Wait for the stream and raise on device-side error words."""
+        _lib.check(self.lib.or_stream_sync(self.ctx, self._stream(stream)), "or_stream_sync")

@@ -1,0 +1,113 @@
+/*
+ * or_gb300.h -- C ABI of the GB300 (sm_103a) online-reconstruction library.
+ *
+ * This is the drop-in boundary for the reference's hot path.  Each stage
+ * entry point replaces one reference kernel launch of the host driver
+ * (OnlineReconstruction/online_reconstruction.cu:776-894) and takes the same
+ * buffers, in the same memory layout (or_layout.h), mutating them in place
+ * the way the reference kernels do:
+ *
+ *   or_event_reduce    <- gkernel_eR<<<N,8>>>                 reconstruction_kernels.cuh:8
+ *   or_xz              <- gKernel_XZ_tracking<<<N,32>>>        reconstruction_kernels.cuh:182
+ *   or_yz              <- gKernel_YZ_tracking<<<N,32>>>        reconstruction_kernels.cuh:864
+ *   or_back_clean      <- gKernel_BackTrackCleaning<<<N,32>>> and
+ *                         gKernel_BackTrackCleaning_crossthreads<<<N,32>>>
+ *                                                              reconstruction_helper.cuh:1789, :1846
+ *   or_global          <- gKernel_Global_tracking<<<N,32>>>    reconstruction_kernels.cuh:1841
+ *   or_run_batch       <- the whole launch chain above
+ *
+ * All pointers inside the views are DEVICE pointers unless the name of the
+ * call says _host.  `stream` is a cudaStream_t passed as void* (NULL = the
+ * legacy default stream).  Calls are asynchronous on that stream, like the
+ * kernel launches they replace, except where noted.
+ *
+ * Per-event outcome: `toomany` (uint8, one per event) is the reference's
+ * gEvent::HasTooManyHits, set by the event reducer on station multiplicity,
+ * by XZ on bin overflow or tracklet-storage exhaustion.  Events with it set
+ * are skipped by the later stages, as in the reference.
+ *
+ * Every call returns an or_status_t.  Argument errors are detected on the
+ * host before any launch; CUDA errors are reported as OR_ERR_CUDA with the
+ * message available from or_last_error().
+ */
+#ifndef OR_GB300_H
+#define OR_GB300_H
+
+#include "or_layout.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum or_status {
+    OR_OK = 0,
+    OR_ERR_ARG = 1,      /* bad pointer, count or size */
+    OR_ERR_CUDA = 2,     /* a CUDA call failed; see or_last_error() */
+    OR_ERR_IO = 3,       /* geometry file missing or unreadable */
+    OR_ERR_NOMEM = 4,    /* device allocation failed */
+    OR_ERR_CAPACITY = 5, /* an input exceeds a fixed capacity */
+    OR_ERR_TIMEOUT = 6,  /* a bounded device wait gave up */
+    OR_ERR_NOGEOM = 7    /* no geometry set on the context */
+} or_status_t;
+
+typedef struct or_ctx or_ctx_t;
+
+/* Library version string and the CUDA arch it was built for. */
+const char *or_version(void);
+/* Text of the most recent error on this thread. */
+const char *or_last_error(void);
+const char *or_status_string(int status);
+
+/* Geometry: parse the plain-text geometry table (online_reconstruction.cu
+ * :123-188) and compute wire positions (:191-218).  wire_pos may be NULL;
+ * otherwise it must hold OR_NDET*OR_WIREPOS_STRIDE doubles.  Host only. */
+int or_geometry_load(const char *path, or_plane_t *plane, double *wire_pos);
+
+/* Context: one per device.  or_create() selects `device`, allocates the
+ * context's small device state, and records a copy of nothing else. */
+int or_create(int device, or_ctx_t **out);
+int or_destroy(or_ctx_t *ctx);
+/* Copy a host or_plane_t to the device (online_reconstruction.cu:754). */
+int or_set_geometry(or_ctx_t *ctx, const or_plane_t *plane);
+/* Wait for `stream` and report the device-side error words raised since the
+ * last call: OR_ERR_TIMEOUT when a bounded bulk-copy wait gave up,
+ * OR_ERR_CAPACITY when a hit-pair window overflowed its 128-entry list (that
+ * tracklet or track is left unextended).  The reference has no such report;
+ * its kernels write past their arrays instead. */
+int or_stream_sync(or_ctx_t *ctx, void *stream);
+
+/* Stage entry points on device buffers (see the table above). */
+int or_event_reduce(or_ctx_t *ctx, or_hits_view_t hits, uint8_t *toomany, int n_events, void *stream);
+int or_xz(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, int32_t *ntracklets, uint8_t *toomany,
+          int n_events, void *stream);
+int or_yz(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany, int n_events,
+          void *stream);
+int or_back_clean(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, void *stream);
+int or_global(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany, int n_events,
+              void *stream);
+/* The five stages in the reference order, one call. */
+int or_run_batch(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, int32_t *ntracklets,
+                 uint8_t *toomany, int n_events, void *stream);
+
+/* Map the reference's fixed-capacity structs (EstnEvtMax = 10000 events)
+ * onto views.  `coll` points at a gEventHitCollections / gEventTrackCollection
+ * laid out exactly as reconstruction_classes.cuh:76-87 / :542-544. */
+or_hits_view_t or_hits_view_from_collection(void *coll);
+or_tracks_view_t or_tracks_view_from_collection(void *coll);
+/* Bytes of the views for n_events events. */
+size_t or_hits_view_bytes(int n_events);
+size_t or_tracks_view_bytes(int n_events);
+
+/* Device-side packer: compact hit records (det, elem, tdc, drift, flag),
+ * sorted by (det, elem, tdc) inside each event, into the reference hit
+ * layout, with pos = (float)wire_pos[det][elem] (online_reconstruction.cu
+ * :589-636).  rec_offsets[e]..rec_offsets[e+1] are event e's records.
+ * wire_pos_f is a device float table [OR_NDET*OR_WIREPOS_STRIDE]. */
+int or_pack_hits(or_ctx_t *ctx, const or_hit_record_t *records, const int64_t *rec_offsets, int n_events,
+                 const float *wire_pos_f, or_hits_view_t hits, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OR_GB300_H */

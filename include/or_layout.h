@@ -1,0 +1,162 @@
+/*
+ * or_layout.h -- in-memory layout of the e1039 online-reconstruction event,
+ * hit, track and geometry records.  Plain C, shared by the CUDA library, its
+ * C-ABI callers and the CPU oracle.
+ *
+ * The layout is the reference's own, kept bit-for-bit so that buffers filled
+ * by a reference-style host (OnlineReconstruction/online_reconstruction.cu
+ * :589-636) can be handed to this library unchanged:
+ *
+ *  - hit slot of plane d in event e starts at
+ *        e*OR_EVT_FLOATS[type] + 5*OR_MAXHITS[type]*(d - d0[type])  floats
+ *    (reconstruction_classes.cuh:89-102, reconstruction_constants.h:166-180);
+ *  - inside a slot the five hit fields are SoA with stride = the plane's
+ *    current hit count n:  [chan | pos | tdc | flag | drift], n floats each
+ *    (reconstruction_classes.cuh:9, :18-46);
+ *  - a track record is 148 floats (reconstruction_classes.cuh:558-635);
+ *  - an event owns 512 track records in 32 slots of 16
+ *    (reconstruction_classes.cuh:542-556); the slot count of slot s in
+ *    event e is ntracks[e*32+s] (unsigned short).
+ *
+ * The fixed-capacity reference structs (gEventHitCollections,
+ * gEventTrackCollection, gEvent) are sized for EstnEvtMax = 10000 events;
+ * the views below carry plain pointers so any number of events can be used,
+ * and or_hits_view_from_collection()/or_tracks_view_from_collection() in
+ * or_gb300.h map a reference struct onto them.
+ */
+#ifndef OR_LAYOUT_H
+#define OR_LAYOUT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* detector planes: 1..30 drift chambers, 31..46 hodoscopes, 47..54 prop tubes
+ * (reconstruction_constants.h:10-13) */
+#define OR_NCHAM 30
+#define OR_NHODO 16
+#define OR_NPROP 8
+#define OR_NDET 55 /* index 0 unused */
+
+#define OR_NHITSPARAM 5
+#define OR_MAXHITS_CHAM 200 /* reconstruction_constants.h:173 */
+#define OR_MAXHITS_HODO 60  /* :174 */
+#define OR_MAXHITS_PROP 120 /* :175 */
+
+#define OR_EVT_CHAM_FLOATS (OR_NCHAM * OR_NHITSPARAM * OR_MAXHITS_CHAM) /* 30000 */
+#define OR_EVT_HODO_FLOATS (OR_NHODO * OR_NHITSPARAM * OR_MAXHITS_HODO) /* 4800 */
+#define OR_EVT_PROP_FLOATS (OR_NPROP * OR_NHITSPARAM * OR_MAXHITS_PROP) /* 4800 */
+
+#define OR_NTRKPARAM 148 /* reconstruction_constants.h:171 */
+#define OR_TRKMAX 512    /* :181 */
+#define OR_NSLOTS 32     /* THREADS_PER_BLOCK, :21 */
+#define OR_SLOTCAP (OR_TRKMAX / OR_NSLOTS) /* 16 */
+#define OR_EVT_TRK_FLOATS (OR_TRKMAX * OR_NTRKPARAM) /* 75776 */
+#define OR_MAXHITS_PER_TRACK 18
+
+/* wire-position table row stride: wire_pos[det*400 + element]
+ * (online_reconstruction.cu:191) */
+#define OR_WIREPOS_STRIDE 400
+
+/* capacity of the reference's fixed structs (reconstruction_constants.h:20) */
+#define OR_REF_EVTMAX 10000
+
+/* track-record field offsets: the setter offsets the kernels write
+ * (reconstruction_classes.cuh:558-635) */
+enum or_trk_field {
+    OR_TRK_STID = 0,
+    OR_TRK_THREAD = 1,
+    OR_TRK_NHITS = 2,
+    OR_TRK_CHI2 = 3,
+    OR_TRK_CHI2VTX = 4,
+    OR_TRK_TX = 5,
+    OR_TRK_TY = 6,
+    OR_TRK_X0 = 7,
+    OR_TRK_Y0 = 8,
+    OR_TRK_INVP = 9,
+    OR_TRK_ERR_TX = 10,
+    OR_TRK_ERR_TY = 11,
+    OR_TRK_ERR_X0 = 12,
+    OR_TRK_ERR_Y0 = 13,
+    OR_TRK_ERR_INVP = 14,
+    OR_TRK_CHARGE = 15,
+    OR_TRK_VX = 16,
+    OR_TRK_PX = 19,
+    OR_TRK_HIT_DETID = 22,
+    OR_TRK_HIT_CHAN = 40,
+    OR_TRK_HIT_POS = 58,
+    OR_TRK_HIT_DRIFT = 76,
+    OR_TRK_HIT_SIGN = 94,
+    OR_TRK_HIT_TDC = 112,
+    OR_TRK_HIT_RESID = 130
+};
+
+/* Geometry carrier: field-for-field the reference's gPlane
+ * (reconstruction_classes.cuh:947-977), 55 entries per field. */
+typedef struct or_plane {
+    float z[OR_NDET];
+    int nelem[OR_NDET];
+    float cellwidth[OR_NDET];
+    float spacing[OR_NDET];
+    float xoffset[OR_NDET];
+    float scalex[OR_NDET];
+    float x0[OR_NDET];
+    float x1[OR_NDET];
+    float x2[OR_NDET];
+    float costheta[OR_NDET];
+    float scaley[OR_NDET];
+    float y0[OR_NDET];
+    float y1[OR_NDET];
+    float y2[OR_NDET];
+    float sintheta[OR_NDET];
+    float resolution[OR_NDET];
+    float p1x_w1[OR_NDET];
+    float p1y_w1[OR_NDET];
+    float p1z_w1[OR_NDET];
+    float deltapx[OR_NDET];
+    float deltapy[OR_NDET];
+    float deltapz[OR_NDET];
+    float dp1x[OR_NDET];
+    float dp1y[OR_NDET];
+    float dp1z[OR_NDET];
+    float slope_max[OR_NDET];
+    float inter_max[OR_NDET];
+} or_plane_t;
+
+/* Hit collections of n_events events in the reference layout.  Either host
+ * or device pointers, depending on the call. */
+typedef struct or_hits_view {
+    uint32_t *nhits_cham; /* [n_events*30] */
+    float *hits_cham;     /* [n_events*30000] */
+    uint32_t *nhits_hodo; /* [n_events*16] */
+    float *hits_hodo;     /* [n_events*4800] */
+    uint32_t *nhits_prop; /* [n_events*8] */
+    float *hits_prop;     /* [n_events*4800] */
+} or_hits_view_t;
+
+/* Track collections of n_events events in the reference layout. */
+typedef struct or_tracks_view {
+    uint16_t *ntracks; /* [n_events*32] */
+    float *tracks;     /* [n_events*512*148] */
+} or_tracks_view_t;
+
+/* Compact hit record, the raw-event format of the reference's input
+ * (OnlineReconstruction/LoadInput.h:10-20: detectorID, elementID, tdcTime,
+ * driftDistance, plus the in-time flag bit the host packer turns into
+ * flag = 1<<in_time, online_reconstruction.cu:599). */
+typedef struct or_hit_record {
+    int16_t det;
+    int16_t elem;
+    float tdc;
+    float drift;
+    int32_t flag; /* the packed float flag value: 2 = in time, 1 = out of time */
+} or_hit_record_t;
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OR_LAYOUT_H */

@@ -1,0 +1,73 @@
+/*
+ * or_oracle.h -- CPU oracle for the e1039 online-reconstruction hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * algorithm (OnlineReconstruction/reconstruction_kernels.cuh and
+ * reconstruction_helper.cuh), used by the tests, by __graft_entry__.smoke()
+ * and by bench.py's CPU baseline as the checker.  The CUDA library never links
+ * or calls it.
+ *
+ * Every stage works on the reference memory layout (or_layout.h) and mutates
+ * the buffers in place exactly like the reference kernels do.  Arithmetic is
+ * IEEE single precision, one rounding per operation (built with
+ * -ffp-contract=off), matching a reference build with -fmad=false.
+ *
+ * Where the reference is not deterministic the oracle fixes one canonical
+ * behaviour, shared with the CUDA kernels:
+ *  - XZ tracklets go to slots round-robin per station-3 half (the k-th
+ *    tracklet of parity p lands in slot 2*(k%16)+p, position k/16), in the
+ *    order (reference thread t, bin pair, candidate);
+ *  - per-thread/per-slot scratch arrays start from a sentinel that never
+ *    pairs (the reference leaves them uninitialised);
+ *  - the cross-slot cleaning pass visits slots 0..31 in order.
+ */
+#ifndef OR_ORACLE_H
+#define OR_ORACLE_H
+
+#include "../include/or_layout.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* geometry: OnlineReconstruction/online_reconstruction.cu:123-218 */
+int orc_parse_geometry(const char *path, or_plane_t *plane, double *wire_pos /* [55*400] */);
+
+/* per-event status bits (the reference's HasTooManyHits plus the reason) */
+#define ORC_ST_TOOMANY_ER 1u      /* station multiplicity over limit, K:135-139 */
+#define ORC_ST_TOOMANY_XZBIN 2u   /* >20 pairs in an element bin, K:359-375 */
+#define ORC_ST_TOOMANY_TKL 4u     /* tracklet storage exhausted, K:719-839 */
+
+/* Stage entry points; n_threads <= 0 uses all hardware threads. */
+void orc_event_reduce(or_hits_view_t h, uint8_t *toomany, uint32_t *status, int n_events, int n_threads);
+void orc_xz(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, int32_t *ntracklets,
+            uint8_t *toomany, uint32_t *status, int n_events, int n_threads);
+void orc_yz(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, const uint8_t *toomany,
+            int n_events, int n_threads);
+void orc_back_clean(or_tracks_view_t t, const uint8_t *toomany, int n_events, int n_threads);
+void orc_global(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, const uint8_t *toomany,
+                int n_events, int n_threads);
+/* all five stages in the reference launch order (online_reconstruction.cu:776-894) */
+void orc_run_all(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, int32_t *ntracklets,
+                 uint8_t *toomany, uint32_t *status, int n_events, int n_threads);
+
+/* orc_run_all plus candidate counters per event for the work accounting:
+ * counts[3e+0] XZ (pair2, pair3) candidates, [3e+1] YZ (u3,v3,u2,v2) combos,
+ * [3e+2] Global (x1, u1, v1) combos, in the reference's enumeration. */
+void orc_run_all_counted(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, int32_t *ntracklets,
+                         uint8_t *toomany, uint32_t *status, int64_t *counts, int n_events, int n_threads);
+
+/* Single-primitive entry points used by the known-answer tests. */
+void orc_fit_2d(int n, const float *x, const float *z, const float *w, float *par, float *err);
+void orc_fit_2d_drift(int n, const float *x, const float *drift, const short *sign, const float *z,
+                      const float *w, float *par, float *err);
+void orc_matinv_2x2(const float *a, float *ainv);
+int orc_reduce_plane(const float *slot, int n, int detid, short *hitflag);
+
+int orc_hardware_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

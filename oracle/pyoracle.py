@@ -1,0 +1,118 @@
+"""ctypes binding of the CPU oracle (or_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg as the checker.  The library path never imports
+this module.
+"""
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(REPO, "e1039-gpu_gb300"))
+from orgpu import layout as L  # noqa: E402
+
+LIB_PATH = os.path.join(HERE, "liborc.so")
+SOURCES = [os.path.join(HERE, "or_oracle.c")]
+
+ST_TOOMANY_ER, ST_TOOMANY_XZBIN, ST_TOOMANY_TKL = 1, 2, 4
+
+
+def build(force=False):
+    """Compile the oracle with one rounding per float operation."""
+    if not force and os.path.exists(LIB_PATH) and all(
+            os.path.getmtime(LIB_PATH) >= os.path.getmtime(s) for s in SOURCES + [
+                os.path.join(HERE, "or_oracle.h"), os.path.join(REPO, "include", "or_layout.h")]):
+        return LIB_PATH
+    cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+           "-pthread", "-o", LIB_PATH + ".tmp"] + SOURCES + ["-lm"]
+    subprocess.check_call(cmd)
+    os.replace(LIB_PATH + ".tmp", LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(LIB_PATH)
+        P = C.POINTER
+        _lib.orc_parse_geometry.argtypes = [C.c_char_p, P(L.OrPlane), C.c_void_p]
+        _lib.orc_event_reduce.argtypes = [L.OrHitsView, C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+        _lib.orc_xz.argtypes = [P(L.OrPlane), L.OrHitsView, L.OrTracksView, C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.c_int, C.c_int]
+        _lib.orc_yz.argtypes = [P(L.OrPlane), L.OrHitsView, L.OrTracksView, C.c_void_p, C.c_int, C.c_int]
+        _lib.orc_back_clean.argtypes = [L.OrTracksView, C.c_void_p, C.c_int, C.c_int]
+        _lib.orc_global.argtypes = [P(L.OrPlane), L.OrHitsView, L.OrTracksView, C.c_void_p, C.c_int, C.c_int]
+        _lib.orc_run_all.argtypes = [P(L.OrPlane), L.OrHitsView, L.OrTracksView, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_int, C.c_int]
+        _lib.orc_run_all_counted.argtypes = [P(L.OrPlane), L.OrHitsView, L.OrTracksView, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+        _lib.orc_fit_2d.argtypes = [C.c_int] + [C.c_void_p] * 5
+        _lib.orc_fit_2d_drift.argtypes = [C.c_int] + [C.c_void_p] * 7
+        _lib.orc_matinv_2x2.argtypes = [C.c_void_p, C.c_void_p]
+        _lib.orc_reduce_plane.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        _lib.orc_reduce_plane.restype = C.c_int
+        _lib.orc_hardware_threads.restype = C.c_int
+    return _lib
+
+
+def parse_geometry(path):
+    p = L.OrPlane()
+    wp = np.zeros(L.NDET * L.WIREPOS_STRIDE, np.float64)
+    rc = lib().orc_parse_geometry(path.encode(), C.byref(p), wp.ctypes.data)
+    if rc != 0:
+        raise OSError(f"oracle could not read geometry {path}")
+    return p, wp.reshape(L.NDET, L.WIREPOS_STRIDE)
+
+
+class OracleState:
+    """Per-event outputs of an oracle run, on top of HostHits/HostTracks."""
+
+    def __init__(self, n):
+        self.toomany = np.zeros(n, np.uint8)
+        self.status = np.zeros(n, np.uint32)
+        self.ntracklets = np.zeros(n, np.int32)
+        self.counts = np.zeros(3 * n, np.int64)
+
+
+def event_reduce(hits, state, n_threads=0):
+    lib().orc_event_reduce(hits.view(), state.toomany.ctypes.data, state.status.ctypes.data, hits.n, n_threads)
+
+
+def xz(plane, hits, tracks, state, n_threads=0):
+    lib().orc_xz(C.byref(plane), hits.view(), tracks.view(), state.ntracklets.ctypes.data,
+                 state.toomany.ctypes.data, state.status.ctypes.data, hits.n, n_threads)
+
+
+def yz(plane, hits, tracks, state, n_threads=0):
+    lib().orc_yz(C.byref(plane), hits.view(), tracks.view(), state.toomany.ctypes.data, hits.n, n_threads)
+
+
+def back_clean(tracks, state, n_threads=0):
+    lib().orc_back_clean(tracks.view(), state.toomany.ctypes.data, tracks.n, n_threads)
+
+
+def global_tracking(plane, hits, tracks, state, n_threads=0):
+    lib().orc_global(C.byref(plane), hits.view(), tracks.view(), state.toomany.ctypes.data, hits.n, n_threads)
+
+
+def run_all(plane, hits, tracks, state, n_threads=0, counted=False):
+    if counted:
+        lib().orc_run_all_counted(C.byref(plane), hits.view(), tracks.view(), state.ntracklets.ctypes.data,
+                                  state.toomany.ctypes.data, state.status.ctypes.data, state.counts.ctypes.data,
+                                  hits.n, n_threads)
+    else:
+        lib().orc_run_all(C.byref(plane), hits.view(), tracks.view(), state.ntracklets.ctypes.data,
+                          state.toomany.ctypes.data, state.status.ctypes.data, hits.n, n_threads)
+
+
+def hardware_threads():
+    return int(lib().orc_hardware_threads())

@@ -1,0 +1,107 @@
+"""Shared test helpers: seeded events, oracle stage snapshots, bitwise
+comparison of the reference-layout buffers over their valid regions."""
+import numpy as np
+
+from oracle import pyoracle as O
+from orgpu import layout as L
+from orgpu import synth as S
+
+
+def make_events(plane, wp, cfg):
+    geo = S.Geometry(plane, wp)
+    rec, off, truth = S.generate(geo, cfg)
+    rec, off = S.cap_records(rec, off)
+    hits = S.pack(rec, off, geo.wire_pos_f32())
+    return geo, rec, off, hits, truth
+
+
+def mixed_events(plane, wp, n_small=160, n_uneven=160, seed=7):
+    """Config-1 style events followed by uneven-occupancy ones, one batch."""
+    geo = S.Geometry(plane, wp)
+    r1, o1, _ = S.generate(geo, S.config_small(n_small, seed))
+    r2, o2, _ = S.generate(geo, S.config_uneven(n_uneven, seed + 1))
+    rec = np.concatenate([r1, r2])
+    off = np.concatenate([o1, o2[1:] + o1[-1]])
+    rec, off = S.cap_records(rec, off)
+    return geo, rec, off, S.pack(rec, off, geo.wire_pos_f32())
+
+
+class Snapshots:
+    """Oracle state after every stage, each a separate copy."""
+
+    def __init__(self, plane, hits0, n_threads=0):
+        n = hits0.n
+        self.hits0 = hits0
+        self.state = O.OracleState(n)
+        self.hits_er = hits0.copy()
+        O.event_reduce(self.hits_er, self.state, n_threads)
+        self.toomany_er = self.state.toomany.copy()
+        t = L.HostTracks(n)
+        O.xz(plane, self.hits_er, t, self.state, n_threads)
+        self.toomany_xz = self.state.toomany.copy()
+        self.ntracklets = self.state.ntracklets.copy()
+        self.tracks_xz = t.copy()
+        O.yz(plane, self.hits_er, t, self.state, n_threads)
+        self.tracks_yz = t.copy()
+        O.back_clean(t, self.state, n_threads)
+        self.tracks_clean = t.copy()
+        O.global_tracking(plane, self.hits_er, t, self.state, n_threads)
+        self.tracks_global = t
+
+
+def hit_mismatches(a, b, max_report=10):
+    """Events/planes whose counts or valid hit data differ bitwise."""
+    out = []
+    for name, per, stride, cap in (("cham", L.NCHAM, L.EVT_CHAM_FLOATS, L.MAXHITS_CHAM),
+                                   ("hodo", L.NHODO, L.EVT_HODO_FLOATS, L.MAXHITS_HODO),
+                                   ("prop", L.NPROP, L.EVT_PROP_FLOATS, L.MAXHITS_PROP)):
+        ca, cb = getattr(a, "nhits_" + name), getattr(b, "nhits_" + name)
+        da, db = getattr(a, "hits_" + name), getattr(b, "hits_" + name)
+        diff = np.nonzero(ca != cb)[0]
+        for k in diff[:max_report]:
+            out.append((name, int(k // per), int(k % per), "count", int(ca[k]), int(cb[k])))
+        for e in range(a.n):
+            for p in range(per):
+                n = int(ca[e * per + p])
+                if n != int(cb[e * per + p]):
+                    continue
+                base = e * stride + L.NHITSPARAM * cap * p
+                x = da[base:base + L.NHITSPARAM * n].view(np.uint32)
+                y = db[base:base + L.NHITSPARAM * n].view(np.uint32)
+                if not np.array_equal(x, y):
+                    out.append((name, e, p, "data"))
+                    if len(out) >= max_report:
+                        return out
+    return out
+
+
+def track_mismatches(a, b, toomany=None, max_report=10):
+    """(event, slot, k, first differing field) of track records that differ
+    bitwise; events flagged in `toomany` are skipped."""
+    out = []
+    na = a.ntracks.reshape(a.n, L.NSLOTS)
+    nb = b.ntracks.reshape(b.n, L.NSLOTS)
+    ta = a.tracks.reshape(a.n, L.NSLOTS, L.SLOTCAP, L.NTRKPARAM).view(np.uint32)
+    tb = b.tracks.reshape(b.n, L.NSLOTS, L.SLOTCAP, L.NTRKPARAM).view(np.uint32)
+    for e in range(a.n):
+        if toomany is not None and toomany[e]:
+            continue
+        if not np.array_equal(na[e], nb[e]):
+            out.append((e, -1, -1, "ntracks"))
+        else:
+            for s in range(L.NSLOTS):
+                k = int(na[e, s])
+                if k and not np.array_equal(ta[e, s, :k], tb[e, s, :k]):
+                    bad = np.nonzero(ta[e, s, :k] != tb[e, s, :k])
+                    out.append((e, s, int(bad[0][0]), int(bad[1][0])))
+        if len(out) >= max_report:
+            break
+    return out
+
+
+def count_tracks(t, stid):
+    n = 0
+    for e in range(t.n):
+        for s, k, r in t.records(e):
+            n += int(r[L.TRK_STID] == stid)
+    return n
