@@ -1,0 +1,337 @@
+"""Throughput of the online-reconstruction hot path on GB300.
+
+Workload: the uneven batch -- 100,000 seeded synthetic E906 events with 0-3
+muons (weights 0.2/0.3/0.4/0.1) and log-normal noise (median 300 hits,
+sigma 0.8, clipped at 3000).  One step = the whole plain path over the
+batch: device packer (compact hit records -> reference layout), event
+reducer, XZ, YZ, back-track cleaning, global tracking.
+
+  value   events/s with the records already in HBM (device-timed, CUDA events)
+  e2e     events/s through the C ABI with host buffers: pinned records H2D,
+          the path, track collection, count + tracks D2H, every step
+  roofline / cpu_baseline / clocks / gpu_launches as the JSON keys say.
+
+`--impl reference` times the reference's algorithm on the host cores (the CPU
+restatement, all threads) on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "e1039-gpu_gb300")
+for p in (REPO, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "events/s (plain path: event reducer + XZ/YZ tracklets + cleaning + global tracking)"
+UNIT = "events/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--events", type=int, default=100000)
+    ap.add_argument("--seed", type=int, default=906002)
+    ap.add_argument("--cpu-sample", type=int, default=0, help="events in the CPU-baseline sample (0 = auto)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def config_json(args, n):
+    return {"workload": "uneven batch: %d seeded synthetic E906 events, 0-3 muons (0.2/0.3/0.4/0.1), "
+                        "log-normal noise median 300 sigma 0.8 clip 3000" % n,
+            "events_per_gpu": n, "seed": args.seed, "geometry": "basic_geometry_e906",
+            "step": "pack + event reducer + XZ + YZ + back-track cleaning + global tracking",
+            "parallelism": "replicas only (events sharded, no collective)"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) > 8:
+                for k, nm in enumerate(names):
+                    if r[5 + k] == "Active":
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_cpu(plane, wp, rec, off, n, threads):
+    from oracle import pyoracle as O
+    from orgpu import layout as L, synth as S
+    geo = S.Geometry(plane, wp)
+    h = S.pack(rec[:off[n]], off[:n + 1], geo.wire_pos_f32())
+    t = L.HostTracks(n)
+    st = O.OracleState(n)
+    t0 = time.perf_counter()
+    O.run_all(plane, h, t, st, n_threads=threads)
+    dt = time.perf_counter() - t0
+    return dt, (threads if threads > 0 else O.hardware_threads())
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    import __graft_entry__
+    __graft_entry__.build()
+    from orgpu import GEOMETRY_E906, _lib, layout as L, synth as S
+
+    plane, wp = _lib.geometry_load(GEOMETRY_E906)
+    n = args.events
+    cfg = S.config_uneven(n, args.seed + 1000 * rank)
+    rec, off, truth = S.generate(S.Geometry(plane, wp), cfg)
+    rec, off = S.cap_records(rec, off)
+    cj = config_json(args, n)
+    cj["l2"] = "inputs larger than L2 (hit collections %.1f GB, records %.0f MB per step)" % (
+        L.EVT_CHAM_FLOATS * 4 * n / 1e9 * (1 + (L.EVT_HODO_FLOATS + L.EVT_PROP_FLOATS) / L.EVT_CHAM_FLOATS),
+        rec.nbytes / 1e6)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        # each step: the CPU restatement on a bounded sample, all host threads
+        ns = args.cpu_sample or min(n, 12000)
+        times = []
+        for i in range(args.warmup + args.steps):
+            dt, cores = run_cpu(plane, wp, rec, off, ns, 0)
+            if i >= args.warmup:
+                times.append(dt)
+        v = ns * len(times) / sum(times)
+        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cj,
+                "impl": "reference",
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                 "sample": "first %d events of the workload per step" % ns},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    from orgpu import pipeline
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    rc = pipeline.Reconstruction(plane, local)
+    b = pipeline.DeviceBatch(n, local)
+    stream = torch.cuda.current_stream(dev)
+    d_rec = torch.from_numpy(rec.view(np.uint8)).to(dev)
+    d_off = torch.from_numpy(off).to(dev)
+    d_wp = torch.from_numpy(wp.astype(np.float32).reshape(-1)).to(dev)
+    out_cap = max(1024, int(n * 3))
+    d_out = torch.empty(out_cap * L.COLLECT_STRIDE, dtype=torch.float32, device=dev)
+    d_cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+
+    stages = ["pack", "event_reduce", "xz", "yz", "back_clean", "global"]
+
+    def step(evs=None):
+        if evs is not None:
+            evs[0].record(stream)
+        rc.pack(b, d_rec, d_off, d_wp)
+        calls = [rc.event_reduce, rc.xz_tracking, rc.yz_tracking, rc.back_track_cleaning, rc.global_tracking]
+        if evs is not None:
+            evs[1].record(stream)
+        b.ntracklets.zero_()
+        for k, fn in enumerate(calls):
+            fn(b)
+            if evs is not None:
+                evs[2 + k].record(stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident throughput -----------------------------------------
+    for _ in range(args.warmup):
+        step()
+    rc.sync()
+    per_stage = {s: [] for s in stages}
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    all_evs = [[torch.cuda.Event(enable_timing=True) for _ in range(len(stages) + 1)] for _ in range(args.steps)]
+    t_start.record(stream)
+    for i in range(args.steps):
+        step(all_evs[i])
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    rc.sync()
+    ms = t_start.elapsed_time(t_end) / args.steps
+    for evs in all_evs:
+        for k, s in enumerate(stages):
+            per_stage[s].append(evs[k].elapsed_time(evs[k + 1]))
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms / 1000.0)
+    stage_ms = {s: statistics.mean(v) for s, v in per_stage.items()}
+
+    # results of the last step, for the roofline accounting
+    toomany = b.toomany.cpu().numpy()
+    cnt = {"cham": b.nhits_cham.cpu().numpy(), "hodo": b.nhits_hodo.cpu().numpy(),
+           "prop": b.nhits_prop.cpu().numpy()}
+
+    # ---- end to end through the C ABI with host buffers ---------------------
+    h_rec = torch.from_numpy(rec.view(np.uint8)).pin_memory()
+    h_off = torch.from_numpy(off).pin_memory()
+    h_cnt = torch.zeros(1, dtype=torch.int64).pin_memory()
+    h_out = torch.empty(out_cap * L.COLLECT_STRIDE, dtype=torch.float32).pin_memory()
+    h_flags = torch.empty(n, dtype=torch.uint8).pin_memory()
+    d2h_bytes = []
+
+    def e2e_step():
+        d_rec.copy_(h_rec, non_blocking=True)
+        d_off.copy_(h_off, non_blocking=True)
+        rc.pack(b, d_rec, d_off, d_wp)
+        rc.run_batch(b)
+        rc.collect(b, d_out, d_cnt, 6.0)
+        h_cnt.copy_(d_cnt, non_blocking=True)
+        h_flags.copy_(b.toomany, non_blocking=True)
+        stream.synchronize()
+        k = min(int(h_cnt.item()), out_cap)
+        h_out[:k * L.COLLECT_STRIDE].copy_(d_out[:k * L.COLLECT_STRIDE], non_blocking=True)
+        stream.synchronize()
+        d2h_bytes.append(8 + n + k * L.COLLECT_STRIDE * 4)
+        return k
+
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    d2h_bytes.clear()
+    e0.record(stream)
+    ntrk = 0
+    for _ in range(args.steps):
+        ntrk = e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    rc.sync()
+
+    if rank != 0:
+        return
+
+    # ---- roofline of the dominant kernel -------------------------------------
+    peaks = {}
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    # event reducer: algorithmic bytes = 20 B per raw hit read + 20 B per kept
+    # hit written + 48 counts read and written + the flag, per event
+    ev = np.repeat(np.arange(n), np.diff(off))
+    path_det = np.isin(rec["det"], np.array(L.PATH_PLANES))
+    raw = int(path_det.sum())
+    kept = int(cnt["cham"].reshape(n, L.NCHAM)[:, [d - 1 for d in L.EFF_DETID_CHAMBERS]].sum() +
+               cnt["hodo"].sum() + cnt["prop"].sum())
+    er_bytes = 20 * raw + 20 * kept + n * (48 * 8 + 1)
+    dominant = max(stage_ms, key=stage_ms.get)
+    er_gbs = er_bytes / (stage_ms["event_reduce"] / 1000.0) / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
+            traffic = json.load(f).get("event_reduce_bytes_per_event")
+            traffic = traffic * n if traffic else None
+    except (OSError, ValueError):
+        traffic = None
+    roofline = {"bound": "hbm", "kernel": "er_kernel (event reducer)", "achieved": er_gbs, "peak": hbm_peak,
+                "unit": "GB/s", "frac": er_gbs / hbm_peak, "traffic": traffic,
+                "peak_source": peak_src,
+                "algorithmic_bytes_per_launch": er_bytes,
+                "note": "dominant stage is %s (%.2f ms of %.2f ms); its bound is FP32/INT issue, not HBM or "
+                        "tensor -- see stage_ms and profiles/" % (dominant, stage_ms[dominant], ms)}
+
+    # ---- CPU baseline ---------------------------------------------------------
+    cpu = None
+    if not args.no_cpu_baseline:
+        ns = args.cpu_sample or min(n, 12000)
+        dt, cores = run_cpu(plane, wp, rec, off, ns, 0)
+        cpu = {"value": ns / dt, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "first %d events of the workload, one pass, all host threads" % ns}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no dataset)", "config": cj,
+            "e2e": {"value": world * n / (e2e_ms / 1000.0), "unit": UNIT, "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": int(rec.nbytes + off.nbytes),
+                    "d2h_bytes_per_step": int(statistics.mean(d2h_bytes)) if d2h_bytes else 0},
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": len(stages) * args.steps,
+            "stage_ms": stage_ms,
+            "events_rejected_frac": float(toomany.mean()), "global_tracks_last_step": ntrk}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

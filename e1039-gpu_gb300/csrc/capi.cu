@@ -18,6 +18,8 @@ cudaError_t launch_global(const or_plane_t *, or_hits_view_t, or_tracks_view_t, 
                           cudaStream_t, int);
 cudaError_t launch_pack(const or_hit_record_t *, const int64_t *, int, const float *, or_hits_view_t, cudaStream_t,
                         int);
+cudaError_t launch_collect(or_tracks_view_t, const uint8_t *, int, float, float *, long long, unsigned long long *,
+                           cudaStream_t);
 }  // namespace orgpu
 
 struct or_ctx {
@@ -256,6 +258,18 @@ int or_pack_hits(or_ctx_t *ctx, const or_hit_record_t *records, const int64_t *r
     cudaError_t e =
         orgpu::launch_pack(records, rec_offsets, n_events, wire_pos_f, hits, S(stream), ctx->sm_count);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "packer launch");
+}
+
+int or_collect_tracks(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, float stid,
+                      float *out, int64_t capacity, uint64_t *d_count, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany || !d_count || capacity < 0 || (capacity > 0 && !out))
+        return fail(OR_ERR_ARG, "bad collect arguments");
+    if ((rc = check_tracks(tracks))) return rc;
+    cudaError_t e = orgpu::launch_collect(tracks, toomany, n_events, stid, out, (long long)capacity,
+                                          reinterpret_cast<unsigned long long *>(d_count), S(stream));
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "collect launch");
 }
 
 }  // extern "C"

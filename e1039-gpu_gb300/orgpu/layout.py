@@ -20,6 +20,7 @@ SLOTCAP = TRKMAX // NSLOTS
 EVT_TRK_FLOATS = TRKMAX * NTRKPARAM
 WIREPOS_STRIDE = 400
 REF_EVTMAX = 10000
+COLLECT_STRIDE = NTRKPARAM + 2
 
 # track record field offsets (reconstruction_classes.cuh:558-635)
 TRK_STID, TRK_THREAD, TRK_NHITS, TRK_CHI2 = 0, 1, 2, 3

@@ -160,6 +160,14 @@ class Reconstruction:
                                           d_wire_pos_f.data_ptr(), b.hits_view(), self._stream(stream)),
                    "or_pack_hits")
 
+    def collect(self, b, d_out, d_count, stid=6.0, stream=None):
+        """Gather tracks with stationID == stid into d_out (float32 rows of
+        COLLECT_STRIDE); d_count (int64[1]) gets the number found."""
+        cap = d_out.numel() // L.COLLECT_STRIDE
+        _lib.check(self.lib.or_collect_tracks(self.ctx, b.tracks_view(), b.toomany.data_ptr(), b.n, float(stid),
+                                              d_out.data_ptr(), cap, d_count.data_ptr(), self._stream(stream)),
+                   "or_collect_tracks")
+
     def sync(self, stream=None):
         """Wait for the stream and raise on device-side error words."""
         _lib.check(self.lib.or_stream_sync(self.ctx, self._stream(stream)), "or_stream_sync")

@@ -84,19 +84,6 @@ class Geometry:
         return self.wire_pos.astype(np.float32)
 
 
-def _track_line(rng, q, invp):
-    """Piecewise-straight x(z) and straight y(z); returns callables' params."""
-    xv, yv = rng.normal(0.0, 0.3), rng.normal(0.0, 0.3)
-    tx23 = rng.uniform(-0.12, 0.12)
-    ty = rng.uniform(-0.05, 0.05)
-    k = invp * q
-    tx1 = tx23 + PT_KICK_KMAG * k
-    tx0 = tx1 + PT_KICK_FMAG * k
-    xf = xv + tx0 * (Z_FMAG_BEND - Z_TARGET)
-    xk = xf + tx1 * (Z_KMAG_BEND - Z_FMAG_BEND)
-    return (xv, yv, tx0, tx1, tx23, ty, xf, xk)
-
-
 def _xy_at(par, z):
     xv, yv, tx0, tx1, tx23, ty, xf, xk = par
     z = np.asarray(z, np.float64)
@@ -111,152 +98,166 @@ def _xy_at(par, z):
 _APERTURES = ((620.0, 48.0, 56.0), (1345.0, 112.0, 128.0), (1915.0, 155.0, 158.0), (2395.0, 178.0, 178.0))
 
 
-def _accepted(par):
-    xv, yv, tx0, tx1, tx23, ty, xf, xk = par
-    x0 = xk - tx23 * Z_KMAG_BEND
-    y0 = yv - ty * Z_TARGET
-    if not (abs(x0) < 140.0 and abs(tx23) < 0.14 and abs(y0) < 45.0 and abs(ty) < 0.09):
-        return False
-    for z, xl, yl in _APERTURES:
-        x, y = _xy_at(par, z)
-        if abs(float(x)) > xl or abs(float(y)) > yl:
-            return False
-    return True
+def _sample_tracks(rng, n, q, p_range):
+    """n accepted muon tracks of charge q (vectorised rejection sampling).
+    Returns a (8, n) array of _track_line parameters and invp."""
+    out = np.zeros((8, n))
+    invp = np.zeros(n)
+    todo = np.arange(n)
+    for _ in range(200):
+        if len(todo) == 0:
+            break
+        m = len(todo)
+        p = rng.uniform(p_range[0], p_range[1], m)
+        k = q[todo] / p
+        xv, yv = rng.normal(0.0, 0.3, m), rng.normal(0.0, 0.3, m)
+        tx23 = rng.uniform(-0.12, 0.12, m)
+        ty = rng.uniform(-0.05, 0.05, m)
+        tx1 = tx23 + PT_KICK_KMAG * k
+        tx0 = tx1 + PT_KICK_FMAG * k
+        xf = xv + tx0 * (Z_FMAG_BEND - Z_TARGET)
+        xk = xf + tx1 * (Z_KMAG_BEND - Z_FMAG_BEND)
+        par = np.stack([xv, yv, tx0, tx1, tx23, ty, xf, xk])
+        x0 = xk - tx23 * Z_KMAG_BEND
+        y0 = yv - ty * Z_TARGET
+        ok = (np.abs(x0) < 140.0) & (np.abs(tx23) < 0.14) & (np.abs(y0) < 45.0) & (np.abs(ty) < 0.09)
+        for z, xl, yl in _APERTURES:
+            x, y = _xy_at(par, z)
+            ok &= (np.abs(x) <= xl) & (np.abs(y) <= yl)
+        out[:, todo[ok]] = par[:, ok]
+        invp[todo[ok]] = 1.0 / p[ok]
+        todo = todo[~ok]
+    keep = np.ones(n, bool)
+    keep[todo] = False
+    return out, invp, keep
 
 
-def _signal_hits(geo, par, rng, eff, dsig):
-    """Hits of one track on the 48 planes: list of (det, elem, drift)."""
+def _plane_hits(geo, par, rng, eff, dsig, d):
+    """Hits of all tracks on plane d: (track index, element, drift)."""
     g = geo.g
-    out = []
-    for d in geo.planes:
-        if rng.random() > eff:
-            continue
-        z = g["z"][d]
-        x, y = _xy_at(par, z)
-        x, y = float(x), float(y)
-        n = int(geo.nelem[d])
+    z = g["z"][d]
+    x, y = _xy_at(par, z)
+    nt = x.shape[0]
+    ok = rng.random(nt) <= eff
+    ok &= (g["x1"][d] <= x) & (x <= g["x2"][d]) & (g["y1"][d] <= y) & (y <= g["y2"][d])
+    n = int(geo.nelem[d])
+    half = 0.5 * g["cellwidth"][d]
+    noise = rng.normal(0.0, dsig, nt)
+    if d <= L.NCHAM:
         dpx, dpy = g["deltapx"][d], g["deltapy"][d]
         ln = np.hypot(dpx, dpy)
-        # active area of the plane (x1..x2, y1..y2 columns of the geometry)
-        if not (g["x1"][d] <= x <= g["x2"][d] and g["y1"][d] <= y <= g["y2"][d]):
-            continue
-        half = 0.5 * g["cellwidth"][d]
-        if d <= L.NCHAM:
-            # drift chambers: nearest wire line; signed distance to wire 1 and
-            # the signed pitch
-            d1 = ((x - g["p1x_w1"][d]) * dpy - (y - g["p1y_w1"][d]) * dpx) / ln
-            pitch = (g["dp1x"][d] * dpy - g["dp1y"][d] * dpx) / ln
-            j = int(np.rint(d1 / pitch)) + 1
-            if j < 1 or j > n:
-                continue
-            dist = abs(d1 - (j - 1) * pitch)
-        elif d > L.NCHAM + L.NHODO:
-            # prop tubes: nearest tube by its packed position, which is what
-            # the reconstruction compares against
-            u = x * g["costheta"][d] + y * g["sintheta"][d]
-            wp = geo.wire_pos[d, 1:n + 1]
-            j = int(np.argmin(np.abs(wp - u))) + 1
-            dist = abs(wp[j - 1] - u)
-            if dist > half:
-                continue
-        if d <= L.NCHAM or d > L.NCHAM + L.NHODO:
-            drift = min(max(dist + rng.normal(0.0, dsig), 0.0), half)
-            out.append((int(d), j, float(drift)))
-        else:
-            # hodoscope paddle: measured coordinate along the plane's axis, and
-            # the paddle row's extent on the other axis
-            u = x * g["costheta"][d] + y * g["sintheta"][d]
+        d1 = ((x - g["p1x_w1"][d]) * dpy - (y - g["p1y_w1"][d]) * dpx) / ln
+        pitch = (g["dp1x"][d] * dpy - g["dp1y"][d] * dpx) / ln
+        j = np.rint(d1 / pitch).astype(np.int64) + 1
+        ok &= (j >= 1) & (j <= n)
+        dist = np.abs(d1 - (j - 1) * pitch)
+        drift = np.clip(dist + noise, 0.0, half)
+    else:
+        u = x * g["costheta"][d] + y * g["sintheta"][d]
+        wp = geo.wire_pos[d, 1:n + 1]
+        order = np.argsort(wp)
+        ws = wp[order]
+        pos = np.clip(np.searchsorted(ws, u), 1, n - 1)
+        left, right = ws[pos - 1], ws[pos]
+        pick = np.where(np.abs(u - left) <= np.abs(u - right), pos - 1, pos)
+        j = order[pick] + 1
+        dist = np.abs(wp[j - 1] - u)
+        if d <= L.NCHAM + L.NHODO:
             if abs(g["costheta"][d]) > 0.5:
                 lo, hi, other = g["y1"][d], g["y2"][d], y
             else:
                 lo, hi, other = g["x1"][d], g["x2"][d], x
-            if not (lo <= other <= hi):
-                continue
-            wp = geo.wire_pos[d, 1:n + 1]
-            j = int(np.argmin(np.abs(wp - u))) + 1
-            if abs(wp[j - 1] - u) > 0.5 * g["cellwidth"][d]:
-                continue
-            out.append((int(d), j, 0.0))
-    return out
+            ok = (rng.random(nt) <= eff) & (lo <= other) & (other <= hi) & (dist <= half)
+            drift = np.zeros(nt)
+        else:
+            ok &= dist <= half
+            drift = np.clip(dist + noise, 0.0, half)
+    idx = np.nonzero(ok)[0]
+    return idx, j[idx], drift[idx]
 
 
 def generate(geo, cfg):
-    """Generate cfg.n_events events.
+    """Generate cfg.n_events events (vectorised over tracks and noise hits).
 
     Returns (records, offsets, truth): records is a HIT_RECORD_DTYPE array
     sorted by (event, det, elem, tdc); offsets[e]..offsets[e+1] index event
-    e; truth is a dict of per-track arrays (event, charge, invp, x0, tx, y0,
-    ty) of the generated muons.
+    e; truth holds per-muon arrays (event, charge, invp, x0, tx, y0, ty).
     """
     rng = np.random.default_rng(cfg.seed)
     g = geo.g
-    planes = geo.planes
-    nel = geo.nelem[planes]
-    cum_el = np.cumsum(nel)
-    tot_el = int(cum_el[-1])
+    n_ev = cfg.n_events
     weights = np.asarray(cfg.track_weights, np.float64)
     weights = weights / weights.sum()
-
-    ev_chunks, off = [], [0]
-    truth = {k: [] for k in ("event", "charge", "invp", "x0", "tx", "y0", "ty")}
+    ntrk = rng.choice(len(weights), size=n_ev, p=weights)
+    tev = np.repeat(np.arange(n_ev), ntrk)
+    # alternate charges inside an event: +, -, +, ...
+    first = np.r_[0, np.cumsum(ntrk)[:-1]]
+    rank = np.arange(len(tev)) - np.repeat(first, ntrk)
+    q = np.where(rank % 2 == 0, 1.0, -1.0)
+    par, invp, keep = _sample_tracks(rng, len(tev), q, cfg.p_range)
+    par, invp, tev, q = par[:, keep], invp[keep], tev[keep], q[keep]
     ptype = np.array([L.plane_type(int(d)) for d in range(L.NDET)])
-    for e in range(cfg.n_events):
-        ntrk = int(rng.choice(len(weights), p=weights))
-        hits = []
-        for t in range(ntrk):
-            q = 1 if t % 2 == 0 else -1
-            for _ in range(200):
-                p = rng.uniform(*cfg.p_range)
-                par = _track_line(rng, q, 1.0 / p)
-                if _accepted(par):
-                    break
-            else:
-                continue
-            for d, j, dr in _signal_hits(geo, par, rng, cfg.efficiency, cfg.drift_sigma):
-                half = 0.5 * g["cellwidth"][d]
-                tlo, thi = _TDC_WIN[ptype[d]]
-                frac = dr / half if half > 0 else 0.0
-                tdc = thi - frac * (thi - tlo) + rng.normal(0.0, 1.0)
-                hits.append((d, j, tdc, dr, 2))
-            xv, yv, tx0, tx1, tx23, ty, xf, xk = par
-            truth["event"].append(e)
-            truth["charge"].append(q)
-            truth["invp"].append(1.0 / p)
-            truth["x0"].append(xk - tx23 * Z_KMAG_BEND)
-            truth["tx"].append(tx23)
-            truth["y0"].append(yv - ty * Z_TARGET)
-            truth["ty"].append(ty)
-        if cfg.noise == "poisson":
-            nn = int(rng.poisson(cfg.noise_mean))
-        else:
-            nn = int(np.rint(cfg.noise_mean * np.exp(rng.normal(0.0, cfg.noise_sigma))))
-            nn = min(nn, cfg.noise_clip)
-        if nn > 0:
-            flat = rng.integers(0, tot_el, nn)
-            pidx = np.searchsorted(cum_el, flat, side="right")
-            det = planes[pidx]
-            elem = flat - np.concatenate(([0], cum_el))[pidx] + 1
-            half = 0.5 * g["cellwidth"][det]
-            drift = np.where(ptype[det] == 1, 0.0, rng.uniform(0.0, 1.0, nn) * half)
-            win = np.array(_TDC_WIN)[ptype[det]]
-            tdc = rng.uniform(win[:, 0], win[:, 1])
-            flag = np.where(rng.random(nn) < cfg.out_of_time_frac, 1, 2)
-            hits.extend(zip(det.tolist(), elem.tolist(), tdc.tolist(), drift.tolist(), flag.tolist()))
-        if cfg.afterpulse_frac > 0 and hits:
-            nap = int(rng.binomial(len(hits), cfg.afterpulse_frac))
-            pick = rng.choice(len(hits), nap, replace=False)
-            for i in pick:
-                d, j, tdc, dr, fl = hits[i]
-                hits.append((d, j, tdc + rng.uniform(50.0, 200.0), dr, fl))
-        a = np.array(hits, dtype=[("det", "<i2"), ("elem", "<i2"), ("tdc", "<f4"), ("drift", "<f4"),
-                                  ("flag", "<i4")]) if hits else np.zeros(0, L.HIT_RECORD_DTYPE)
-        a = a.astype(L.HIT_RECORD_DTYPE)
-        a = a[np.lexsort((a["tdc"], a["elem"], a["det"]))]
-        ev_chunks.append(a)
-        off.append(off[-1] + len(a))
-    records = np.concatenate(ev_chunks) if ev_chunks else np.zeros(0, L.HIT_RECORD_DTYPE)
-    truth = {k: np.asarray(v) for k, v in truth.items()}
-    return records, np.asarray(off, np.int64), truth
+    win = np.array(_TDC_WIN)
+
+    dets, elems, drifts, evs, flags, tdcs = [], [], [], [], [], []
+    for d in geo.planes:
+        d = int(d)
+        idx, j, dr = _plane_hits(geo, par, rng, cfg.efficiency, cfg.drift_sigma, d)
+        half = 0.5 * g["cellwidth"][d]
+        tlo, thi = win[ptype[d]]
+        frac = dr / half if half > 0 else np.zeros_like(dr)
+        tdc = thi - frac * (thi - tlo) + rng.normal(0.0, 1.0, len(dr))
+        dets.append(np.full(len(idx), d)); elems.append(j); drifts.append(dr)
+        evs.append(tev[idx]); flags.append(np.full(len(idx), 2)); tdcs.append(tdc)
+    # noise, uniform over the (plane, element) pairs of the path's planes
+    if cfg.noise == "poisson":
+        nn = rng.poisson(cfg.noise_mean, n_ev)
+    else:
+        nn = np.rint(cfg.noise_mean * np.exp(rng.normal(0.0, cfg.noise_sigma, n_ev))).astype(np.int64)
+        nn = np.minimum(nn, cfg.noise_clip)
+    tot = int(nn.sum())
+    planes = geo.planes
+    cum_el = np.cumsum(geo.nelem[planes])
+    flat = rng.integers(0, int(cum_el[-1]), tot)
+    pidx = np.searchsorted(cum_el, flat, side="right")
+    det = planes[pidx]
+    dets.append(det)
+    elems.append(flat - np.concatenate(([0], cum_el))[pidx] + 1)
+    half = 0.5 * g["cellwidth"][det]
+    drifts.append(np.where(ptype[det] == 1, 0.0, rng.uniform(0.0, 1.0, tot) * half))
+    evs.append(np.repeat(np.arange(n_ev), nn))
+    flags.append(np.where(rng.random(tot) < cfg.out_of_time_frac, 1, 2))
+    tdcs.append(rng.uniform(win[ptype[det], 0], win[ptype[det], 1]))
+
+    det = np.concatenate(dets).astype(np.int16)
+    elem = np.concatenate(elems).astype(np.int16)
+    drift = np.concatenate(drifts).astype(np.float32)
+    ev = np.concatenate(evs).astype(np.int64)
+    flag = np.concatenate(flags).astype(np.int32)
+    tdc = np.concatenate(tdcs).astype(np.float32)
+    if cfg.afterpulse_frac > 0 and len(det):
+        pick = np.nonzero(rng.random(len(det)) < cfg.afterpulse_frac)[0]
+        det = np.r_[det, det[pick]]
+        elem = np.r_[elem, elem[pick]]
+        drift = np.r_[drift, drift[pick]]
+        ev = np.r_[ev, ev[pick]]
+        flag = np.r_[flag, flag[pick]]
+        tdc = np.r_[tdc, (tdc[pick] + rng.uniform(50.0, 200.0, len(pick))).astype(np.float32)]
+    # (event, det, elem, tdc) order with one integer radix sort: all tdc lie in
+    # [512, 4096), where the float bit pattern minus that of 512.0 is
+    # monotonic and fits 25 bits
+    assert len(tdc) == 0 or (tdc.min() >= 512.0 and tdc.max() < 4096.0)
+    tkey = tdc.view(np.int32).astype(np.int64) - int(np.float32(512.0).view(np.int32))
+    key = (ev << 39) | (det.astype(np.int64) << 33) | (elem.astype(np.int64) << 25) | tkey
+    order = np.argsort(key, kind="stable")
+    rec = np.zeros(len(order), L.HIT_RECORD_DTYPE)
+    rec["det"], rec["elem"], rec["tdc"] = det[order], elem[order], tdc[order]
+    rec["drift"], rec["flag"] = drift[order], flag[order]
+    offsets = np.concatenate(([0], np.cumsum(np.bincount(ev, minlength=n_ev)))).astype(np.int64)
+    xv, yv, tx0, tx1, tx23, ty, xf, xk = par
+    truth = {"event": tev, "charge": q.astype(np.int64), "invp": invp, "x0": xk - tx23 * Z_KMAG_BEND,
+             "tx": tx23, "y0": yv - ty * Z_TARGET, "ty": ty}
+    return rec, offsets, truth
 
 
 def cap_records(records, offsets):

@@ -106,6 +106,15 @@ size_t or_tracks_view_bytes(int n_events);
 int or_pack_hits(or_ctx_t *ctx, const or_hit_record_t *records, const int64_t *rec_offsets, int n_events,
                  const float *wire_pos_f, or_hits_view_t hits, void *stream);
 
+/* Gather the tracks whose stationID equals `stid` (6 = global tracks) into
+ * `out`, OR_COLLECT_STRIDE floats per row: [event, slot*16 + position,
+ * 148-float record].  *d_count (device, uint64) receives the number of
+ * matching tracks; rows past `capacity` are counted but not written.  Rows of
+ * different thread blocks come in no fixed order.  Replaces the host walk of
+ * the copied-back collections (online_reconstruction.cu:1023-1224). */
+int or_collect_tracks(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, float stid,
+                      float *out, int64_t capacity, uint64_t *d_count, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -61,6 +61,9 @@ extern "C" {
  * (online_reconstruction.cu:191) */
 #define OR_WIREPOS_STRIDE 400
 
+/* row of the track-collection output: [event, slot*16+position, record] */
+#define OR_COLLECT_STRIDE (OR_NTRKPARAM + 2)
+
 /* capacity of the reference's fixed structs (reconstruction_constants.h:20) */
 #define OR_REF_EVTMAX 10000
 

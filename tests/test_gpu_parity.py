@@ -123,3 +123,29 @@ def test_device_packer(setup):
     rc.pack(b, d_rec, d_off, d_wp)
     rc.sync()
     assert hit_mismatches(b.download_hits(), hits0) == []
+
+
+def test_collect_tracks(setup):
+    """The dense track output holds exactly the oracle's global tracks."""
+    import torch
+    from orgpu import layout as L, pipeline
+    plane, geo, rec, off, hits0, snap, rc = setup
+    b = _batch(rc, hits0.n, pipeline)
+    b.upload_hits(snap.hits_er)
+    b.toomany.copy_(torch.from_numpy(snap.state.toomany))
+    b.upload_tracks(snap.tracks_global)
+    out = torch.zeros(4096 * L.COLLECT_STRIDE, dtype=torch.float32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
+    rc.collect(b, out, cnt, 6.0)
+    rc.sync()
+    k = int(cnt.item())
+    rows = out[:k * L.COLLECT_STRIDE].cpu().numpy().reshape(k, L.COLLECT_STRIDE)
+    got = sorted((int(r[0]), int(r[1]), r[2:].tobytes()) for r in rows)
+    want = []
+    for e in range(hits0.n):
+        if snap.state.toomany[e]:
+            continue
+        for s, j, r in snap.tracks_global.records(e):
+            if r[L.TRK_STID] == 6:
+                want.append((e, s * L.SLOTCAP + j, r.tobytes()))
+    assert got == sorted(want)
