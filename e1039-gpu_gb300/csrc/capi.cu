@@ -11,8 +11,9 @@ namespace orgpu {
 cudaError_t launch_event_reduce(or_hits_view_t, uint8_t *, int, uint32_t *, cudaStream_t, int);
 cudaError_t launch_xz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, int32_t *, uint8_t *, int, cudaStream_t,
                       int);
-cudaError_t launch_yz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
-                      cudaStream_t, int);
+cudaError_t launch_yz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *, void *,
+                      int, int, int, cudaStream_t, int);
+size_t yz_scratch_bytes(int, int, int);
 cudaError_t launch_back_clean(or_tracks_view_t, const uint8_t *, int, cudaStream_t, int);
 cudaError_t launch_global(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
                           cudaStream_t, int);
@@ -28,6 +29,9 @@ struct or_ctx {
     or_plane_t *d_plane;
     bool has_geom;
     uint32_t *d_errw;
+    // YZ work queue: units of heavy tracklets, their best records, overflow arenas
+    void *yz_scratch;
+    int yz_cap_units, yz_cap_heavy, yz_garena_warps;
 };
 
 namespace {
@@ -106,6 +110,16 @@ int or_create(int device, or_ctx_t **out) {
         delete c;
         return fail(OR_ERR_NOMEM, "cudaMalloc error word");
     }
+    c->yz_cap_units = 1 << 20;
+    c->yz_cap_heavy = 1 << 18;
+    c->yz_garena_warps = c->sm_count * 16;
+    if ((e = cudaMalloc(&c->yz_scratch,
+                        orgpu::yz_scratch_bytes(c->yz_cap_units, c->yz_cap_heavy, c->yz_garena_warps))) != cudaSuccess) {
+        cudaFree(c->d_plane);
+        cudaFree(c->d_errw);
+        delete c;
+        return fail(OR_ERR_NOMEM, "cudaMalloc YZ work queue");
+    }
     *out = c;
     return OR_OK;
 }
@@ -115,6 +129,7 @@ int or_destroy(or_ctx_t *ctx) {
     cudaSetDevice(ctx->device);
     cudaFree(ctx->d_plane);
     cudaFree(ctx->d_errw);
+    cudaFree(ctx->yz_scratch);
     delete ctx;
     return OR_OK;
 }
@@ -172,8 +187,9 @@ int or_yz(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uin
     if (rc) return rc;
     if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
     if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
-    cudaError_t e =
-        orgpu::launch_yz(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw, S(stream), ctx->sm_count);
+    cudaError_t e = orgpu::launch_yz(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw, ctx->yz_scratch,
+                                     ctx->yz_cap_units, ctx->yz_cap_heavy, ctx->yz_garena_warps, S(stream),
+                                     ctx->sm_count);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "YZ launch");
 }
 

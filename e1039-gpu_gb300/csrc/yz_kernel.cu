@@ -13,32 +13,43 @@
 //     station 3+ the last v3' hit can pair with the first u2 hit
 //     (planes 19/18), whose resolution re-sets that sign whenever it
 //     succeeds (H:714-780);
-//   - the walk reads the scratch entry just past the hit count
-//     (H:725-735), which holds the last hit load attempted at that index.
-// Here lanes evaluate 32 (u3,v3,u2,v2) combinations at a time in the
-// reference order and recover both pieces of state with ballot/shuffle
-// scans carried across chunks, so the result equals the sequential loop.
-// One warp per event walks the 32 slots and their tracklets in order.
+//   - the left/right walk reads the scratch entry just past the hit count
+//     (H:725-735), which holds the last hit load attempted at that index --
+//     possibly by an earlier combination, (u3,v3) iteration or tracklet of
+//     the same slot.
+// Work per event is heavily skewed (a few events hold most combinations),
+// so the GPU version splits it:
+//   yz_plan_kernel   one warp per event walks its slots and tracklets in
+//                    order; builds each tracklet's hit windows once (y, error
+//                    and acceptance of every windowed hit for this tracklet);
+//                    evaluates light tracklets itself, and cuts heavy ones
+//                    into units of whole (u3,v3) iterations on a device queue;
+//   yz_work_kernel   persistent warps drain the queue;
+//   yz_apply_kernel  writes each heavy tracklet's best combination.
+// Inside a range, lanes evaluate 32 combinations at a time in the reference
+// order; ballot/shuffle scans recover the sign state and the scratch entry.
+// A unit starts with the scratch entries left by everything before it, which
+// depend only on which hit loads were attempted (not on any fit), so the plan
+// pass and each unit derive them without evaluating the earlier work.  The
+// best combination of a tracklet is the minimum of (chi2, combination index),
+// the reference's first-strictly-smaller rule.
 #include "window_pairs.cuh"
 
 namespace orgpu {
 
 constexpr int YZ_WARPS = 4;
-constexpr int YZ_PAIRCAP = 128;
+constexpr int YZ_MAXWIN = 100;          // windowed hits per plane (the reference's hitidx arrays)
+constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's hitpairs arrays)
+constexpr int YZ_ARENA_HITS = 224;      // windowed hits kept in shared memory per warp
+constexpr long YZ_LIGHT = 4096;         // combinations a planning warp evaluates itself per tracklet
+constexpr long YZ_EVENT_INLINE = 16384; // ... and per event
+constexpr long YZ_UNIT = 4096;          // combinations per queued unit (whole (u3,v3) iterations)
+constexpr int YZ_GARENA_HITS = 8 * YZ_MAXWIN;  // per-warp global overflow arena
 
-struct YzWarp {
-    short2 pairs[4][YZ_PAIRCAP];  // u2, v2, u3, v3
-    WindowScratch W;
-    float xdd[4], xres[4], xp1x[4], xp1y[4], xp1z[4], xdpx[4], xdpy[4], xdpz[4];
-    short xhs[4];
-    float b_chi2, b_ty, b_y0, b_ety, b_ey0;
-    int b_nuv;
-    float b_det[8], b_el[8], b_pos[8], b_drift[8], b_sign[8], b_tdc[8], b_res[12];
-};
-
-struct UvHit {
-    short det, el, sign;
-    float pos, drift, tdc, Y, eY, Z;
+struct YzHit {
+    float Y, eY, pos, drift, tdc;
+    short det, el;
+    int acc;  // calculate_y_uvhit accepted this hit for the tracklet
 };
 
 struct Stale {
@@ -46,8 +57,218 @@ struct Stale {
     float pos, drift;
 };
 
-// resolve_leftright_newhits walk over hits[0..n) with the scratch entry past
-// the end given by `st` (H:714-780), then the singles (H:785-804).
+// one queued unit: combinations [g0*C2, g1*C2) of heavy tracklet `heavy`
+struct YzUnit {
+    int heavy;
+    int g0, g1;
+    int pad;
+};
+// a heavy tracklet
+struct YzHeavy {
+    int e, slot, k;
+    int unit0, nunits;
+    Stale entry[4];
+};
+// best combination of one unit
+struct YzBest {
+    unsigned long long key;
+    int nuv;
+    float chi2, ty, y0, ety, ey0;
+    float det[8], el[8], pos[8], drift[8], sign[8], tdc[8], res[12];
+    int pad;
+};
+
+struct YzScratch {
+    YzUnit *units;
+    YzHeavy *heavy;
+    YzBest *best;
+    unsigned int *counters;  // [0] units reserved, [1] heavy reserved, [2] queue head
+    YzHit *garena;           // per-warp overflow arenas
+    int cap_units, cap_heavy, garena_warps;
+};
+
+struct PassEntryStore {
+    int c;
+    float y0, ty, ey0, ety, stpos, stdrift;
+    int stdet;
+};
+
+struct YzWarp {
+    YzHit arena[YZ_ARENA_HITS];
+    short2 pair[4][YZ_MAXPAIR];  // windowed indices (or -1) in sides 0, 1 of list q
+    short widx[8][YZ_MAXWIN];    // plane hit index of each windowed hit
+    uint8_t wfl[2][YZ_MAXWIN];
+    int np[4], nw[8], woff[8];
+    float x0, tx, ex0, etx;
+    int nhx;
+    float xdd[4], xres[4], xp1x[4], xp1y[4], xp1z[4], xdpx[4], xdpy[4], xdpz[4];
+    short xhs[4];
+    YzBest b;
+    PassEntryStore q[64];  // survivors of the first cut, in order
+};
+
+struct YzEvent {
+    HitPlane hc[8];
+    HitPlane p1y1, p1y2, p2y1, p2y2;
+    HitPlane hod[3][2];
+    short dl[8];
+};
+
+__device__ __forceinline__ void yz_event_planes(YzEvent &E, const or_hits_view_t &hv, long e, int st3) {
+    // u2 u2' v2 v2' u3 u3' v3 v3' (K:910-984)
+    const short dl[8] = {DET_U2, DET_UP2, DET_V2, DET_VP2, (short)det_u3(st3), (short)(det_u3(st3) - 1),
+                         (short)det_v3(st3), (short)(det_v3(st3) - 1)};
+    for (int k = 0; k < 8; ++k) {
+        E.dl[k] = dl[k];
+        E.hc[k] = hits_of(hv, e, dl[k]);
+    }
+    E.p1y1 = hits_of(hv, e, DET_P1Y1);
+    E.p1y2 = hits_of(hv, e, DET_P1Y2);
+    E.p2y1 = hits_of(hv, e, DET_P2Y1);
+    E.p2y2 = hits_of(hv, e, DET_P2Y2);
+    for (int q = 0; q < 3; ++q)
+        for (int c = 0; c < 2; ++c) E.hod[q][c] = hits_of(hv, e, c_hodoplanesx[q + 1][c]);
+}
+
+// Build the tracklet's windows (make_hitpairs_in_station, H:464-549) with the
+// per-hit y of this tracklet (calculate_y_uvhit, H:75-100).  Returns false
+// when a window or a pair list exceeds the reference's 100-entry arrays.
+__device__ bool yz_build(YzWarp &S, const YzEvent &E, const float *T, const or_plane_t &P, int st3,
+                         const YzHit *&base, YzHit *garena) {
+    const int lane = lane_id();
+    const float x0 = T[OR_TRK_X0], tx = T[OR_TRK_TX], ex0 = T[OR_TRK_ERR_X0], etx = T[OR_TRK_ERR_TX];
+    const int stid_of[4] = {2, 2, st3, st3}, proj_of[4] = {1, 2, 1, 2};
+    bool ok = true;
+    int total = 0;
+    // windowed hit lists, in plane order (H:480-511)
+    for (int q = 0; q < 4; ++q) {
+        const int a = 2 * q;
+        const float za = P.z[E.dl[a]], zb = P.z[E.dl[a + 1]];
+        const float sp = P.spacing[E.dl[a]];
+        const float xmin = fminf((tx - etx) * za, (tx - etx) * zb) + x0 - ex0 - sp;
+        const float xmax = fmaxf((tx + etx) * za, (tx + etx) * zb) + x0 + ex0 + sp;
+        for (int side = 0; side < 2; ++side) {
+            const HitPlane &h = E.hc[a + side];
+            const int det = E.dl[a + side];
+            int c = 0;
+            for (int b0 = 0; b0 < h.n; b0 += 32) {
+                const int i = b0 + lane;
+                const bool in = i < h.n && wp_in_window(det, h.chan(i), xmin, xmax, P);
+                const unsigned m = __ballot_sync(0xffffffffu, in);
+                if (in) {
+                    const int k = c + __popc(m & lanemask_lt());
+                    if (k < YZ_MAXWIN) S.widx[a + side][k] = (short)i;
+                }
+                c += __popc(m);
+            }
+            if (c > YZ_MAXWIN) ok = false;
+            c = min(c, YZ_MAXWIN);
+            if (lane == 0) {
+                S.nw[a + side] = c;
+                S.woff[a + side] = total;
+            }
+            total += c;
+        }
+    }
+    __syncwarp();
+    // pairs over each projection's two windowed lists (H:513-546)
+    for (int q = 0; q < 4; ++q) {
+        const int a = 2 * q;
+        const int c1 = S.nw[a], c2 = S.nw[a + 1];
+        for (int i = lane; i < c1; i += 32) S.wfl[0][i] = 0;
+        for (int i = lane; i < c2; i += 32) S.wfl[1][i] = 0;
+        __syncwarp();
+        const float spacing = c_spacingplane[c_detsuperid[stid_of[q]][proj_of[q]]];
+        int np = 0;
+        for (int b0 = 0; b0 < c1 * c2; b0 += 32) {
+            const int c = b0 + lane;
+            bool take = false;
+            short2 v = make_short2(0, 0);
+            if (c < c1 * c2) {
+                const int ia = c / c2, ib = c - ia * c2;
+                if (!(fabsf(E.hc[a].pos(S.widx[a][ia]) - E.hc[a + 1].pos(S.widx[a + 1][ib])) > spacing)) {
+                    take = true;
+                    v = make_short2((short)ia, (short)ib);
+                    S.wfl[0][ia] = 1;
+                    S.wfl[1][ib] = 1;
+                }
+            }
+            wp_append(take, v, S.pair[q], YZ_MAXPAIR, np);
+        }
+        __syncwarp();
+        for (int b0 = 0; b0 < c1; b0 += 32) {
+            const int ia = b0 + lane;
+            const bool take = ia < c1 && !S.wfl[0][ia];
+            wp_append(take, make_short2((short)ia, -1), S.pair[q], YZ_MAXPAIR, np);
+        }
+        for (int b0 = 0; b0 < c2; b0 += 32) {
+            const int ib = b0 + lane;
+            const bool take = ib < c2 && !S.wfl[1][ib];
+            wp_append(take, make_short2(-1, (short)ib), S.pair[q], YZ_MAXPAIR, np);
+        }
+        if (np > YZ_MAXPAIR) ok = false;
+        if (lane == 0) S.np[q] = min(np, YZ_MAXPAIR);
+        __syncwarp();
+    }
+    // windowed hit records (K:1326-1355 computes these per combination)
+    YzHit *dst = (total <= YZ_ARENA_HITS) ? S.arena : garena;
+    for (int l = 0; l < 8; ++l) {
+        const HitPlane &h = E.hc[l];
+        const int det = E.dl[l];
+        for (int i = lane; i < S.nw[l]; i += 32) {
+            const int hi = S.widx[l][i];
+            YzHit r;
+            r.det = (short)det;
+            r.el = (short)h.chan(hi);
+            r.tdc = h.tdc(hi);
+            r.drift = h.drift(hi);
+            r.pos = h.pos(hi);
+            float yy = 0.f, ey = 0.f;
+            r.acc = calculate_y_uvhit(det, r.el, r.drift, 0, x0, tx, P, yy, ey) ? 1 : 0;
+            r.Y = yy;
+            r.eY = ey;
+            dst[S.woff[l] + i] = r;
+        }
+    }
+    base = dst;
+    if (lane == 0) {
+        S.x0 = x0;
+        S.tx = tx;
+        S.ex0 = ex0;
+        S.etx = etx;
+    }
+    __syncwarp();
+    return ok;
+}
+
+// x hits of the tracklet (K:1300-1316)
+__device__ __forceinline__ void yz_xhits(YzWarp &S, const float *T, const or_plane_t &P) {
+    const int lane = lane_id();
+    const int nhx = min((int)T[OR_TRK_NHITS], 4);  // XZ tracklets carry 2-4 hits
+    if (lane < nhx) {
+        const short d = (short)T[OR_TRK_HIT_DETID + lane];
+        const short ch = (short)T[OR_TRK_HIT_CHAN + lane];
+        S.xdd[lane] = T[OR_TRK_HIT_DRIFT + lane];
+        S.xhs[lane] = (short)T[OR_TRK_HIT_SIGN + lane];
+        S.xres[lane] = P.resolution[d];
+        S.xp1x[lane] = x_bep(d, ch, P);
+        S.xp1y[lane] = y_bep(d, ch, P);
+        S.xp1z[lane] = z_bep(d, ch, P);
+        S.xdpx[lane] = P.deltapx[d];
+        S.xdpy[lane] = P.deltapy[d];
+        S.xdpz[lane] = P.deltapz[d];
+    }
+    if (lane == 0) S.nhx = nhx;
+    __syncwarp();
+}
+
+struct UvHit {
+    short det, el, sign;
+    float pos, drift, tdc, Y, eY, Z;
+};
+
+// resolve_leftright_newhits walk over h[0..n) with the scratch entry past the
+// end given by `st` (H:714-780), then the singles (H:785-804).
 __device__ __forceinline__ void walk_newhits(int n, UvHit *h, const Stale &st, float x0, float tx, float y0, float ty,
                                              float ex0, float etx, float ey0, float ety, const or_plane_t &P) {
     for (int i = 0; i < n;) {
@@ -91,9 +312,435 @@ __device__ __forceinline__ int cross_pair_index(int n3, const UvHit *h, int nuv)
     return -1;
 }
 
+__device__ __forceinline__ const YzHit *yz_list(const YzWarp &S, const YzHit *base, int l) { return base + S.woff[l]; }
+
+// Station-2 load attempts of the inner combination (iu2, iv2) in the
+// reference order (K:1467-1597): the scratch offsets they write (relative to
+// the station-3 count).
+struct S2Writes {
+    int n;
+    int off[4];
+    const YzHit *hit[4];
+};
+
+__device__ __forceinline__ S2Writes s2_writes(const YzWarp &S, const YzHit *base, int iu2, int iv2) {
+    S2Writes w;
+    w.n = 0;
+    const short2 pu = S.pair[0][iu2], pv = S.pair[1][iv2];
+    int acc = 0;
+    if (pu.x >= 0) { const YzHit *r = yz_list(S, base, 0) + pu.x; w.off[w.n] = acc; w.hit[w.n++] = r; acc += r->acc; }
+    if (pu.y >= 0) { const YzHit *r = yz_list(S, base, 1) + pu.y; w.off[w.n] = acc; w.hit[w.n++] = r; acc += r->acc; }
+    if (acc > 0) {
+        if (pv.x >= 0) { const YzHit *r = yz_list(S, base, 2) + pv.x; w.off[w.n] = acc; w.hit[w.n++] = r; acc += r->acc; }
+        if (pv.y >= 0) { const YzHit *r = yz_list(S, base, 3) + pv.y; w.off[w.n] = acc; w.hit[w.n++] = r; }
+    }
+    return w;
+}
+
+// accepted station-3 hits of the outer iteration (iu3, iv3)
+__device__ __forceinline__ int s3_count(const YzWarp &S, const YzHit *base, int iu3, int iv3, bool &valid) {
+    const short2 pu = S.pair[2][iu3], pv = S.pair[3][iv3];
+    int nu = 0, nv = 0;
+    if (pu.x >= 0) nu += yz_list(S, base, 4)[pu.x].acc;
+    if (pu.y >= 0) nu += yz_list(S, base, 5)[pu.y].acc;
+    if (nu > 0) {
+        if (pv.x >= 0) nv += yz_list(S, base, 6)[pv.x].acc;
+        if (pv.y >= 0) nv += yz_list(S, base, 7)[pv.y].acc;
+    }
+    valid = nu > 0 && nv > 0;
+    return nu + nv;
+}
+
+// Scratch entries 4..7 after outer iterations [0, g_end) of the current
+// tracklet, starting from `st` -- from the load pattern alone.
+__device__ void yz_advance_state(const YzWarp &S, const YzHit *base, int g_end, Stale st[4]) {
+    const int lane = lane_id();
+    const int nu2 = S.np[0], nu3 = S.np[2];
+    const int C2 = S.np[0] * S.np[1];
+    // last inner combination writing each offset m, and its hit
+    int lastc[4] = {-1, -1, -1, -1};
+    unsigned long long lasth[4] = {0, 0, 0, 0};
+    for (int b0 = 0; b0 < C2; b0 += 32) {
+        const int c = b0 + lane;
+        int mine[4] = {-1, -1, -1, -1};
+        unsigned long long mh[4] = {0, 0, 0, 0};
+        if (c < C2) {
+            const S2Writes w = s2_writes(S, base, c % nu2, c / nu2);
+            for (int k = 0; k < w.n; ++k) {
+                mine[w.off[k]] = c;
+                mh[w.off[k]] = (unsigned long long)w.hit[k];
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const int l = last_lane(__ballot_sync(0xffffffffu, mine[m] >= 0));
+            if (l >= 0) {
+                lastc[m] = __shfl_sync(0xffffffffu, mine[m], l);
+                lasth[m] = __shfl_sync(0xffffffffu, mh[m], l);
+            }
+        }
+    }
+    // the last valid outer iteration whose station-3 count maps an offset with
+    // a writer onto entry k
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        int bestm = -1;
+        for (int b0 = 0; b0 < g_end; b0 += 32) {
+            const int g = b0 + lane;
+            int m = -1;
+            if (g < g_end) {
+                bool valid;
+                const int n3 = s3_count(S, base, g % nu3, g / nu3, valid);
+                const int mm = k + 4 - n3;
+                if (valid && mm >= 0 && mm < 4 && lastc[mm] >= 0) m = mm;
+            }
+            const int l = last_lane(__ballot_sync(0xffffffffu, m >= 0));
+            if (l >= 0) bestm = __shfl_sync(0xffffffffu, m, l);
+        }
+        if (bestm >= 0) {
+            const YzHit *r = (const YzHit *)lasth[bestm];
+            st[k] = Stale{r->det, r->pos, r->drift};
+        }
+    }
+}
+
+// A combination that passed the first y cut, queued for the full evaluation:
+// index inside the tracklet, first fit, scratch entry past its hit count.
+using PassEntry = PassEntryStore;
+
+// Gather the accepted hits of combination c in the reference order
+// (K:1326-1597); returns nuv, sets n3.
+__device__ __forceinline__ int yz_gather(const YzWarp &S, const YzHit *base, int c, int C2, UvHit *h, int &n3,
+                                         const or_plane_t &P) {
+    const int iuv3 = c / C2, iuv2 = c - iuv3 * C2;
+    const int nu2 = S.np[0], nu3 = S.np[2];
+    const short2 pq[4] = {S.pair[2][iuv3 % nu3], S.pair[3][iuv3 / nu3], S.pair[0][iuv2 % nu2], S.pair[1][iuv2 / nu2]};
+    const int lists[8] = {4, 5, 6, 7, 0, 1, 2, 3};
+    int nuv = 0;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        if (a == 4) n3 = nuv;  // station-3 hits come first
+        const short2 p = pq[a >> 1];
+        const int wi = (a & 1) ? p.y : p.x;
+        if (wi < 0) continue;
+        const YzHit &r = yz_list(S, base, lists[a])[wi];
+        if (!r.acc) continue;
+        UvHit &u = h[nuv];
+        u.det = r.det;
+        u.el = r.el;
+        u.tdc = r.tdc;
+        u.sign = 0;
+        u.drift = r.drift;
+        u.pos = r.pos;
+        u.Z = P.z[r.det];
+        u.Y = r.Y;
+        u.eY = r.eY;
+        ++nuv;
+    }
+    return nuv;
+}
+
+// Evaluate combinations [c0, c1) (whole outer iterations) of the current
+// tracklet.  `st` is advanced to the scratch state after the range.  Returns
+// the best key (chi2 bits << 32 | combination index) or ~0, with that
+// combination's record in S.b.
+//
+// Phase 1 (every combination, registers only): station-3/2 load attempts in
+// the reference order, the first y fit, its 2-sigma cut (K:1602-1611) and the
+// scratch-entry scan.  Survivors (about 6% on the uneven batch) go to a
+// shared-memory queue in order.  Phase 2 (survivors, 32 at a time): sign
+// state, left/right walk, prop and hodoscope gates, chi2 (K:1613-1799).
+__device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l, long c1l, Stale st[4],
+                                       const or_plane_t &P) {
+    const int lane = lane_id();
+    const int nu2 = S.np[0], nu3 = S.np[2];
+    const int C2 = S.np[0] * S.np[1];
+    const int c0 = (int)c0l, c1 = (int)c1l;  // at most 100^4 combinations
+    const float x0 = S.x0, tx = S.tx, ex0 = S.ex0, etx = S.etx;
+    const int nhx = S.nhx;
+    unsigned long long best = ~0ull;
+    int cg = -1;
+    bool cg_hasf = false, cg_hascross = false;
+    short cg_sig[4] = {0, 0, 0, 0};
+    short cg_cross = 0;
+    int qn = 0;  // queued survivors
+
+    auto phase2 = [&](int n) {
+        // --- one chunk of survivors ------------------------------------------
+        const bool valid = lane < n;
+        PassEntry q;
+        if (valid) q = S.q[lane];
+        const int c = valid ? q.c : 0;
+        const int g = valid ? c / C2 : -1 - lane;
+        UvHit h[8];
+        int n3 = 0, nuv = 0;
+        if (valid) nuv = yz_gather(S, base, c, C2, h, n3, P);
+        const Stale stj{(short)(valid ? q.stdet : DET_SENTINEL), valid ? q.stpos : 0.f, valid ? q.stdrift : 0.f};
+        const float y0 = valid ? q.y0 : 0.f, ty = valid ? q.ty : 0.f;
+        const float ey0 = valid ? q.ey0 : 0.f, ety = valid ? q.ety : 0.f;
+        const unsigned seg = __match_any_sync(0xffffffffu, g);
+        const unsigned vm = __ballot_sync(0xffffffffu, valid);
+        const bool carried_f = (g == cg) && cg_hasf;
+        const int fl = __ffs(vm & seg) - 1;
+        const bool is_first = valid && !carried_f && fl == lane;
+        if (is_first) walk_newhits(nuv, h, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
+        short sig[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const short mine = (k < n3) ? h[k].sign : (short)0;
+            const short v = (short)__shfl_sync(0xffffffffu, (int)mine, fl < 0 ? 0 : fl);
+            sig[k] = carried_f ? cg_sig[k] : v;
+        }
+        bool xok = false;
+        short xval = 0;
+        if (valid && !is_first) {
+            const int xi = cross_pair_index(n3, h, nuv);
+            if (xi >= 0) {
+                const int k = lr_pair_newhits(x0, tx, y0, ty, ex0, etx, ey0, ety, h[xi].det, h[xi + 1].det, h[xi].pos,
+                                              h[xi].drift, h[xi + 1].pos, h[xi + 1].drift, P, 150.f);
+                if (k >= 0) {
+                    xok = true;
+                    xval = c_lrpossibility[k][0];
+                }
+            }
+        }
+        const unsigned xm = __ballot_sync(0xffffffffu, xok);
+        const int xs = last_lane(xm & seg & lanemask_lt());
+        const short xprev = (short)__shfl_sync(0xffffffffu, (int)xval, xs < 0 ? 0 : xs);
+        bool pass = false;
+        float chi2 = 0.f;
+        float resid[12];
+        if (valid && !is_first) {
+            for (int k = 0; k < n3 && k < 4; ++k) h[k].sign = sig[k];
+            if (n3 > 0) {
+                if (xs >= 0) h[n3 - 1].sign = xprev;
+                else if (g == cg && cg_hascross) h[n3 - 1].sign = cg_cross;
+            }
+            walk_newhits(nuv, h, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
+        }
+        if (valid) {
+            // the refit repeats the first fit exactly (same inputs); hard cut K:1638
+            pass = !(fabsf(y0) > Y0_MAX || fabsf(ty) > TY_MAX);
+            if (pass) {
+                const int nprop = prop_hits(E.p1y1, P.z[DET_P1Y1], E.p1y2, P.z[DET_P1Y2], 5.08f, y0, ty) +
+                                  prop_hits(E.p2y1, P.z[DET_P2Y1], E.p2y2, P.z[DET_P2Y2], 10.16f, y0, ty);
+                pass = nprop >= NPROP_MIN;
+            }
+            for (int qq = 0; qq < 3 && pass; ++qq) {
+                pass = match_tracklet_to_hodo(qq + 1, c_hodoplanesx[qq + 1][0], E.hod[qq][0], x0, y0, tx, ty, ex0, ey0,
+                                              etx, ety, P) ||
+                       match_tracklet_to_hodo(qq + 1, c_hodoplanesx[qq + 1][1], E.hod[qq][1], x0, y0, tx, ty, ex0, ey0,
+                                              etx, ety, P);
+            }
+            if (pass) {  // chi2_track, H:1182-1204
+                for (int m = 0; m < nhx; ++m) {
+                    resid[m] = residual_line(S.xp1x[m], S.xp1y[m], S.xp1z[m], S.xdpx[m], S.xdpy[m], S.xdpz[m],
+                                             S.xdd[m], S.xhs[m], x0, y0, tx, ty);
+                    chi2 += resid[m] * resid[m] / S.xres[m] / S.xres[m];
+                }
+                for (int k = 0; k < nuv; ++k) {
+                    const short d = h[k].det;
+                    const float r = residual_line(x_bep(d, h[k].el, P), y_bep(d, h[k].el, P), z_bep(d, h[k].el, P),
+                                                  P.deltapx[d], P.deltapy[d], P.deltapz[d], h[k].drift, h[k].sign, x0,
+                                                  y0, tx, ty);
+                    resid[nhx + k] = r;
+                    chi2 += r * r / P.resolution[d] / P.resolution[d];
+                }
+            }
+        }
+        // carry of the sign state to the next survivor chunk
+        {
+            const int last = last_lane(vm);
+            const int gl = __shfl_sync(0xffffffffu, g, last < 0 ? 0 : last);
+            const unsigned segl = __ballot_sync(0xffffffffu, valid && g == gl);
+            const int fnew = __ffs(__ballot_sync(0xffffffffu, is_first) & segl) - 1;
+            short ns[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) ns[k] = (short)__shfl_sync(0xffffffffu, (int)sig[k], fnew < 0 ? 0 : fnew);
+            const int xl = last_lane(xm & segl);
+            const short nx = (short)__shfl_sync(0xffffffffu, (int)xval, xl < 0 ? 0 : xl);
+            const bool cont = (gl == cg);
+            if (fnew >= 0) {
+                cg_hasf = true;
+                for (int k = 0; k < 4; ++k) cg_sig[k] = ns[k];
+            } else if (!cont) {
+                cg_hasf = false;
+            }
+            if (xl >= 0) {
+                cg_hascross = true;
+                cg_cross = nx;
+            } else if (!cont) {
+                cg_hascross = false;
+            }
+            cg = gl;
+        }
+        // best: min (chi2, index) over chi2 < 10000.1 (K:1778)
+        const bool elig = pass && chi2 < 10000.1f;
+        const unsigned key = elig ? __float_as_uint(chi2) : 0xffffffffu;
+        const unsigned kmin = __reduce_min_sync(0xffffffffu, key);
+        if (kmin != 0xffffffffu) {
+            const int win = __ffs(__ballot_sync(0xffffffffu, key == kmin)) - 1;
+            const int cw = __shfl_sync(0xffffffffu, c, win);
+            const unsigned long long full = ((unsigned long long)kmin << 32) | (unsigned long long)(unsigned)cw;
+            if (full < best) {
+                best = full;
+                if (lane == win) {
+                    S.b.key = full;
+                    S.b.nuv = nuv;
+                    S.b.chi2 = chi2;
+                    S.b.ty = ty;
+                    S.b.y0 = y0;
+                    S.b.ety = ety;
+                    S.b.ey0 = ey0;
+                    for (int n = 0; n < nuv; ++n) {
+                        S.b.det[n] = h[n].det;
+                        S.b.el[n] = h[n].el;
+                        S.b.pos[n] = h[n].pos;
+                        S.b.drift[n] = h[n].drift;
+                        S.b.sign[n] = h[n].sign;
+                        S.b.tdc[n] = h[n].tdc;
+                    }
+                    for (int n = 0; n < nhx + nuv; ++n) S.b.res[n] = resid[n];
+                }
+            }
+        }
+        __syncwarp();
+    };
+
+    const YzHit *Lh[8];
+#pragma unroll
+    for (int l = 0; l < 8; ++l) Lh[l] = yz_list(S, base, l);
+    for (int basec = c0; basec < c1; basec += 32) {
+        const int c = basec + lane;
+        const bool valid = c < c1;
+        int nuv = 0;
+        Stale own0{DET_SENTINEL, 0.f, 0.f}, own1 = own0, own2 = own0, own3 = own0;
+        unsigned wmask = 0u;
+        float y0 = 0.f, ty = 0.f, ey0 = 0.f, ety = 0.f;
+        bool pass1 = false;
+        if (valid) {
+            const int iuv3 = c / C2, iuv2 = c - iuv3 * C2;
+            const short2 pq[4] = {S.pair[2][iuv3 % nu3], S.pair[3][iuv3 / nu3], S.pair[0][iuv2 % nu2],
+                                  S.pair[1][iuv2 / nu2]};
+            Fit2 f;
+            // attempts in reference order: u3 a/b, v3 a/b, u2 a/b, v2 a/b
+            const int lists[8] = {4, 5, 6, 7, 0, 1, 2, 3};
+            int nbefore = 0;
+            bool alive = true;
+#pragma unroll
+            for (int a = 0; a < 8; ++a) {
+                if (a == 2 || a == 4 || a == 6) {
+                    // a u3 (v3, u2, v2) group must have given an accepted hit
+                    alive = alive && nuv > nbefore;
+                    nbefore = nuv;
+                }
+                if (!alive) break;
+                const short2 p = pq[a >> 1];
+                const int wi = (a & 1) ? p.y : p.x;
+                if (wi < 0) continue;
+                const YzHit &r = Lh[lists[a]][wi];
+                if (a >= 4) {  // station-2 attempts write the scratch entry nuv
+                    if (nuv == 4) { own0 = Stale{r.det, r.pos, r.drift}; wmask |= 1u; }
+                    else if (nuv == 5) { own1 = Stale{r.det, r.pos, r.drift}; wmask |= 2u; }
+                    else if (nuv == 6) { own2 = Stale{r.det, r.pos, r.drift}; wmask |= 4u; }
+                    else if (nuv == 7) { own3 = Stale{r.det, r.pos, r.drift}; wmask |= 8u; }
+                }
+                if (r.acc) {
+                    f.add(r.Y, P.z[r.det], r.eY);
+                    ++nuv;
+                }
+            }
+            const bool reached = alive && nuv > nbefore;  // the v2 group gave a hit
+            if (reached) {
+                f.solve(y0, ty, ey0, ety);
+                pass1 = !(fabsf(y0) > Y0_MAX + 2 * ey0 || fabsf(ty) > TY_MAX + 2 * ety);
+            }
+        }
+        // --- scratch entry past the hit count ----------------------------------
+        Stale stj{DET_SENTINEL, 0.f, 0.f};
+        {
+            const int j = nuv;
+            const unsigned lt = lanemask_lt();
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const Stale own = k == 0 ? own0 : (k == 1 ? own1 : (k == 2 ? own2 : own3));
+                const unsigned m = __ballot_sync(0xffffffffu, (wmask >> k) & 1u);
+                const int src = last_lane(m & lt);
+                const short sd = (short)__shfl_sync(0xffffffffu, (int)own.det, src < 0 ? 0 : src);
+                const float sp = __shfl_sync(0xffffffffu, own.pos, src < 0 ? 0 : src);
+                const float sdr = __shfl_sync(0xffffffffu, own.drift, src < 0 ? 0 : src);
+                if (j == k + 4) {
+                    if ((wmask >> k) & 1u) stj = own;
+                    else if (src >= 0) stj = Stale{sd, sp, sdr};
+                    else stj = st[k];
+                }
+                const int lw = last_lane(m);
+                const short cd = (short)__shfl_sync(0xffffffffu, (int)own.det, lw < 0 ? 0 : lw);
+                const float cp = __shfl_sync(0xffffffffu, own.pos, lw < 0 ? 0 : lw);
+                const float cdr = __shfl_sync(0xffffffffu, own.drift, lw < 0 ? 0 : lw);
+                if (lw >= 0) st[k] = Stale{cd, cp, cdr};
+            }
+        }
+        // --- queue the survivors in order --------------------------------------
+        const unsigned pm = __ballot_sync(0xffffffffu, pass1);
+        if (pass1) {
+            PassEntry e;
+            e.c = c;
+            e.y0 = y0;
+            e.ty = ty;
+            e.ey0 = ey0;
+            e.ety = ety;
+            e.stdet = stj.det;
+            e.stpos = stj.pos;
+            e.stdrift = stj.drift;
+            S.q[qn + __popc(pm & lanemask_lt())] = e;
+        }
+        qn += __popc(pm);
+        __syncwarp();
+        if (qn >= 32) {
+            phase2(32);
+            if (lane < qn - 32) S.q[lane] = S.q[32 + lane];
+            qn -= 32;
+            __syncwarp();
+        }
+    }
+    if (qn > 0) phase2(qn);
+    return best;
+}
+
+// write the best combination into the track record (K:1804-1825)
+__device__ __forceinline__ void yz_store(float *T, const YzBest &b, int nhx) {
+    const int lane = lane_id();
+    const int nuv = b.nuv;
+    if (lane == 0) {
+        T[OR_TRK_STID] = 5.f;
+        T[OR_TRK_NHITS] = (float)nhx + (float)nuv;
+        T[OR_TRK_CHI2] = b.chi2;
+        T[OR_TRK_TY] = b.ty;
+        T[OR_TRK_Y0] = b.y0;
+        T[OR_TRK_ERR_TY] = b.ety;
+        T[OR_TRK_ERR_Y0] = b.ey0;
+    }
+    if (lane < nuv) {
+        const int n = lane;
+        T[OR_TRK_HIT_DETID + nhx + n] = b.det[n];
+        T[OR_TRK_HIT_CHAN + nhx + n] = b.el[n];
+        T[OR_TRK_HIT_POS + nhx + n] = b.pos[n];
+        T[OR_TRK_HIT_DRIFT + nhx + n] = b.drift[n];
+        T[OR_TRK_HIT_SIGN + nhx + n] = b.sign[n];
+        T[OR_TRK_HIT_TDC + nhx + n] = b.tdc[n];
+        if (n < nhx) T[OR_TRK_HIT_RESID + n] = b.res[n];
+        T[OR_TRK_HIT_RESID + nhx + n] = b.res[nhx + n];
+    }
+}
+
+__device__ __forceinline__ YzHit *yz_garena(const YzScratch &sc, int gwarp) {
+    return sc.garena + (long)(gwarp % sc.garena_warps) * YZ_GARENA_HITS;
+}
+
 __global__ void __launch_bounds__(YZ_WARPS * 32)
-    yz_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
-              const uint8_t *__restrict__ toomany, int n_events, uint32_t *__restrict__ errw) {
+    yz_plan_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
+                   const uint8_t *__restrict__ toomany, int n_events, YzScratch sc, uint32_t *__restrict__ errw) {
     extern __shared__ __align__(16) unsigned char yz_smem[];
     or_plane_t &P = *reinterpret_cast<or_plane_t *>(yz_smem);
     YzWarp *warps = reinterpret_cast<YzWarp *>(yz_smem + ((sizeof(or_plane_t) + 15) & ~size_t(15)));
@@ -102,323 +749,79 @@ __global__ void __launch_bounds__(YZ_WARPS * 32)
     const int w = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     YzWarp &S = warps[w];
+    YzHit *garena = yz_garena(sc, blockIdx.x * YZ_WARPS + w);
 
     for (long e = (long)blockIdx.x * YZ_WARPS + w; e < n_events; e += (long)gridDim.x * YZ_WARPS) {
         if (toomany[e]) continue;  // K:873-878
-        const HitPlane p1y1 = hits_of(hv, e, DET_P1Y1), p1y2 = hits_of(hv, e, DET_P1Y2);
-        const HitPlane p2y1 = hits_of(hv, e, DET_P2Y1), p2y2 = hits_of(hv, e, DET_P2Y2);
-        HitPlane hod[3][2];
-        for (int q = 0; q < 3; ++q)
-            for (int c = 0; c < 2; ++c) hod[q][c] = hits_of(hv, e, c_hodoplanesx[q + 1][c]);
-
+        long budget = YZ_EVENT_INLINE;
         for (int slot = 0; slot < OR_NSLOTS; ++slot) {
             const int ntr = min((int)tv.ntracks[e * OR_NSLOTS + slot], OR_SLOTCAP);
             if (ntr == 0) continue;
             const int st3 = 3 + (slot & 1);  // K:884
-            // u2 u2' v2 v2' u3 u3' v3 v3' (K:910-984)
-            const short dl[8] = {DET_U2, DET_UP2, DET_V2, DET_VP2, (short)det_u3(st3), (short)(det_u3(st3) - 1),
-                                 (short)det_v3(st3), (short)(det_v3(st3) - 1)};
-            HitPlane hc[8];
-            for (int k = 0; k < 8; ++k) hc[k] = hits_of(hv, e, dl[k]);
-            // scratch entries 4..7 as last written in this slot (sentinel start)
-            Stale carry_st[4];
-            for (int k = 0; k < 4; ++k) carry_st[k] = Stale{DET_SENTINEL, 0.f, 0.f};
-
+            YzEvent E;
+            yz_event_planes(E, hv, e, st3);
+            Stale st[4];
+            for (int k = 0; k < 4; ++k) st[k] = Stale{DET_SENTINEL, 0.f, 0.f};
             for (int it = 0; it < ntr; ++it) {
                 float *T = trk_rec(tv, e, slot, it);
-                const float x0 = T[OR_TRK_X0], tx = T[OR_TRK_TX], ex0 = T[OR_TRK_ERR_X0], etx = T[OR_TRK_ERR_TX];
-                const int nhx = min((int)T[OR_TRK_NHITS], 4);  // XZ tracklets carry 2-4 hits
-                // windowed pairs (K:1249-1283)
-                int np[4];
-                const int stid_of[4] = {2, 2, st3, st3}, proj_of[4] = {1, 2, 1, 2};
-                bool overcap = false;
-                for (int q = 0; q < 4; ++q) {
-                    const int a = 2 * q;
-                    const float za = P.z[dl[a]], zb = P.z[dl[a + 1]];
-                    const float sp = P.spacing[dl[a]];
-                    const float xmin = fminf((tx - etx) * za, (tx - etx) * zb) + x0 - ex0 - sp;
-                    const float xmax = fmaxf((tx + etx) * za, (tx + etx) * zb) + x0 + ex0 + sp;
-                    const float spacing = c_spacingplane[c_detsuperid[stid_of[q]][proj_of[q]]];
-                    np[q] = window_pairs(hc[a], dl[a], hc[a + 1], dl[a + 1], spacing, xmin, xmax, P, S.pairs[q],
-                                         YZ_PAIRCAP, S.W);
-                    overcap |= np[q] > YZ_PAIRCAP;
-                }
+                const YzHit *base;
+                const bool fits = yz_build(S, E, T, P, st3, base, garena);
                 if (lane == 0) T[OR_TRK_STID] = 3.f;  // K:1285
-                const int nu2 = np[0], nv2 = np[1], nu3 = np[2], nv3 = np[3];
-                if (overcap) {
+                if (!fits) {
                     if (lane == 0) atomicOr(errw, ERRW_CAPACITY);
                     continue;
                 }
+                const int nu2 = S.np[0], nv2 = S.np[1], nu3 = S.np[2], nv3 = S.np[3];
                 if (nu2 == 0 || nu3 == 0 || nv2 == 0 || nv3 == 0) continue;
-                // x hits of the tracklet (K:1300-1316)
-                if (lane < nhx && lane < 4) {
-                    const short d = (short)T[OR_TRK_HIT_DETID + lane];
-                    const short ch = (short)T[OR_TRK_HIT_CHAN + lane];
-                    S.xdd[lane] = T[OR_TRK_HIT_DRIFT + lane];
-                    S.xhs[lane] = (short)T[OR_TRK_HIT_SIGN + lane];
-                    S.xres[lane] = P.resolution[d];
-                    S.xp1x[lane] = x_bep(d, ch, P);
-                    S.xp1y[lane] = y_bep(d, ch, P);
-                    S.xp1z[lane] = z_bep(d, ch, P);
-                    S.xdpx[lane] = P.deltapx[d];
-                    S.xdpy[lane] = P.deltapy[d];
-                    S.xdpz[lane] = P.deltapz[d];
-                }
-                __syncwarp();
-                const int C2 = nu2 * nv2;
-                const long C = (long)nu3 * nv3 * C2;
-                float run_min = 10000.1f;
-                bool update = false;
-                // sign-state carry of the current (u3,v3) iteration
-                long cg = -1;
-                bool cg_hasf = false, cg_hascross = false;
-                short cg_sig[4] = {0, 0, 0, 0};
-                short cg_cross = 0;
-
-                for (long base = 0; base < C; base += 32) {
-                    const long c = base + lane;
-                    const bool valid = c < C;
-                    const long g = valid ? c / C2 : -1 - (long)lane;
-                    UvHit h[8];
-                    int nuv = 0, n3 = 0;
-                    bool v3ok = false, v2ok = false;
-                    Stale own[4];
-                    unsigned wmask = 0u;
-                    float y0 = 0.f, ty = 0.f, ey0 = 0.f, ety = 0.f;
-                    bool pass1 = false;
-                    if (valid) {
-                        const int iuv3 = (int)(c / C2), iuv2 = (int)(c - (long)iuv3 * C2);
-                        const int iu3 = iuv3 % nu3, iv3 = iuv3 / nu3;
-                        const int iu2 = iuv2 % nu2, iv2 = iuv2 / nu2;
-                        const short2 pu3 = S.pairs[2][iu3], pv3 = S.pairs[3][iv3];
-                        const short2 pu2 = S.pairs[0][iu2], pv2 = S.pairs[1][iv2];
-                        // one load attempt (K:1326-1355); S2 attempts are recorded
-                        // for the scratch-entry scan
-                        auto attempt = [&](int lk, int hidx, bool record) {
-                            UvHit &u = h[nuv];
-                            u.det = dl[lk];
-                            u.el = (short)hc[lk].chan(hidx);
-                            u.tdc = hc[lk].tdc(hidx);
-                            u.sign = 0;
-                            u.drift = hc[lk].drift(hidx);
-                            u.pos = hc[lk].pos(hidx);
-                            u.Z = P.z[dl[lk]];
-                            if (record && nuv >= 4 && nuv < 8) {
-                                own[nuv - 4] = Stale{u.det, u.pos, u.drift};
-                                wmask |= 1u << (nuv - 4);
-                            }
-                            float yy, ey;
-                            if (calculate_y_uvhit(u.det, u.el, u.drift, 0, x0, tx, P, yy, ey)) {
-                                u.Y = yy;
-                                u.eY = ey;
-                                ++nuv;
-                            }
-                        };
-                        if (pu3.x >= 0) attempt(4, pu3.x, false);
-                        if (pu3.y >= 0) attempt(5, pu3.y, false);
-                        const int nhu3 = nuv;
-                        if (nhu3 > 0) {
-                            if (pv3.x >= 0) attempt(6, pv3.x, false);
-                            if (pv3.y >= 0) attempt(7, pv3.y, false);
-                            v3ok = nuv > nhu3;
-                        }
-                        n3 = nuv;
-                        if (v3ok) {
-                            if (pu2.x >= 0) attempt(0, pu2.x, true);
-                            if (pu2.y >= 0) attempt(1, pu2.y, true);
-                            if (nuv > n3) {
-                                const int nb = nuv;
-                                if (pv2.x >= 0) attempt(2, pv2.x, true);
-                                if (pv2.y >= 0) attempt(3, pv2.y, true);
-                                v2ok = nuv > nb;
-                            }
-                        }
-                        if (v2ok) {  // K:1602-1611
-                            Fit2 f;
-                            for (int k = 0; k < nuv; ++k) f.add(h[k].Y, h[k].Z, h[k].eY);
-                            f.solve(y0, ty, ey0, ety);
-                            pass1 = !(fabsf(y0) > Y0_MAX + 2 * ey0 || fabsf(ty) > TY_MAX + 2 * ety);
-                        }
-                    }
-                    // --- scratch entry past the hit count -----------------------
-                    Stale st{DET_SENTINEL, 0.f, 0.f};
-                    {
-                        const int j = nuv;
-                        const unsigned lt = lanemask_lt();
-#pragma unroll
-                        for (int k = 0; k < 4; ++k) {
-                            const unsigned m = __ballot_sync(0xffffffffu, (wmask >> k) & 1u);
-                            const int src = last_lane(m & lt);
-                            const short sd = (short)__shfl_sync(0xffffffffu, (int)own[k].det, src < 0 ? 0 : src);
-                            const float sp = __shfl_sync(0xffffffffu, own[k].pos, src < 0 ? 0 : src);
-                            const float sdr = __shfl_sync(0xffffffffu, own[k].drift, src < 0 ? 0 : src);
-                            if (j == k + 4) {
-                                if ((wmask >> k) & 1u) st = own[k];
-                                else if (src >= 0) st = Stale{sd, sp, sdr};
-                                else st = carry_st[k];
-                            }
-                            const int lw = last_lane(m);
-                            const short cd = (short)__shfl_sync(0xffffffffu, (int)own[k].det, lw < 0 ? 0 : lw);
-                            const float cp = __shfl_sync(0xffffffffu, own[k].pos, lw < 0 ? 0 : lw);
-                            const float cdr = __shfl_sync(0xffffffffu, own[k].drift, lw < 0 ? 0 : lw);
-                            if (lw >= 0) carry_st[k] = Stale{cd, cp, cdr};
-                        }
-                    }
-                    // --- station-3 sign state --------------------------------------
-                    const unsigned seg = __match_any_sync(0xffffffffu, (unsigned long long)g);
-                    const unsigned pm = __ballot_sync(0xffffffffu, pass1);
-                    const bool carried_f = (g == cg) && cg_hasf;
-                    const int fl = __ffs(pm & seg) - 1;
-                    const bool is_first = pass1 && !carried_f && fl == lane;
-                    // the first passing combination resolves from zero signs
-                    if (is_first) walk_newhits(nuv, h, st, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
-                    // its station-3 signs, to every lane of the same iteration
-                    short sig[4];
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const short mine = (k < n3) ? h[k].sign : (short)0;
-                        const short v = (short)__shfl_sync(0xffffffffu, (int)mine, fl < 0 ? 0 : fl);
-                        sig[k] = carried_f ? cg_sig[k] : v;
-                    }
-                    // cross pair (last station-3 hit, first station-2 hit)
-                    int xi = -1;
-                    short xval = 0;
-                    bool xok = false;
-                    if (pass1 && !is_first) {
-                        xi = cross_pair_index(n3, h, nuv);
-                        if (xi >= 0) {
-                            const int k = lr_pair_newhits(x0, tx, y0, ty, ex0, etx, ey0, ety, h[xi].det,
-                                                          h[xi + 1].det, h[xi].pos, h[xi].drift, h[xi + 1].pos,
-                                                          h[xi + 1].drift, P, 150.f);
-                            if (k >= 0) {
-                                xok = true;
-                                xval = c_lrpossibility[k][0];
-                            }
-                        }
-                    }
-                    const unsigned xm = __ballot_sync(0xffffffffu, xok);
-                    const int xs = last_lane(xm & seg & lanemask_lt());
-                    const short xprev = (short)__shfl_sync(0xffffffffu, (int)xval, xs < 0 ? 0 : xs);
-                    bool pass = false;
-                    float chi2 = 0.f;
-                    float resid[12];
-                    if (pass1 && !is_first) {
-                        // station-3 signs at the start of this combination
-                        for (int k = 0; k < n3 && k < 4; ++k) h[k].sign = sig[k];
-                        if (n3 > 0) {
-                            const int last3 = n3 - 1;
-                            if (xs >= 0) h[last3].sign = xprev;
-                            else if (g == cg && cg_hascross) h[last3].sign = cg_cross;
-                        }
-                        walk_newhits(nuv, h, st, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
-                    }
-                    if (pass1) {
-                        // refit gives the same y0/ty (same inputs); hard cut, K:1638
-                        pass = !(fabsf(y0) > Y0_MAX || fabsf(ty) > TY_MAX);
-                        if (pass) {
-                            const int nprop = prop_hits(p1y1, P.z[DET_P1Y1], p1y2, P.z[DET_P1Y2], 5.08f, y0, ty) +
-                                              prop_hits(p2y1, P.z[DET_P2Y1], p2y2, P.z[DET_P2Y2], 10.16f, y0, ty);
-                            pass = nprop >= NPROP_MIN;
-                        }
-                        for (int q = 0; q < 3 && pass; ++q) {
-                            pass = match_tracklet_to_hodo(q + 1, c_hodoplanesx[q + 1][0], hod[q][0], x0, y0, tx, ty,
-                                                          ex0, ey0, etx, ety, P) ||
-                                   match_tracklet_to_hodo(q + 1, c_hodoplanesx[q + 1][1], hod[q][1], x0, y0, tx, ty,
-                                                          ex0, ey0, etx, ety, P);
-                        }
-                        if (pass) {  // chi2_track, H:1182-1204
-                            for (int m = 0; m < nhx; ++m) {
-                                resid[m] = residual_line(S.xp1x[m], S.xp1y[m], S.xp1z[m], S.xdpx[m], S.xdpy[m],
-                                                         S.xdpz[m], S.xdd[m], S.xhs[m], x0, y0, tx, ty);
-                                chi2 += resid[m] * resid[m] / S.xres[m] / S.xres[m];
-                            }
-                            for (int k = 0; k < nuv; ++k) {
-                                const short d = h[k].det;
-                                const float r = residual_line(x_bep(d, h[k].el, P), y_bep(d, h[k].el, P),
-                                                              z_bep(d, h[k].el, P), P.deltapx[d], P.deltapy[d],
-                                                              P.deltapz[d], h[k].drift, h[k].sign, x0, y0, tx, ty);
-                                resid[nhx + k] = r;
-                                chi2 += r * r / P.resolution[d] / P.resolution[d];
-                            }
-                        }
-                    }
-                    // --- carry of the sign state to the next chunk -----------------
-                    {
-                        const int last = last_lane(__ballot_sync(0xffffffffu, valid));
-                        const long gl = __shfl_sync(0xffffffffu, g, last < 0 ? 0 : last);
-                        const unsigned segl = __ballot_sync(0xffffffffu, valid && g == gl);
-                        const int fnew = __ffs(__ballot_sync(0xffffffffu, is_first) & segl) - 1;
-                        short ns[4];
-#pragma unroll
-                        for (int k = 0; k < 4; ++k) ns[k] = (short)__shfl_sync(0xffffffffu, (int)sig[k], fnew < 0 ? 0 : fnew);
-                        const int xl = last_lane(xm & segl);
-                        const short nx = (short)__shfl_sync(0xffffffffu, (int)xval, xl < 0 ? 0 : xl);
-                        const bool cont = (gl == cg);
-                        if (fnew >= 0) {
-                            cg_hasf = true;
-                            for (int k = 0; k < 4; ++k) cg_sig[k] = ns[k];
-                        } else if (!cont) {
-                            cg_hasf = false;
-                        }
-                        if (xl >= 0) {
-                            cg_hascross = true;
-                            cg_cross = nx;
-                        } else if (!cont) {
-                            cg_hascross = false;
-                        }
-                        cg = gl;
-                    }
-                    // --- best chi2, strict < in combination order (K:1778) ----------
-                    const bool elig = pass && chi2 < run_min;
-                    const unsigned key = elig ? __float_as_uint(chi2) : 0xffffffffu;
-                    const unsigned kmin = __reduce_min_sync(0xffffffffu, key);
-                    if (kmin != 0xffffffffu) {
-                        const int win = __ffs(__ballot_sync(0xffffffffu, key == kmin)) - 1;
-                        if (lane == win) {
-                            S.b_nuv = nuv;
-                            S.b_chi2 = chi2;
-                            S.b_ty = ty;
-                            S.b_y0 = y0;
-                            S.b_ety = ety;
-                            S.b_ey0 = ey0;
-                            for (int n = 0; n < nuv; ++n) {
-                                S.b_det[n] = h[n].det;
-                                S.b_el[n] = h[n].el;
-                                S.b_pos[n] = h[n].pos;
-                                S.b_drift[n] = h[n].drift;
-                                S.b_sign[n] = h[n].sign;
-                                S.b_tdc[n] = h[n].tdc;
-                            }
-                            for (int n = 0; n < nhx + nuv; ++n) S.b_res[n] = resid[n];
-                        }
-                        run_min = __uint_as_float(kmin);
-                        update = true;
-                        __syncwarp();
-                    }
-                }
-                if (update) {  // K:1804-1825
-                    __syncwarp();
-                    const int nuv = S.b_nuv;
+                yz_xhits(S, T, P);
+                const long C2 = (long)nu2 * nv2;
+                const long G = (long)nu3 * nv3;
+                const long C = G * C2;
+                bool inline_it = C <= YZ_LIGHT && C <= budget;
+                if (!inline_it) {
+                    // whole outer iterations per unit
+                    const long gper = max(1L, YZ_UNIT / C2);
+                    const int nunits = (int)((G + gper - 1) / gper);
+                    int hid = 0, u0 = 0;
                     if (lane == 0) {
-                        T[OR_TRK_STID] = 5.f;
-                        T[OR_TRK_NHITS] = (float)nhx + (float)nuv;
-                        T[OR_TRK_CHI2] = S.b_chi2;
-                        T[OR_TRK_TY] = S.b_ty;
-                        T[OR_TRK_Y0] = S.b_y0;
-                        T[OR_TRK_ERR_TY] = S.b_ety;
-                        T[OR_TRK_ERR_Y0] = S.b_ey0;
+                        hid = (int)atomicAdd(&sc.counters[1], 1u);
+                        u0 = (int)atomicAdd(&sc.counters[0], (unsigned)nunits);
                     }
-                    if (lane < nuv) {
-                        const int n = lane;
-                        T[OR_TRK_HIT_DETID + nhx + n] = S.b_det[n];
-                        T[OR_TRK_HIT_CHAN + nhx + n] = S.b_el[n];
-                        T[OR_TRK_HIT_POS + nhx + n] = S.b_pos[n];
-                        T[OR_TRK_HIT_DRIFT + nhx + n] = S.b_drift[n];
-                        T[OR_TRK_HIT_SIGN + nhx + n] = S.b_sign[n];
-                        T[OR_TRK_HIT_TDC + nhx + n] = S.b_tdc[n];
-                        if (n < nhx) T[OR_TRK_HIT_RESID + n] = S.b_res[n];
-                        T[OR_TRK_HIT_RESID + nhx + n] = S.b_res[nhx + n];
+                    hid = __shfl_sync(0xffffffffu, hid, 0);
+                    u0 = __shfl_sync(0xffffffffu, u0, 0);
+                    if (hid >= sc.cap_heavy || (long)u0 + nunits > sc.cap_units) {
+                        // no room on the queue: evaluate here; void the reserved units
+                        for (int u = lane; u < nunits; u += 32)
+                            if (u0 + u < sc.cap_units) sc.units[u0 + u].heavy = -1;
+                        if (lane == 0 && hid < sc.cap_heavy) sc.heavy[hid].nunits = 0;
+                        inline_it = true;
+                    } else {
+                        if (lane == 0) {
+                            YzHeavy hv2;
+                            hv2.e = (int)e;
+                            hv2.slot = slot;
+                            hv2.k = it;
+                            hv2.unit0 = u0;
+                            hv2.nunits = nunits;
+                            for (int k = 0; k < 4; ++k) hv2.entry[k] = st[k];
+                            sc.heavy[hid] = hv2;
+                        }
+                        for (int u = lane; u < nunits; u += 32) {
+                            YzUnit un;
+                            un.heavy = hid;
+                            un.g0 = (int)(u * gper);
+                            un.g1 = (int)min(G, (u + 1) * gper);
+                            un.pad = 0;
+                            sc.units[u0 + u] = un;
+                        }
+                        yz_advance_state(S, base, (int)G, st);
                     }
+                }
+                if (inline_it) {
+                    budget -= C;
+                    const unsigned long long bk = yz_range(S, E, base, 0, C, st, P);
+                    __syncwarp();
+                    if (bk != ~0ull) yz_store(T, S.b, S.nhx);
                 }
                 __syncwarp();
             }
@@ -426,18 +829,127 @@ __global__ void __launch_bounds__(YZ_WARPS * 32)
     }
 }
 
+// persistent warps drain the unit queue
+__global__ void __launch_bounds__(YZ_WARPS * 32)
+    yz_work_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv, YzScratch sc) {
+    extern __shared__ __align__(16) unsigned char yz_smem[];
+    or_plane_t &P = *reinterpret_cast<or_plane_t *>(yz_smem);
+    YzWarp *warps = reinterpret_cast<YzWarp *>(yz_smem + ((sizeof(or_plane_t) + 15) & ~size_t(15)));
+    load_plane_smem(&P, gplane);
+    __syncthreads();
+    const int w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    YzWarp &S = warps[w];
+    YzHit *garena = yz_garena(sc, blockIdx.x * YZ_WARPS + w);
+    const int nunits = min((int)sc.counters[0], sc.cap_units);
+    for (;;) {
+        int u = 0;
+        if (lane == 0) u = (int)atomicAdd(&sc.counters[2], 1u);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= nunits) break;
+        const YzUnit un = sc.units[u];
+        if (un.heavy < 0) continue;
+        const YzHeavy hv2 = sc.heavy[un.heavy];
+        const float *T = trk_rec(tv, hv2.e, hv2.slot, hv2.k);
+        const int st3 = 3 + (hv2.slot & 1);
+        YzEvent E;
+        yz_event_planes(E, hv, hv2.e, st3);
+        const YzHit *base;
+        yz_build(S, E, T, P, st3, base, garena);
+        yz_xhits(S, T, P);
+        Stale st[4];
+        for (int k = 0; k < 4; ++k) st[k] = hv2.entry[k];
+        yz_advance_state(S, base, un.g0, st);
+        const long C2 = (long)S.np[0] * S.np[1];
+        const unsigned long long bk = yz_range(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P);
+        __syncwarp();
+        YzBest *dst = sc.best + u;
+        if (bk == ~0ull) {
+            if (lane == 0) dst->key = ~0ull;
+        } else {
+            const unsigned *src = reinterpret_cast<const unsigned *>(&S.b);
+            unsigned *d = reinterpret_cast<unsigned *>(dst);
+            for (int i = lane; i < (int)(sizeof(YzBest) / 4); i += 32) d[i] = src[i];
+        }
+        __syncwarp();
+    }
+}
+
+// one warp per heavy tracklet: its units' minimum key wins
+__global__ void __launch_bounds__(128) yz_apply_kernel(or_tracks_view_t tv, YzScratch sc) {
+    const int lane = threadIdx.x & 31;
+    const int nheavy = min((int)sc.counters[1], sc.cap_heavy);
+    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < nheavy; h += (gridDim.x * blockDim.x) >> 5) {
+        const YzHeavy hv2 = sc.heavy[h];
+        if (hv2.nunits <= 0 || (long)hv2.unit0 + hv2.nunits > sc.cap_units) continue;
+        unsigned long long best = ~0ull;
+        int bu = -1;
+        for (int u = lane; u < hv2.nunits; u += 32) {
+            const unsigned long long k = sc.best[hv2.unit0 + u].key;
+            if (k < best) {
+                best = k;
+                bu = hv2.unit0 + u;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long ok = __shfl_xor_sync(0xffffffffu, best, o);
+            const int ou = __shfl_xor_sync(0xffffffffu, bu, o);
+            if (ok < best) {
+                best = ok;
+                bu = ou;
+            }
+        }
+        if (best == ~0ull) continue;
+        float *T = trk_rec(tv, hv2.e, hv2.slot, hv2.k);
+        const int nhx = min((int)T[OR_TRK_NHITS], 4);
+        yz_store(T, sc.best[bu], nhx);
+    }
+}
+
 size_t yz_smem_bytes() { return ((sizeof(or_plane_t) + 15) & ~size_t(15)) + sizeof(YzWarp) * YZ_WARPS; }
 
+// Scratch the YZ stage needs: queue of units, per-unit best records, heavy
+// tracklets, per-warp overflow arenas.
+size_t yz_scratch_bytes(int cap_units, int cap_heavy, int garena_warps) {
+    size_t b = 256 + (sizeof(YzUnit) + sizeof(YzBest)) * (size_t)cap_units + sizeof(YzHeavy) * (size_t)cap_heavy;
+    b = (b + 255) & ~size_t(255);
+    return b + sizeof(YzHit) * YZ_GARENA_HITS * (size_t)garena_warps;
+}
+
 cudaError_t launch_yz(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, const uint8_t *toomany,
-                      int n_events, uint32_t *errw, cudaStream_t stream, int sm_count) {
+                      int n_events, uint32_t *errw, void *scratch, int cap_units, int cap_heavy, int garena_warps,
+                      cudaStream_t stream, int sm_count) {
     if (n_events <= 0) return cudaSuccess;
     const size_t smem = yz_smem_bytes();
-    cudaError_t err = cudaFuncSetAttribute(yz_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (err != cudaSuccess) return err;
-    long blocks = (n_events + YZ_WARPS - 1) / YZ_WARPS;
-    const long cap = (long)sm_count * 8;
-    if (blocks > cap) blocks = cap;
-    yz_kernel<<<(unsigned)blocks, YZ_WARPS * 32, smem, stream>>>(d_plane, hv, tv, toomany, n_events, errw);
+    cudaError_t err;
+    if ((err = cudaFuncSetAttribute(yz_plan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+        return err;
+    if ((err = cudaFuncSetAttribute(yz_work_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+        return err;
+    char *p = static_cast<char *>(scratch);
+    YzScratch sc;
+    sc.counters = reinterpret_cast<unsigned int *>(p);
+    p += 256;
+    sc.units = reinterpret_cast<YzUnit *>(p);
+    p += sizeof(YzUnit) * (size_t)cap_units;
+    sc.best = reinterpret_cast<YzBest *>(p);
+    p += sizeof(YzBest) * (size_t)cap_units;
+    sc.heavy = reinterpret_cast<YzHeavy *>(p);
+    p += sizeof(YzHeavy) * (size_t)cap_heavy;
+    p = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
+    sc.garena = reinterpret_cast<YzHit *>(p);
+    sc.cap_units = cap_units;
+    sc.cap_heavy = cap_heavy;
+    sc.garena_warps = garena_warps;
+    if ((err = cudaMemsetAsync(sc.counters, 0, 256, stream))) return err;
+    const long blocks = garena_warps / YZ_WARPS;
+    const long blocks_plan = min((long)(n_events + YZ_WARPS - 1) / YZ_WARPS, blocks);
+    yz_plan_kernel<<<(unsigned)blocks_plan, YZ_WARPS * 32, smem, stream>>>(d_plane, hv, tv, toomany, n_events, sc,
+                                                                           errw);
+    if ((err = cudaGetLastError())) return err;
+    yz_work_kernel<<<(unsigned)blocks, YZ_WARPS * 32, smem, stream>>>(d_plane, hv, tv, sc);
+    if ((err = cudaGetLastError())) return err;
+    yz_apply_kernel<<<(unsigned)(sm_count * 4), 128, 0, stream>>>(tv, sc);
     return cudaGetLastError();
 }
 

@@ -1233,7 +1233,9 @@ static void yz_event(const or_plane_t *P, or_hits_view_t hv, or_tracks_view_t tv
                     float par[2], perr[2];
                     orc_fit_2d(nuv, Y, Z, errY, par, perr); /* K:1602-1611 */
                     float y0 = par[0], ty = par[1], err_y0 = perr[0], err_ty = perr[1];
+                    if (cnt) cnt[3]++;
                     if (fabsf(y0) > Y0_MAX + 2 * err_y0 || fabsf(ty) > TY_MAX + 2 * err_ty) continue;
+                    if (cnt) cnt[4]++;
                     resolve_leftright_newhits(x0, tx, y0, ty, err_x0, err_tx, err_y0, err_ty, nuv, detID, pos, drift,
                                               sign, P, 150.f);
                     resolve_single_leftright_newhits(x0, tx, y0, ty, nuv, detID, pos, sign, P);
@@ -1294,6 +1296,7 @@ static void yz_event(const or_plane_t *P, or_hits_view_t hv, or_tracks_view_t tv
                         ok = m;
                     }
                     if (!ok) continue;
+                    if (cnt) cnt[5]++;
                     float chi2 = chi2_track(nhits_x + nuv, residuals, dd, hs, res, p1x, p1y, p1z, dpx, dpy, dpz, x0,
                                             y0, tx, ty); /* K:1773 */
                     if (chi2 < chi2min) {              /* K:1778-1799 */
@@ -1707,7 +1710,7 @@ static void *worker(void *arg) {
         for (int q = 0; q < 4; q++) ps->pairs[q] = alloc_pairs();
     }
     for (long e = j->e0; e < j->e1; e++) {
-        int64_t *c = j->counts ? j->counts + 3 * e : NULL;
+        int64_t *c = j->counts ? j->counts + ORC_NCOUNTS * e : NULL;
         switch (j->stage) {
         case ST_ER: er_event(j->h, e, j->toomany, j->status); break;
         case ST_XZ: xz_event(j->P, j->h, j->t, e, j->ntkl, j->toomany, j->status, xs, c); break;
@@ -1791,6 +1794,6 @@ void orc_run_all(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, int3
 }
 void orc_run_all_counted(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, int32_t *ntracklets,
                          uint8_t *toomany, uint32_t *status, int64_t *counts, int n_events, int n_threads) {
-    for (long e = 0; e < 3L * n_events; e++) counts[e] = 0;
+    for (long e = 0; e < (long)ORC_NCOUNTS * n_events; e++) counts[e] = 0;
     run_stage(ST_ALL, p, h, t, ntracklets, toomany, status, counts, n_events, n_threads);
 }

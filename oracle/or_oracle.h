@@ -51,9 +51,12 @@ void orc_global(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, const
 void orc_run_all(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, int32_t *ntracklets,
                  uint8_t *toomany, uint32_t *status, int n_events, int n_threads);
 
-/* orc_run_all plus candidate counters per event for the work accounting:
- * counts[3e+0] XZ (pair2, pair3) candidates, [3e+1] YZ (u3,v3,u2,v2) combos,
- * [3e+2] Global (x1, u1, v1) combos, in the reference's enumeration. */
+/* orc_run_all plus work counters per event (ORC_NCOUNTS each), in the
+ * reference's enumeration: [0] XZ (pair2, pair3) candidates, [1] YZ
+ * (u3,v3,u2,v2) combinations, [2] Global (x1,u1,v1) combinations, [3] YZ
+ * combinations reaching the first y fit, [4] passing its 2-sigma cut,
+ * [5] passing every gate up to the chi2. */
+#define ORC_NCOUNTS 6
 void orc_run_all_counted(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, int32_t *ntracklets,
                          uint8_t *toomany, uint32_t *status, int64_t *counts, int n_events, int n_threads);
 

@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(HERE, "liborc.so")
 SOURCES = [os.path.join(HERE, "or_oracle.c")]
 
 ST_TOOMANY_ER, ST_TOOMANY_XZBIN, ST_TOOMANY_TKL = 1, 2, 4
+NCOUNTS = 6
 
 
 def build(force=False):
@@ -80,7 +81,7 @@ class OracleState:
         self.toomany = np.zeros(n, np.uint8)
         self.status = np.zeros(n, np.uint32)
         self.ntracklets = np.zeros(n, np.int32)
-        self.counts = np.zeros(3 * n, np.int64)
+        self.counts = np.zeros(NCOUNTS * n, np.int64)
 
 
 def event_reduce(hits, state, n_threads=0):
