@@ -57,17 +57,18 @@ struct Stale {
     float pos, drift;
 };
 
-// one queued unit: combinations [g0*C2, g1*C2) of heavy tracklet `heavy`
+// one queued unit: combinations [g0*C2, g1*C2) of heavy tracklet `heavy`,
+// with the scratch entries 4..7 as they stand when the unit starts
 struct YzUnit {
     int heavy;
     int g0, g1;
     int pad;
+    Stale entry[4];
 };
 // a heavy tracklet
 struct YzHeavy {
     int e, slot, k;
     int unit0, nunits;
-    Stale entry[4];
 };
 // best combination of one unit
 struct YzBest {
@@ -351,9 +352,14 @@ __device__ __forceinline__ int s3_count(const YzWarp &S, const YzHit *base, int 
     return nu + nv;
 }
 
-// Scratch entries 4..7 after outer iterations [0, g_end) of the current
-// tracklet, starting from `st` -- from the load pattern alone.
-__device__ void yz_advance_state(const YzWarp &S, const YzHit *base, int g_end, Stale st[4]) {
+// Walk the outer iterations of the current tracklet in order and track the
+// scratch entries 4..7 from the load pattern alone (no fits): entry k is set
+// by the last inner combination writing offset k-4+... of the last valid
+// outer iteration that reaches it.  When `units` is given, the state at the
+// start of every unit (each `gper` outer iterations) is stored there.  `st`
+// goes in as the state before the tracklet and comes out as the state after.
+__device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gper, Stale st[4], YzUnit *units,
+                               int heavy) {
     const int lane = lane_id();
     const int nu2 = S.np[0], nu3 = S.np[2];
     const int C2 = S.np[0] * S.np[1];
@@ -380,28 +386,48 @@ __device__ void yz_advance_state(const YzWarp &S, const YzHit *base, int g_end, 
             }
         }
     }
-    // the last valid outer iteration whose station-3 count maps an offset with
-    // a writer onto entry k
+    const Stale st_in[4] = {st[0], st[1], st[2], st[3]};
+    int carry[4] = {-1, -1, -1, -1};  // offset m last mapped onto entry k, -1 = unchanged
+    auto resolve = [&](int k, int m) -> Stale {
+        if (m < 0) return st_in[k];
+        const YzHit *r = (const YzHit *)lasth[m];
+        return Stale{r->det, r->pos, r->drift};
+    };
+    for (int b0 = 0; b0 < G; b0 += 32) {
+        const int g = b0 + lane;
+        int mk[4] = {-1, -1, -1, -1};
+        if (g < G) {
+            bool valid;
+            const int n3 = s3_count(S, base, g % nu3, g / nu3, valid);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        int bestm = -1;
-        for (int b0 = 0; b0 < g_end; b0 += 32) {
-            const int g = b0 + lane;
-            int m = -1;
-            if (g < g_end) {
-                bool valid;
-                const int n3 = s3_count(S, base, g % nu3, g / nu3, valid);
+            for (int k = 0; k < 4; ++k) {
                 const int mm = k + 4 - n3;
-                if (valid && mm >= 0 && mm < 4 && lastc[mm] >= 0) m = mm;
+                if (valid && mm >= 0 && mm < 4 && lastc[mm] >= 0) mk[k] = mm;
             }
-            const int l = last_lane(__ballot_sync(0xffffffffu, m >= 0));
-            if (l >= 0) bestm = __shfl_sync(0xffffffffu, m, l);
         }
-        if (bestm >= 0) {
-            const YzHit *r = (const YzHit *)lasth[bestm];
-            st[k] = Stale{r->det, r->pos, r->drift};
+        const bool ustart = units && g < G && (g % gper) == 0;
+        Stale ent[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const unsigned wm = __ballot_sync(0xffffffffu, mk[k] >= 0);
+            const int src = last_lane(wm & lanemask_lt());
+            const int msrc = __shfl_sync(0xffffffffu, mk[k], src < 0 ? 0 : src);
+            ent[k] = resolve(k, src >= 0 ? msrc : carry[k]);
+            const int l = last_lane(wm);
+            if (l >= 0) carry[k] = __shfl_sync(0xffffffffu, mk[k], l);
+        }
+        if (ustart) {
+            YzUnit &u = units[g / gper];
+            u.heavy = heavy;
+            u.g0 = g;
+            u.g1 = min(G, g + gper);
+            u.pad = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) u.entry[k] = ent[k];
         }
     }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) st[k] = resolve(k, carry[k]);
 }
 
 // A combination that passed the first y cut, queued for the full evaluation:
@@ -803,18 +829,9 @@ __global__ void __launch_bounds__(YZ_WARPS * 32)
                             hv2.k = it;
                             hv2.unit0 = u0;
                             hv2.nunits = nunits;
-                            for (int k = 0; k < 4; ++k) hv2.entry[k] = st[k];
                             sc.heavy[hid] = hv2;
                         }
-                        for (int u = lane; u < nunits; u += 32) {
-                            YzUnit un;
-                            un.heavy = hid;
-                            un.g0 = (int)(u * gper);
-                            un.g1 = (int)min(G, (u + 1) * gper);
-                            un.pad = 0;
-                            sc.units[u0 + u] = un;
-                        }
-                        yz_advance_state(S, base, (int)G, st);
+                        yz_unit_states(S, base, (int)G, (int)gper, st, sc.units + u0, hid);
                     }
                 }
                 if (inline_it) {
@@ -858,8 +875,7 @@ __global__ void __launch_bounds__(YZ_WARPS * 32)
         yz_build(S, E, T, P, st3, base, garena);
         yz_xhits(S, T, P);
         Stale st[4];
-        for (int k = 0; k < 4; ++k) st[k] = hv2.entry[k];
-        yz_advance_state(S, base, un.g0, st);
+        for (int k = 0; k < 4; ++k) st[k] = un.entry[k];
         const long C2 = (long)S.np[0] * S.np[1];
         const unsigned long long bk = yz_range(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P);
         __syncwarp();
