@@ -613,7 +613,7 @@ typedef struct {
 /* H:464-549.  `pairs` must hold n1*n2+n1+n2 entries. */
 static int make_hitpairs_in_station(hitcoll_t h1, int n1, hitcoll_t h2, int n2, pair_t *pairs, int stID, int projID,
                                     const or_plane_t *p, float xmin, float xmax, short *idx1buf, short *idx2buf,
-                                    short *flag1, short *flag2) {
+                                    short *flag1, short *flag2, int64_t *dommax) {
     int npairs = 0;
     const int detid1 = detsuperid[stID][projID] * 2;
     const int detid2 = detsuperid[stID][projID] * 2 - 1;
@@ -666,6 +666,12 @@ static int make_hitpairs_in_station(hitcoll_t h1, int n1, hitcoll_t h2, int n2, 
             pairs[npairs].second = idx2buf[b];
             npairs++;
         }
+    /* the reference's hitidx/hitpairs arrays hold 100 entries (K:890-903, K:1857-1867) */
+    if (dommax) {
+        int m = c1 > c2 ? c1 : c2;
+        if (npairs > m) m = npairs;
+        if (m > *dommax) *dommax = m;
+    }
     return npairs;
 }
 
@@ -1157,7 +1163,8 @@ static void yz_event(const or_plane_t *P, or_hits_view_t hv, or_tracks_view_t tv
                 float xmin = fminf((tx - err_tx) * zl[a], (tx - err_tx) * zl[a + 1]) + x0 - err_x0 - det_spacing[a];
                 float xmax = fmaxf((tx + err_tx) * zl[a], (tx + err_tx) * zl[a + 1]) + x0 + err_x0 + det_spacing[a];
                 npair[q] = make_hitpairs_in_station(hc[a], hc[a].n, hc[a + 1], hc[a + 1].n, ps->pairs[q], stids[q],
-                                                    projs[q], P, xmin, xmax, ps->idx1, ps->idx2, ps->flag1, ps->flag2);
+                                                    projs[q], P, xmin, xmax, ps->idx1, ps->idx2, ps->flag1, ps->flag2,
+                                                    cnt ? cnt + 6 : NULL);
             }
             const int nu2 = npair[0], nv2 = npair[1], nu3 = npair[2], nv3 = npair[3];
             T[OR_TRK_STID] = 3.f; /* K:1285 */
@@ -1488,7 +1495,7 @@ static void global_event(const or_plane_t *P, or_hits_view_t hv, or_tracks_view_
                 np[q] = make_hitpairs_in_station(hc[2 * q], hc[2 * q].n, hc[2 * q + 1], hc[2 * q + 1].n, ps->pairs[q],
                                                  0, q, P, pos_exp[q] - window[q] * 1.0f,
                                                  pos_exp[q] + window[q] * 1.0f, ps->idx1, ps->idx2, ps->flag1,
-                                                 ps->flag2);
+                                                 ps->flag2, cnt ? cnt + 7 : NULL);
             const int nx1 = np[0], nu1 = np[1], nv1 = np[2];
             if (nx1 == 0 || nu1 == 0 || nv1 == 0) continue;
             short nyhits = 0; /* K:2086-2102 */

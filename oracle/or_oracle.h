@@ -55,8 +55,10 @@ void orc_run_all(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, int3
  * reference's enumeration: [0] XZ (pair2, pair3) candidates, [1] YZ
  * (u3,v3,u2,v2) combinations, [2] Global (x1,u1,v1) combinations, [3] YZ
  * combinations reaching the first y fit, [4] passing its 2-sigma cut,
- * [5] passing every gate up to the chi2. */
-#define ORC_NCOUNTS 6
+ * [5] passing every gate up to the chi2, [6] the largest windowed hit list
+ * or pair list of any YZ tracklet, [7] the same for global tracking (the
+ * reference's arrays hold 100, K:890-903, K:1857-1867). */
+#define ORC_NCOUNTS 8
 void orc_run_all_counted(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, int32_t *ntracklets,
                          uint8_t *toomany, uint32_t *status, int64_t *counts, int n_events, int n_threads);
 

@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(HERE, "liborc.so")
 SOURCES = [os.path.join(HERE, "or_oracle.c")]
 
 ST_TOOMANY_ER, ST_TOOMANY_XZBIN, ST_TOOMANY_TKL = 1, 2, 4
-NCOUNTS = 6
+NCOUNTS = 8
 
 
 def build(force=False):
