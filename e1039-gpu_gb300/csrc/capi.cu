@@ -21,6 +21,8 @@ cudaError_t launch_pack(const or_hit_record_t *, const int64_t *, int, const flo
                         int);
 cudaError_t launch_collect(or_tracks_view_t, const uint8_t *, int, float, float *, long long, unsigned long long *,
                            cudaStream_t);
+cudaError_t launch_yz_noalloc(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
+                              cudaStream_t, const char **);
 }  // namespace orgpu
 
 struct or_ctx {
@@ -191,6 +193,24 @@ int or_yz(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uin
                                      ctx->yz_cap_units, ctx->yz_cap_heavy, ctx->yz_garena_warps, S(stream),
                                      ctx->sm_count);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "YZ launch");
+}
+
+int or_yz_noalloc(const or_plane_t *d_plane, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany,
+                  int n_events, uint32_t *d_errw, void *stream) {
+    if (n_events < 0) return fail(OR_ERR_ARG, "or_yz_noalloc: negative event count");
+    if (n_events > OR_YZ_NOALLOC_MAX_EVENTS)
+        return fail(OR_ERR_CAPACITY, "or_yz_noalloc: " + std::to_string(n_events) +
+                                         " events exceed its static scratch limit of " +
+                                         std::to_string(OR_YZ_NOALLOC_MAX_EVENTS) +
+                                         " events per call; split the batch or use or_yz");
+    if (!d_plane || !toomany || !d_errw) return fail(OR_ERR_ARG, "or_yz_noalloc: null geometry, flag or error word");
+    int rc;
+    if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
+    const char *why = nullptr;
+    cudaError_t e = orgpu::launch_yz_noalloc(d_plane, hits, tracks, toomany, n_events, d_errw, S(stream), &why);
+    if (e == cudaSuccess) return OR_OK;
+    if (why) return fail(OR_ERR_CAPACITY, std::string("or_yz_noalloc: ") + why);
+    return cuda_fail(e, "or_yz_noalloc");
 }
 
 int or_back_clean(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, void *stream) {

@@ -17,7 +17,10 @@ OR_OK, OR_ERR_ARG, OR_ERR_CUDA, OR_ERR_IO, OR_ERR_NOMEM, OR_ERR_CAPACITY, OR_ERR
 EXPORTS = ("or_version", "or_last_error", "or_status_string", "or_geometry_load", "or_create", "or_destroy",
            "or_set_geometry", "or_stream_sync", "or_event_reduce", "or_xz", "or_yz", "or_back_clean", "or_global",
            "or_run_batch", "or_hits_view_from_collection", "or_tracks_view_from_collection", "or_hits_view_bytes",
-           "or_tracks_view_bytes", "or_pack_hits", "or_collect_tracks")
+           "or_tracks_view_bytes", "or_pack_hits", "or_collect_tracks", "or_yz_noalloc")
+
+OR_YZ_NOALLOC_MAX_EVENTS = 10000
+OR_ERRW_CAPACITY = 2
 
 
 class OrError(RuntimeError):
@@ -64,6 +67,7 @@ def lib():
     lb.or_tracks_view_bytes.restype = C.c_size_t
     lb.or_pack_hits.argtypes = [vp, vp, vp, C.c_int, vp, L.OrHitsView, vp]
     lb.or_collect_tracks.argtypes = [vp, L.OrTracksView, vp, C.c_int, C.c_float, vp, C.c_int64, vp, vp]
+    lb.or_yz_noalloc.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, C.c_int, vp, vp]
     for name in EXPORTS:
         getattr(lb, name)
     _lib = lb

@@ -71,7 +71,8 @@ int or_destroy(or_ctx_t *ctx);
 int or_set_geometry(or_ctx_t *ctx, const or_plane_t *plane);
 /* Wait for `stream` and report the device-side error words raised since the
  * last call: OR_ERR_TIMEOUT when a bounded bulk-copy wait gave up,
- * OR_ERR_CAPACITY when a hit-pair window overflowed its 128-entry list (that
+ * OR_ERR_CAPACITY when a hit window overflowed its fixed list (100 windowed
+ * hits or pairs per projection in YZ, 128 pairs in global tracking; that
  * tracklet or track is left unextended).  The reference has no such report;
  * its kernels write past their arrays instead. */
 int or_stream_sync(or_ctx_t *ctx, void *stream);
@@ -114,6 +115,40 @@ int or_pack_hits(or_ctx_t *ctx, const or_hit_record_t *records, const int64_t *r
  * the copied-back collections (online_reconstruction.cu:1023-1224). */
 int or_collect_tracks(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, float stid,
                       float *out, int64_t capacity, uint64_t *d_count, void *stream);
+
+/* YZ tracklet stage that allocates nothing and needs no context.  This entry
+ * point has no counterpart in the reference, whose host code allocates all of
+ * its device memory up front (online_reconstruction.cu:738-744).
+ *
+ * It is for callers that cannot allocate device memory when they call: a
+ * trigger or serving process that gives all free HBM to its own pool at
+ * start-up (or_create() would need about 390 MB for or_yz()'s work queue), or
+ * a latency-critical loop that must not call cudaMalloc/cudaFree because they
+ * synchronise the device.  Results are those of or_yz() on the same buffers.
+ *
+ *   d_plane  device copy of the geometry (sizeof(or_plane_t) bytes, owned by
+ *            the caller);
+ *   d_errw   device uint32 owned by the caller; OR_ERRW_CAPACITY is OR'ed
+ *            into it when a hit window overflowed (the tracklet is left
+ *            unextended; or_stream_sync() reports the same event for or_yz()
+ *            as OR_ERR_CAPACITY);
+ *   other arguments as or_yz().
+ *
+ * Scratch: a static device array of OR_YZ_NOALLOC_SCRATCH_BYTES per device,
+ * reserved by the CUDA runtime when the library's module is loaded.  The
+ * first call on a device, with that device current, looks its address up
+ * (cudaGetSymbolAddress) and caches it: make that first call before any
+ * stream capture.  Each call clears the queue counters on `stream`.
+ * Calls that overlap on one device (several streams or host threads) share
+ * the array and race: serialise them.
+ *
+ * n_events above OR_YZ_NOALLOC_MAX_EVENTS (the reference's batch, EstnEvtMax
+ * in reconstruction_constants.h:20) returns OR_ERR_CAPACITY before any launch. */
+#define OR_YZ_NOALLOC_MAX_EVENTS 10000
+#define OR_ERRW_CAPACITY 2u
+#define OR_YZ_NOALLOC_SCRATCH_BYTES (56u << 20)
+int or_yz_noalloc(const or_plane_t *d_plane, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany,
+                  int n_events, uint32_t *d_errw, void *stream);
 
 #ifdef __cplusplus
 }
