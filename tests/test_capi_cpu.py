@@ -1,0 +1,61 @@
+"""The C-ABI library without a GPU: it loads, exports every function that
+include/*.h declares, and its host-side argument checks return the
+documented status codes before any CUDA call."""
+import ctypes as C
+import os
+import re
+
+from conftest import REPO
+
+
+def _declared_functions():
+    names = set()
+    for h in ("or_gb300.h", "or_layout.h"):
+        text = open(os.path.join(REPO, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"^[A-Za-z_][\w \*]*?\b(or_\w+)\s*\(", text, flags=re.M))
+    return names
+
+
+def test_library_exports_every_declared_function():
+    from orgpu import _lib
+    lb = _lib.lib()
+    declared = _declared_functions()
+    assert "or_run_batch" in declared and "or_yz_noalloc" in declared
+    assert declared == set(_lib.EXPORTS)
+    for name in declared:
+        getattr(lb, name)
+
+
+def test_status_strings_and_version():
+    from orgpu import _lib
+    lb = _lib.lib()
+    assert b"sm_103a" in lb.or_version()
+    assert lb.or_status_string(_lib.OR_ERR_CAPACITY) == b"capacity exceeded"
+    assert lb.or_status_string(99) == b"unknown status"
+
+
+def test_host_argument_checks():
+    from orgpu import _lib, layout as L
+    lb = _lib.lib()
+    assert lb.or_create(0, None) == _lib.OR_ERR_ARG
+    assert lb.or_destroy(None) == _lib.OR_OK
+    assert lb.or_yz(None, L.OrHitsView(), L.OrTracksView(), None, 1, None) == _lib.OR_ERR_ARG
+    assert b"null context" in lb.or_last_error()
+    assert lb.or_geometry_load(b"/nonexistent/geometry.txt", C.byref(L.OrPlane()), None) == _lib.OR_ERR_IO
+
+
+def test_collection_views_follow_reference_layout():
+    from orgpu import _lib, layout as L
+    lb = _lib.lib()
+    base = 1 << 40
+    v = lb.or_hits_view_from_collection(base)
+    E = L.REF_EVTMAX
+    assert v.nhits_cham == base
+    assert v.hits_cham == base + 4 * E * L.NCHAM
+    assert v.nhits_hodo == v.hits_cham + 4 * E * L.EVT_CHAM_FLOATS
+    assert v.hits_prop == v.nhits_prop + 4 * E * L.NPROP
+    t = lb.or_tracks_view_from_collection(base)
+    assert t.tracks == base + 2 * E * L.NSLOTS
+    assert lb.or_hits_view_bytes(3) == 3 * (4 * (L.NCHAM + L.NHODO + L.NPROP) + 4 * (
+        L.EVT_CHAM_FLOATS + L.EVT_HODO_FLOATS + L.EVT_PROP_FLOATS))
