@@ -1397,28 +1397,46 @@ static void clean_event(or_tracks_view_t tv, long e, const uint8_t *toomany) {
 
 static void clean_cross_event(or_tracks_view_t tv, long e, const uint8_t *toomany) {
     if (toomany[e]) return;
-    /* H:1846-1909, slots visited in order 0..31 */
+    /* H:1846-1909.  The reference block's 32 threads (one slot each) run this
+     * loop together: at each step (i_trd, i, j) every thread whose slot is
+     * not i_trd compares its track i with track j of slot i_trd, reading the
+     * stationIDs left by the steps before, and the demotions of the step
+     * (stationID = 3, H:1895-1903) land together after it.  The threads are
+     * emulated in that lockstep order. */
+    int nt[OR_NSLOTS], maxn = 0;
     for (int t = 0; t < OR_NSLOTS; t++) {
-        int n = tv.ntracks[e * OR_NSLOTS + t];
-        for (int u = 0; u < OR_NSLOTS; u++) {
-            if (u == t) continue;
-            int m = tv.ntracks[e * OR_NSLOTS + u];
-            for (int i = 0; i < n; i++) {
-                float *Ti = trk_rec(tv, e, t, i);
-                if (Ti[OR_TRK_STID] < 5) continue;
-                short ni = (short)Ti[OR_TRK_NHITS];
-                int nc = 0;
-                for (int j = 0; j < m; j++) {
-                    float *Tj = trk_rec(tv, e, u, j);
-                    if (Tj[OR_TRK_STID] < 5) continue;
-                    short nj = (short)Tj[OR_TRK_NHITS];
-                    nc = common_hits(Ti, ni, Tj, nj, nc);
-                    if (Ti[OR_TRK_CHI2] / (float)(ni - 4) < Tj[OR_TRK_CHI2] / (float)(nj - 4)) {
-                        if ((float)nc > (float)ni * 0.3333f) Tj[OR_TRK_STID] = 3.f;
+        nt[t] = tv.ntracks[e * OR_NSLOTS + t];
+        if (nt[t] > maxn) maxn = nt[t];
+    }
+    for (int u = 0; u < OR_NSLOTS; u++) { /* i_trd */
+        const int m = nt[u];
+        for (int i = 0; i < maxn; i++) {
+            int act[OR_NSLOTS], nc[OR_NSLOTS];
+            short ni[OR_NSLOTS];
+            for (int t = 0; t < OR_NSLOTS; t++) {
+                act[t] = t != u && i < nt[t] && trk_rec(tv, e, t, i)[OR_TRK_STID] >= 5;
+                ni[t] = act[t] ? (short)trk_rec(tv, e, t, i)[OR_TRK_NHITS] : 0;
+                nc[t] = 0;
+            }
+            for (int j = 0; j < m; j++) {
+                float *Tj = trk_rec(tv, e, u, j);
+                if (Tj[OR_TRK_STID] < 5) continue;
+                const short nj = (short)Tj[OR_TRK_NHITS];
+                int demote_j = 0, demote_i[OR_NSLOTS];
+                for (int t = 0; t < OR_NSLOTS; t++) {
+                    demote_i[t] = 0;
+                    if (!act[t]) continue;
+                    const float *Ti = trk_rec(tv, e, t, i);
+                    nc[t] = common_hits(Ti, ni[t], Tj, nj, nc[t]);
+                    if (Ti[OR_TRK_CHI2] / (float)(ni[t] - 4) < Tj[OR_TRK_CHI2] / (float)(nj - 4)) {
+                        if ((float)nc[t] > (float)ni[t] * 0.3333f) demote_j = 1;
                     } else {
-                        if ((float)nc > (float)nj * 0.3333f) Ti[OR_TRK_STID] = 3.f;
+                        if ((float)nc[t] > (float)nj * 0.3333f) demote_i[t] = 1;
                     }
                 }
+                if (demote_j) Tj[OR_TRK_STID] = 3.f;
+                for (int t = 0; t < OR_NSLOTS; t++)
+                    if (demote_i[t]) trk_rec(tv, e, t, i)[OR_TRK_STID] = 3.f;
             }
         }
     }

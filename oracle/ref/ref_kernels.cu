@@ -1,0 +1,12 @@
+// ref_kernels.cu -- translation unit that compiles the reference's own path
+// kernels, unchanged, from their sources (OnlineReconstruction/
+// reconstruction_kernels.cuh and the headers it includes) into a device
+// image.  TEST INFRASTRUCTURE ONLY: the image is the reference the oracle is
+// pinned against; nothing in the library loads it.
+//
+// The reference's headers are found through -I at build time
+// (oracle/ref/build_ref.py); this file holds no reference code.
+#include <cassert>
+#include <thrust/pair.h>
+
+#include "reconstruction_kernels.cuh"

@@ -1,0 +1,154 @@
+"""Run the reference's own kernels, compiled by build_ref.py, on the GPU
+through the CUDA driver API.  TEST INFRASTRUCTURE ONLY: used to pin the CPU
+oracle (tests/golden/make_golden.py); the library never loads these images.
+
+The kernels take the reference's fixed-capacity structs (EstnEvtMax = 10000
+events, reconstruction_constants.h:20): gEventHitCollections
+(reconstruction_classes.cuh:76-87), gEventTrackCollection (:542-544), gPlane
+(:947-977) and a bool per event.  Each stage is launched as the reference
+host launches it (online_reconstruction.cu:776-894): one block per event,
+8 threads for the event reducer, 32 for the others.
+
+The reference's XZ kernel (reconstruction_kernels.cuh:182-855) is not
+exposed: it calls __syncthreads() inside thread-dependent branches (K:684,
+K:724, K:767, K:807), which CUDA leaves undefined and which may hang.
+
+Inputs must stay inside the reference's array bounds (raw chamber hits per
+plane <= 120, windowed hits and pairs <= 100 per projection); callers filter
+events with the oracle's domain counters before launching.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from orgpu import layout as L
+
+from . import build_ref
+
+E = L.REF_EVTMAX
+HITS_BYTES = 4 * E * (L.NCHAM + L.NHODO + L.NPROP) + 4 * E * (L.EVT_CHAM_FLOATS + L.EVT_HODO_FLOATS +
+                                                             L.EVT_PROP_FLOATS)
+TRACKS_BYTES = 2 * E * L.NSLOTS + 4 * E * L.EVT_TRK_FLOATS
+
+KERNELS = {
+    "er": "_Z10gkernel_eRP20gEventHitCollectionsPb",
+    "yz": "_Z19gKernel_YZ_trackingP20gEventHitCollectionsP21gEventTrackCollectionPK6gPlanePb",
+    "clean": "_Z25gKernel_BackTrackCleaningP21gEventTrackCollectionPKb",
+    "clean_x": "_Z38gKernel_BackTrackCleaning_crossthreadsP21gEventTrackCollectionPKb",
+    "global": "_Z23gKernel_Global_trackingP20gEventHitCollectionsP21gEventTrackCollectionPK6gPlanePb",
+}
+
+# byte offsets of the members of gEventHitCollections (4-byte members, no padding)
+_HIT_SECTIONS = []
+_o = 0
+for _name, _cnt, _dt in (("nhits_cham", E * L.NCHAM, np.uint32), ("hits_cham", E * L.EVT_CHAM_FLOATS, np.float32),
+                         ("nhits_hodo", E * L.NHODO, np.uint32), ("hits_hodo", E * L.EVT_HODO_FLOATS, np.float32),
+                         ("nhits_prop", E * L.NPROP, np.uint32), ("hits_prop", E * L.EVT_PROP_FLOATS, np.float32)):
+    _HIT_SECTIONS.append((_name, _o, _dt))
+    _o += 4 * _cnt
+assert _o == HITS_BYTES
+_TRK_OFF = 2 * E * L.NSLOTS
+
+
+class CudaDriverError(RuntimeError):
+    pass
+
+
+class RefKernels:
+    """One loaded image ("fmad0" or "fmad1") plus the device structs."""
+
+    def __init__(self, variant="fmad0", device=0):
+        import torch
+        self.torch = torch
+        path = build_ref.image_path(variant)
+        if not os.path.exists(path):
+            raise FileNotFoundError(f"reference image {path} not built (oracle/ref/build_ref.py)")
+        torch.cuda.set_device(device)
+        torch.zeros(1, device="cuda")  # the primary context is current from here on
+        self.cu = C.CDLL("libcuda.so.1")
+        self.mod = C.c_void_p()
+        self._chk(self.cu.cuModuleLoad(C.byref(self.mod), path.encode()), "cuModuleLoad")
+        self.fn = {}
+        for key, name in KERNELS.items():
+            f = C.c_void_p()
+            self._chk(self.cu.cuModuleGetFunction(C.byref(f), self.mod, name.encode()), f"cuModuleGetFunction {key}")
+            self.fn[key] = f
+        dev = torch.device("cuda", device)
+        self.hits = torch.zeros(HITS_BYTES, dtype=torch.uint8, device=dev)
+        self.tracks = torch.zeros(TRACKS_BYTES, dtype=torch.uint8, device=dev)
+        self.plane = torch.zeros(C.sizeof(L.OrPlane), dtype=torch.uint8, device=dev)
+        self.flags = torch.zeros(E, dtype=torch.uint8, device=dev)
+
+    def _chk(self, rc, what):
+        if rc != 0:
+            name = C.c_char_p()
+            self.cu.cuGetErrorName(rc, C.byref(name))
+            raise CudaDriverError(f"{what}: CUresult {rc} ({name.value.decode() if name.value else '?'})")
+
+    def close(self):
+        if self.mod:
+            self.torch.cuda.synchronize()
+            self.cu.cuModuleUnload(self.mod)
+            self.mod = C.c_void_p()
+
+    # -- struct I/O ------------------------------------------------------------
+    def set_plane(self, plane):
+        self.plane.copy_(self.torch.frombuffer(bytearray(plane.to_bytes()), dtype=self.torch.uint8))
+
+    def put_hits(self, h):
+        assert h.n <= E
+        t = self.torch
+        for (name, off, dt), arr in zip(_HIT_SECTIONS, h.arrays()):
+            b = arr.view(np.uint8)
+            self.hits[off:off + b.size].copy_(t.from_numpy(b))
+
+    def get_hits(self, n):
+        h = L.HostHits(n)
+        for (name, off, dt), arr in zip(_HIT_SECTIONS, h.arrays()):
+            b = self.hits[off:off + arr.nbytes].cpu().numpy()
+            arr[:] = b.view(dt)
+        return h
+
+    def put_tracks(self, t):
+        assert t.n <= E
+        self.tracks[:t.ntracks.nbytes].copy_(self.torch.from_numpy(t.ntracks.view(np.uint8)))
+        self.tracks[_TRK_OFF:_TRK_OFF + t.tracks.nbytes].copy_(self.torch.from_numpy(t.tracks.view(np.uint8)))
+
+    def get_tracks(self, n):
+        t = L.HostTracks(n)
+        t.ntracks[:] = self.tracks[:t.ntracks.nbytes].cpu().numpy().view(np.uint16)
+        t.tracks[:] = self.tracks[_TRK_OFF:_TRK_OFF + t.tracks.nbytes].cpu().numpy().view(np.float32)
+        return t
+
+    def put_flags(self, toomany):
+        n = toomany.size
+        self.flags[:n].copy_(self.torch.from_numpy(np.ascontiguousarray(toomany, np.uint8)))
+
+    def get_flags(self, n):
+        return self.flags[:n].cpu().numpy().copy()
+
+    # -- launches --------------------------------------------------------------
+    def _launch(self, key, n, threads, *ptrs):
+        vals = [C.c_void_p(p) for p in ptrs]
+        args = (C.c_void_p * len(vals))(*[C.cast(C.byref(v), C.c_void_p) for v in vals])
+        stream = C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+        self._chk(self.cu.cuLaunchKernel(self.fn[key], n, 1, 1, threads, 1, 1, 0, stream, args, None),
+                  f"launch {key}")
+        self.torch.cuda.synchronize()
+        self._chk(self.cu.cuCtxSynchronize(), f"after {key}")
+
+    def event_reduce(self, n):
+        self._launch("er", n, 8, self.hits.data_ptr(), self.flags.data_ptr())
+
+    def yz(self, n):
+        self._launch("yz", n, 32, self.hits.data_ptr(), self.tracks.data_ptr(), self.plane.data_ptr(),
+                     self.flags.data_ptr())
+
+    def back_clean(self, n):
+        self._launch("clean", n, 32, self.tracks.data_ptr(), self.flags.data_ptr())
+        self._launch("clean_x", n, 32, self.tracks.data_ptr(), self.flags.data_ptr())
+
+    def global_tracking(self, n):
+        self._launch("global", n, 32, self.hits.data_ptr(), self.tracks.data_ptr(), self.plane.data_ptr(),
+                     self.flags.data_ptr())

@@ -1,0 +1,127 @@
+"""Compact forms of the reference-layout buffers for golden fixtures, and the
+comparisons the golden tests use.
+
+Hit collections are stored as per-event counts [n, 54] (index = detector id)
+plus the concatenated valid hit fields; track collections as slot counts
+[n, 32] plus (event, slot, position) and the 148-float record of every valid
+track.  Both are built from layout.HostHits / HostTracks and compare bit for
+bit or, for fit parameters, within a relative tolerance.
+"""
+import numpy as np
+
+from orgpu import layout as L
+
+# track-record fields that are discrete (ids, counts, signs, charge) and must
+# match exactly under any float rounding of the fits
+DISCRETE_FIELDS = np.zeros(L.NTRKPARAM, bool)
+DISCRETE_FIELDS[[L.TRK_STID, L.TRK_THREAD, L.TRK_NHITS, L.TRK_CHARGE]] = True
+DISCRETE_FIELDS[L.TRK_HIT_DETID:L.TRK_HIT_DETID + 18] = True
+DISCRETE_FIELDS[L.TRK_HIT_CHAN:L.TRK_HIT_CHAN + 18] = True
+DISCRETE_FIELDS[L.TRK_HIT_SIGN:L.TRK_HIT_SIGN + 18] = True
+# fit parameters the 1e-5 relative tolerance is stated for
+FIT_FIELDS = [L.TRK_CHI2, L.TRK_TX, L.TRK_TY, L.TRK_X0, L.TRK_Y0, L.TRK_INVP, L.TRK_ERR_TX, L.TRK_ERR_TY,
+              L.TRK_ERR_X0, L.TRK_ERR_Y0, L.TRK_ERR_INVP]
+
+
+def compact_hits(h):
+    """(counts int32 [n, 55], hits float32 [m]) -- hits in event, detector
+    order, each plane's 5*count floats as stored (SoA)."""
+    counts = np.zeros((h.n, L.NDET), np.int32)
+    parts = []
+    for e in range(h.n):
+        for det in range(1, L.NDET):
+            n, data = h.plane(e, det)
+            counts[e, det] = n
+            if n:
+                parts.append(data.reshape(-1))
+    flat = np.concatenate(parts) if parts else np.zeros(0, np.float32)
+    return counts, flat.astype(np.float32)
+
+
+def compact_tracks(t, toomany=None):
+    """(ntracks uint16 [n, 32], where int32 [m, 3], records float32 [m, 148]).
+    Events flagged in `toomany` are stored with no tracks."""
+    nt = t.ntracks.reshape(t.n, L.NSLOTS).copy()
+    if toomany is not None:
+        nt[np.asarray(toomany, bool)] = 0
+    where, recs = [], []
+    for e in range(t.n):
+        for s in range(L.NSLOTS):
+            for k in range(int(nt[e, s])):
+                base = e * L.EVT_TRK_FLOATS + (s * L.SLOTCAP + k) * L.NTRKPARAM
+                where.append((e, s, k))
+                recs.append(t.tracks[base:base + L.NTRKPARAM])
+    w = np.array(where, np.int32).reshape(-1, 3)
+    r = np.array(recs, np.float32).reshape(-1, L.NTRKPARAM)
+    return nt, w, r
+
+
+def compare_hits(a, b):
+    """Bitwise: list of (event, detector) whose counts or hit data differ."""
+    ca, fa = a
+    cb, fb = b
+    out = []
+    if ca.shape != cb.shape:
+        return [("shape", ca.shape, cb.shape)]
+    oa = np.concatenate([[0], np.cumsum(5 * ca.reshape(-1))])
+    ob = np.concatenate([[0], np.cumsum(5 * cb.reshape(-1))])
+    for i in range(ca.size):
+        if ca.flat[i] != cb.flat[i]:
+            out.append((i // L.NDET, i % L.NDET, "count"))
+        elif not np.array_equal(fa[oa[i]:oa[i + 1]].view(np.uint32), fb[ob[i]:ob[i + 1]].view(np.uint32)):
+            out.append((i // L.NDET, i % L.NDET, "data"))
+    return out
+
+
+RESID_FIELDS = np.zeros(L.NTRKPARAM, bool)
+RESID_FIELDS[L.TRK_HIT_RESID:L.TRK_HIT_RESID + 18] = True
+
+
+def compare_tracks(a, b, rtol=0.0, resid_atol=None):
+    """Compare compact track sets.  rtol == 0: every field bit for bit.
+    rtol > 0: discrete fields exactly, the rest within rtol relative to
+    max(|a|, |b|) (absolute 1e-6 near zero); hit residuals, which are
+    differences of nearly equal numbers, within resid_atol (cm) when given.
+    Returns a dict with the events whose slot counts differ, the records
+    with a discrete difference, the records outside the tolerance, and the
+    largest relative difference seen on the fit parameters."""
+    nta, wa, ra = a
+    ntb, wb, rb = b
+    res = {"events": int(nta.shape[0]), "tracks": int(wa.shape[0]), "count_mismatch": [], "discrete_mismatch": [],
+           "value_mismatch": [], "max_rel_fit": 0.0}
+    bad_events = np.nonzero((nta != ntb).any(axis=1))[0]
+    res["count_mismatch"] = [int(e) for e in bad_events]
+    if bad_events.size:
+        keep_a = ~np.isin(wa[:, 0], bad_events)
+        keep_b = ~np.isin(wb[:, 0], bad_events)
+        wa, ra, wb, rb = wa[keep_a], ra[keep_a], wb[keep_b], rb[keep_b]
+    assert np.array_equal(wa, wb)
+    if rtol == 0.0:
+        diff = (ra.view(np.uint32) != rb.view(np.uint32)).any(axis=1)
+        res["value_mismatch"] = [tuple(int(x) for x in wa[i]) for i in np.nonzero(diff)[0]]
+        return res
+    disc = (ra[:, DISCRETE_FIELDS] != rb[:, DISCRETE_FIELDS]).any(axis=1)
+    res["discrete_mismatch"] = [tuple(int(x) for x in wa[i]) for i in np.nonzero(disc)[0]]
+    ok = ~disc
+    scale = np.maximum(np.abs(ra), np.abs(rb))
+    err = np.abs(ra.astype(np.float64) - rb.astype(np.float64))
+    tol = np.maximum(rtol * scale, 1e-6)
+    if resid_atol is not None:
+        tol[:, RESID_FIELDS] = resid_atol
+    both_nan = np.isnan(ra) & np.isnan(rb)
+    out = ((err > tol) & ~both_nan & ~DISCRETE_FIELDS[None, :]).any(axis=1) & ok
+    res["value_mismatch"] = [tuple(int(x) for x in wa[i]) for i in np.nonzero(out)[0]]
+    if ok.any():
+        rel = err[ok][:, FIT_FIELDS] / np.maximum(scale[ok][:, FIT_FIELDS], 1e-30)
+        rel[~np.isfinite(rel)] = 0.0
+        res["max_rel_fit"] = float(rel.max()) if rel.size else 0.0
+    return res
+
+
+def select_events(rec, off, idx):
+    """Records and offsets of the events `idx` (in that order)."""
+    idx = np.asarray(idx, np.int64)
+    parts = [rec[off[e]:off[e + 1]] for e in idx]
+    lens = np.array([len(p) for p in parts], np.int64)
+    new_off = np.concatenate([[0], np.cumsum(lens)]).astype(off.dtype)
+    return (np.concatenate(parts) if parts else rec[:0]), new_off
