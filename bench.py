@@ -132,7 +132,8 @@ def main():
 
     plane, wp = _lib.geometry_load(GEOMETRY_E906)
     n = args.events
-    cfg = S.config_uneven(n, args.seed + 1000 * rank)
+    from orgpu import shard
+    cfg = S.config_uneven(n, shard.rank_seed(args.seed, rank))
     rec, off, truth = S.generate(S.Geometry(plane, wp), cfg)
     rec, off = S.cap_records(rec, off)
     cj = config_json(args, n)
@@ -221,10 +222,7 @@ def main():
     for evs in all_evs:
         for k, s in enumerate(stages):
             per_stage[s].append(evs[k].elapsed_time(evs[k + 1]))
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = shard.max_over_ranks(ms, device=dev)
     value = world * n / (ms / 1000.0)
     stage_ms = {s: statistics.mean(v) for s, v in per_stage.items()}
 
@@ -270,10 +268,7 @@ def main():
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = shard.max_over_ranks(e2e_ms, device=dev)
     rc.sync()
 
     if rank != 0:
