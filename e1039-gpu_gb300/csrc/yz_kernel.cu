@@ -46,11 +46,13 @@ constexpr long YZ_EVENT_INLINE = 16384; // ... and per event
 constexpr long YZ_UNIT = 4096;          // combinations per queued unit (whole (u3,v3) iterations)
 constexpr int YZ_GARENA_HITS = 8 * YZ_MAXWIN;  // per-warp global overflow arena
 
-struct YzHit {
-    float Y, eY, pos, drift, tdc;
+struct __align__(16) YzHit {
+    float Y, eY, pos, drift;
+    float tdc, z;  // z = the plane's z, read by every fit
     short det, el;
     int acc;  // calculate_y_uvhit accepted this hit for the tracklet
 };
+static_assert(sizeof(YzHit) == 32, "YzHit is two 16-byte words");
 
 struct Stale {
     short det;
@@ -228,6 +230,7 @@ __device__ bool yz_build(YzWarp &S, const YzEvent &E, const float *T, const or_p
             r.acc = calculate_y_uvhit(det, r.el, r.drift, 0, x0, tx, P, yy, ey) ? 1 : 0;
             r.Y = yy;
             r.eY = ey;
+            r.z = P.z[det];
             dst[S.woff[l] + i] = r;
         }
     }
@@ -458,7 +461,7 @@ __device__ __forceinline__ int yz_gather(const YzWarp &S, const YzHit *base, int
         u.sign = 0;
         u.drift = r.drift;
         u.pos = r.pos;
-        u.Z = P.z[r.det];
+        u.Z = r.z;
         u.Y = r.Y;
         u.eY = r.eY;
         ++nuv;
@@ -636,101 +639,153 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
     const YzHit *Lh[8];
 #pragma unroll
     for (int l = 0; l < 8; ++l) Lh[l] = yz_list(S, base, l);
-    for (int basec = c0; basec < c1; basec += 32) {
-        const int c = basec + lane;
-        const bool valid = c < c1;
-        int nuv = 0;
-        Stale own0{DET_SENTINEL, 0.f, 0.f}, own1 = own0, own2 = own0, own3 = own0;
-        unsigned wmask = 0u;
-        float y0 = 0.f, ty = 0.f, ey0 = 0.f, ety = 0.f;
-        bool pass1 = false;
-        if (valid) {
-            const int iuv3 = c / C2, iuv2 = c - iuv3 * C2;
-            const short2 pq[4] = {S.pair[2][iuv3 % nu3], S.pair[3][iuv3 / nu3], S.pair[0][iuv2 % nu2],
-                                  S.pair[1][iuv2 / nu2]};
-            Fit2 f;
-            // attempts in reference order: u3 a/b, v3 a/b, u2 a/b, v2 a/b
-            const int lists[8] = {4, 5, 6, 7, 0, 1, 2, 3};
-            int nbefore = 0;
-            bool alive = true;
+    const int nv2 = S.np[1];
+    // Lane's combination as digits (iu2, iv2, iu3, iv3) in radices (nu2, nv2,
+    // nu3, nv3) -- the reference's index order (u2 fastest) -- advanced by 32
+    // per chunk with carries instead of divisions.
+    int d0, d1, d2, d3, s0, s1, s2, s3;
+    {
+        const int c = c0 + lane;
+        const int g = c / C2, r = c - g * C2;
+        d0 = r % nu2;
+        d1 = r / nu2;
+        d2 = g % nu3;
+        d3 = g / nu3;
+        const int sg = 32 / C2, sr = 32 - sg * C2;
+        s0 = sr % nu2;
+        s1 = sr / nu2;
+        s2 = sg % nu3;
+        s3 = sg / nu3;
+    }
+    // station-3 part of the lane's current outer iteration (iu3, iv3): the
+    // fit sums over its accepted hits in the reference order, their count,
+    // and whether both u3 and v3 gave one (K:1326-1390); recomputed only
+    // when the outer digits move.
+    Fit2 f3;
+    int n3 = 0;
+    bool alive3 = false, need3 = true;
+    int basec = c0;
+    for (;;) {
+        const bool more = basec < c1;
+        if (!more && qn == 0) break;
+        if (more) {
+            const int c = basec + lane;
+            const bool valid = c < c1;
+            int nuv = 0;
+            Stale own0{DET_SENTINEL, 0.f, 0.f}, own1 = own0, own2 = own0, own3 = own0;
+            unsigned wmask = 0u;
+            float y0 = 0.f, ty = 0.f, ey0 = 0.f, ety = 0.f;
+            bool pass1 = false;
+            if (valid) {
+                if (need3) {
+                    const short2 pu = S.pair[2][d2], pv = S.pair[3][d3];
+                    Fit2 f;
+                    int nu = 0, nv = 0;
+                    if (pu.x >= 0) { const YzHit &r = Lh[4][pu.x]; if (r.acc) { f.add(r.Y, r.z, r.eY); ++nu; } }
+                    if (pu.y >= 0) { const YzHit &r = Lh[5][pu.y]; if (r.acc) { f.add(r.Y, r.z, r.eY); ++nu; } }
+                    if (nu > 0) {
+                        if (pv.x >= 0) { const YzHit &r = Lh[6][pv.x]; if (r.acc) { f.add(r.Y, r.z, r.eY); ++nv; } }
+                        if (pv.y >= 0) { const YzHit &r = Lh[7][pv.y]; if (r.acc) { f.add(r.Y, r.z, r.eY); ++nv; } }
+                    }
+                    f3 = f;
+                    n3 = nu + nv;
+                    alive3 = nu > 0 && nv > 0;
+                    need3 = false;
+                }
+                if (alive3) {
+                    // station-2 attempts in the reference order (K:1467-1597):
+                    // every attempted hit writes the scratch entry at the
+                    // running count, accepted ones enter the fit
+                    Fit2 f = f3;
+                    nuv = n3;
+                    const short2 pu = S.pair[0][d0];
+                    auto attempt = [&](const YzHit &r) {
+                        if (nuv == 4) { own0 = Stale{r.det, r.pos, r.drift}; wmask |= 1u; }
+                        else if (nuv == 5) { own1 = Stale{r.det, r.pos, r.drift}; wmask |= 2u; }
+                        else if (nuv == 6) { own2 = Stale{r.det, r.pos, r.drift}; wmask |= 4u; }
+                        else if (nuv == 7) { own3 = Stale{r.det, r.pos, r.drift}; wmask |= 8u; }
+                        if (r.acc) {
+                            f.add(r.Y, r.z, r.eY);
+                            ++nuv;
+                        }
+                    };
+                    if (pu.x >= 0) attempt(Lh[0][pu.x]);
+                    if (pu.y >= 0) attempt(Lh[1][pu.y]);
+                    const int nu2hits = nuv;
+                    if (nu2hits > n3) {
+                        const short2 pv = S.pair[1][d1];
+                        if (pv.x >= 0) attempt(Lh[2][pv.x]);
+                        if (pv.y >= 0) attempt(Lh[3][pv.y]);
+                        if (nuv > nu2hits) {  // the v2 group gave a hit: the fit is reached
+                            f.solve(y0, ty, ey0, ety);
+                            pass1 = !(fabsf(y0) > Y0_MAX + 2 * ey0 || fabsf(ty) > TY_MAX + 2 * ety);
+                        }
+                    }
+                }
+            }
+            // --- scratch entry past the hit count ------------------------------
+            Stale stj{DET_SENTINEL, 0.f, 0.f};
+            {
+                const int j = nuv;
+                const unsigned lt = lanemask_lt();
 #pragma unroll
-            for (int a = 0; a < 8; ++a) {
-                if (a == 2 || a == 4 || a == 6) {
-                    // a u3 (v3, u2, v2) group must have given an accepted hit
-                    alive = alive && nuv > nbefore;
-                    nbefore = nuv;
-                }
-                if (!alive) break;
-                const short2 p = pq[a >> 1];
-                const int wi = (a & 1) ? p.y : p.x;
-                if (wi < 0) continue;
-                const YzHit &r = Lh[lists[a]][wi];
-                if (a >= 4) {  // station-2 attempts write the scratch entry nuv
-                    if (nuv == 4) { own0 = Stale{r.det, r.pos, r.drift}; wmask |= 1u; }
-                    else if (nuv == 5) { own1 = Stale{r.det, r.pos, r.drift}; wmask |= 2u; }
-                    else if (nuv == 6) { own2 = Stale{r.det, r.pos, r.drift}; wmask |= 4u; }
-                    else if (nuv == 7) { own3 = Stale{r.det, r.pos, r.drift}; wmask |= 8u; }
-                }
-                if (r.acc) {
-                    f.add(r.Y, P.z[r.det], r.eY);
-                    ++nuv;
+                for (int k = 0; k < 4; ++k) {
+                    const Stale own = k == 0 ? own0 : (k == 1 ? own1 : (k == 2 ? own2 : own3));
+                    const unsigned m = __ballot_sync(0xffffffffu, (wmask >> k) & 1u);
+                    const int src = last_lane(m & lt);
+                    const short sd = (short)__shfl_sync(0xffffffffu, (int)own.det, src < 0 ? 0 : src);
+                    const float sp = __shfl_sync(0xffffffffu, own.pos, src < 0 ? 0 : src);
+                    const float sdr = __shfl_sync(0xffffffffu, own.drift, src < 0 ? 0 : src);
+                    if (j == k + 4) {
+                        if ((wmask >> k) & 1u) stj = own;
+                        else if (src >= 0) stj = Stale{sd, sp, sdr};
+                        else stj = st[k];
+                    }
+                    const int lw = last_lane(m);
+                    const short cd = (short)__shfl_sync(0xffffffffu, (int)own.det, lw < 0 ? 0 : lw);
+                    const float cp = __shfl_sync(0xffffffffu, own.pos, lw < 0 ? 0 : lw);
+                    const float cdr = __shfl_sync(0xffffffffu, own.drift, lw < 0 ? 0 : lw);
+                    if (lw >= 0) st[k] = Stale{cd, cp, cdr};
                 }
             }
-            const bool reached = alive && nuv > nbefore;  // the v2 group gave a hit
-            if (reached) {
-                f.solve(y0, ty, ey0, ety);
-                pass1 = !(fabsf(y0) > Y0_MAX + 2 * ey0 || fabsf(ty) > TY_MAX + 2 * ety);
+            // --- queue the survivors in order ----------------------------------
+            const unsigned pm = __ballot_sync(0xffffffffu, pass1);
+            if (pass1) {
+                PassEntry e;
+                e.c = c;
+                e.y0 = y0;
+                e.ty = ty;
+                e.ey0 = ey0;
+                e.ety = ety;
+                e.stdet = stj.det;
+                e.stpos = stj.pos;
+                e.stdrift = stj.drift;
+                S.q[qn + __popc(pm & lanemask_lt())] = e;
             }
+            qn += __popc(pm);
+            __syncwarp();
+            // --- next chunk: digits + 32 -----------------------------------------
+            basec += 32;
+            d0 += s0;
+            int cy = d0 >= nu2;
+            d0 -= cy ? nu2 : 0;
+            d1 += s1 + cy;
+            cy = d1 >= nv2;
+            d1 -= cy ? nv2 : 0;
+            if (cy || s2 || s3) need3 = true;
+            d2 += s2 + cy;
+            cy = d2 >= nu3;
+            d2 -= cy ? nu3 : 0;
+            d3 += s3 + cy;
         }
-        // --- scratch entry past the hit count ----------------------------------
-        Stale stj{DET_SENTINEL, 0.f, 0.f};
-        {
-            const int j = nuv;
-            const unsigned lt = lanemask_lt();
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const Stale own = k == 0 ? own0 : (k == 1 ? own1 : (k == 2 ? own2 : own3));
-                const unsigned m = __ballot_sync(0xffffffffu, (wmask >> k) & 1u);
-                const int src = last_lane(m & lt);
-                const short sd = (short)__shfl_sync(0xffffffffu, (int)own.det, src < 0 ? 0 : src);
-                const float sp = __shfl_sync(0xffffffffu, own.pos, src < 0 ? 0 : src);
-                const float sdr = __shfl_sync(0xffffffffu, own.drift, src < 0 ? 0 : src);
-                if (j == k + 4) {
-                    if ((wmask >> k) & 1u) stj = own;
-                    else if (src >= 0) stj = Stale{sd, sp, sdr};
-                    else stj = st[k];
-                }
-                const int lw = last_lane(m);
-                const short cd = (short)__shfl_sync(0xffffffffu, (int)own.det, lw < 0 ? 0 : lw);
-                const float cp = __shfl_sync(0xffffffffu, own.pos, lw < 0 ? 0 : lw);
-                const float cdr = __shfl_sync(0xffffffffu, own.drift, lw < 0 ? 0 : lw);
-                if (lw >= 0) st[k] = Stale{cd, cp, cdr};
-            }
-        }
-        // --- queue the survivors in order --------------------------------------
-        const unsigned pm = __ballot_sync(0xffffffffu, pass1);
-        if (pass1) {
-            PassEntry e;
-            e.c = c;
-            e.y0 = y0;
-            e.ty = ty;
-            e.ey0 = ey0;
-            e.ety = ety;
-            e.stdet = stj.det;
-            e.stpos = stj.pos;
-            e.stdrift = stj.drift;
-            S.q[qn + __popc(pm & lanemask_lt())] = e;
-        }
-        qn += __popc(pm);
-        __syncwarp();
-        if (qn >= 32) {
-            phase2(32);
-            if (lane < qn - 32) S.q[lane] = S.q[32 + lane];
-            qn -= 32;
+        if (qn >= 32 || (!more && qn > 0)) {
+            const int n = min(qn, 32);
+            phase2(n);
+            if (lane < qn - n) S.q[lane] = S.q[n + lane];
+            qn -= n;
             __syncwarp();
         }
     }
-    if (qn > 0) phase2(qn);
     return best;
 }
 
