@@ -16,7 +16,7 @@ cudaError_t launch_yz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, cons
 size_t yz_scratch_bytes(int, int, int);
 cudaError_t launch_back_clean(or_tracks_view_t, const uint8_t *, int, cudaStream_t, int);
 cudaError_t launch_global(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
-                          cudaStream_t, int);
+                          unsigned long long *, cudaStream_t, int);
 cudaError_t launch_pack(const or_hit_record_t *, const int64_t *, int, const float *, or_hits_view_t, cudaStream_t,
                         int);
 cudaError_t launch_collect(or_tracks_view_t, const uint8_t *, int, float, float *, long long, unsigned long long *,
@@ -31,6 +31,7 @@ struct or_ctx {
     or_plane_t *d_plane;
     bool has_geom;
     uint32_t *d_errw;
+    unsigned long long *d_sched;  // work-unit counters of the dynamically scheduled kernels
     // YZ work queue: units of heavy tracklets, their best records, overflow arenas
     void *yz_scratch;
     int yz_cap_units, yz_cap_heavy, yz_garena_warps;
@@ -112,6 +113,12 @@ int or_create(int device, or_ctx_t **out) {
         delete c;
         return fail(OR_ERR_NOMEM, "cudaMalloc error word");
     }
+    if ((e = cudaMalloc(&c->d_sched, 256)) != cudaSuccess) {
+        cudaFree(c->d_plane);
+        cudaFree(c->d_errw);
+        delete c;
+        return fail(OR_ERR_NOMEM, "cudaMalloc work counters");
+    }
     c->yz_cap_units = 1 << 20;
     c->yz_cap_heavy = 1 << 18;
     c->yz_garena_warps = c->sm_count * 16;
@@ -119,6 +126,7 @@ int or_create(int device, or_ctx_t **out) {
                         orgpu::yz_scratch_bytes(c->yz_cap_units, c->yz_cap_heavy, c->yz_garena_warps))) != cudaSuccess) {
         cudaFree(c->d_plane);
         cudaFree(c->d_errw);
+        cudaFree(c->d_sched);
         delete c;
         return fail(OR_ERR_NOMEM, "cudaMalloc YZ work queue");
     }
@@ -131,6 +139,7 @@ int or_destroy(or_ctx_t *ctx) {
     cudaSetDevice(ctx->device);
     cudaFree(ctx->d_plane);
     cudaFree(ctx->d_errw);
+    cudaFree(ctx->d_sched);
     cudaFree(ctx->yz_scratch);
     delete ctx;
     return OR_OK;
@@ -229,7 +238,8 @@ int or_global(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const
     if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
     if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
     cudaError_t e =
-        orgpu::launch_global(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw, S(stream), ctx->sm_count);
+        orgpu::launch_global(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw, ctx->d_sched, S(stream),
+                             ctx->sm_count);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "global tracking launch");
 }
 

@@ -76,9 +76,16 @@ static __device__ void sagitta_st1(float x0, float tx, float y0, float ty, int d
     }
 }
 
+// Work units are (event, group of GL_CHUNK slots), taken from a device
+// counter: slots are independent in the reference (one thread each, state
+// kept per thread), and the cost per event is very uneven, so warps that
+// finish early keep taking units instead of idling behind a heavy event.
+constexpr int GL_CHUNK = 8;
+
 __global__ void __launch_bounds__(GL_WARPS * 32)
     global_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
-                  const uint8_t *__restrict__ toomany, int n_events, uint32_t *__restrict__ errw) {
+                  const uint8_t *__restrict__ toomany, int n_events, uint32_t *__restrict__ errw,
+                  unsigned long long *__restrict__ sched) {
     extern __shared__ __align__(16) unsigned char gl_smem[];
     or_plane_t &P = *reinterpret_cast<or_plane_t *>(gl_smem);
     GlWarp *warps = reinterpret_cast<GlWarp *>(gl_smem + ((sizeof(or_plane_t) + 15) & ~size_t(15)));
@@ -90,11 +97,18 @@ __global__ void __launch_bounds__(GL_WARPS * 32)
     // station-1 planes x x' u u' v v' (K:1880-1923, E1039 chamber ids)
     const short dl[6] = {4, 3, 2, 1, 6, 5};
 
-    for (long e = (long)blockIdx.x * GL_WARPS + w; e < n_events; e += (long)gridDim.x * GL_WARPS) {
+    const unsigned long long nunits = (unsigned long long)n_events * (OR_NSLOTS / GL_CHUNK);
+    for (;;) {
+        unsigned long long u = 0;
+        if (lane == 0) u = atomicAdd(sched, 1ull);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= nunits) break;
+        const long e = (long)(u / (OR_NSLOTS / GL_CHUNK));
+        const int slot0 = (int)(u % (OR_NSLOTS / GL_CHUNK)) * GL_CHUNK;
         if (toomany[e]) continue;
         HitPlane hc[6];
         for (int k = 0; k < 6; ++k) hc[k] = hits_of(hv, e, dl[k]);
-        for (int slot = 0; slot < OR_NSLOTS; ++slot) {
+        for (int slot = slot0; slot < slot0 + GL_CHUNK; ++slot) {
             const int ntr = min((int)tv.ntracks[e * OR_NSLOTS + slot], OR_SLOTCAP);
             if (ntr == 0) continue;
             Stale stc[GL_NST];
@@ -471,15 +485,18 @@ __global__ void __launch_bounds__(GL_WARPS * 32)
 size_t global_smem_bytes() { return ((sizeof(or_plane_t) + 15) & ~size_t(15)) + sizeof(GlWarp) * GL_WARPS; }
 
 cudaError_t launch_global(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, const uint8_t *toomany,
-                          int n_events, uint32_t *errw, cudaStream_t stream, int sm_count) {
+                          int n_events, uint32_t *errw, unsigned long long *sched, cudaStream_t stream,
+                          int sm_count) {
     if (n_events <= 0) return cudaSuccess;
     const size_t smem = global_smem_bytes();
     cudaError_t err = cudaFuncSetAttribute(global_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return err;
-    long blocks = (n_events + GL_WARPS - 1) / GL_WARPS;
+    if ((err = cudaMemsetAsync(sched, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return err;
+    long blocks = ((long)n_events * (OR_NSLOTS / GL_CHUNK) + GL_WARPS - 1) / GL_WARPS;
     const long cap = (long)sm_count * 8;
     if (blocks > cap) blocks = cap;
-    global_kernel<<<(unsigned)blocks, GL_WARPS * 32, smem, stream>>>(d_plane, hv, tv, toomany, n_events, errw);
+    global_kernel<<<(unsigned)blocks, GL_WARPS * 32, smem, stream>>>(d_plane, hv, tv, toomany, n_events, errw,
+                                                                      sched);
     return cudaGetLastError();
 }
 

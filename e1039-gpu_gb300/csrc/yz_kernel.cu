@@ -40,9 +40,10 @@ namespace orgpu {
 constexpr int YZ_WARPS = 4;
 constexpr int YZ_MAXWIN = 100;          // windowed hits per plane (the reference's hitidx arrays)
 constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's hitpairs arrays)
-constexpr int YZ_ARENA_HITS = 224;      // windowed hits kept in shared memory per warp
+constexpr int YZ_ARENA_HITS = 192;      // windowed hits kept in shared memory per warp
 constexpr long YZ_LIGHT = 4096;         // combinations a planning warp evaluates itself per tracklet
-constexpr long YZ_EVENT_INLINE = 16384; // ... and per event
+constexpr long YZ_CHUNK_INLINE = 4096;  // ... and per planning unit
+constexpr int YZ_PLAN_CHUNK = 8;        // slots per planning unit
 constexpr long YZ_UNIT = 4096;          // combinations per queued unit (whole (u3,v3) iterations)
 constexpr int YZ_GARENA_HITS = 8 * YZ_MAXWIN;  // per-warp global overflow arena
 
@@ -85,7 +86,7 @@ struct YzScratch {
     YzUnit *units;
     YzHeavy *heavy;
     YzBest *best;
-    unsigned int *counters;  // [0] units reserved, [1] heavy reserved, [2] queue head
+    unsigned int *counters;  // [0] units reserved, [1] heavy reserved, [2] queue head, [4..5] planning units
     YzHit *garena;           // per-warp overflow arenas
     int cap_units, cap_heavy, garena_warps;
 };
@@ -819,7 +820,7 @@ __device__ __forceinline__ YzHit *yz_garena(const YzScratch &sc, int gwarp) {
     return sc.garena + (long)(gwarp % sc.garena_warps) * YZ_GARENA_HITS;
 }
 
-__global__ void __launch_bounds__(YZ_WARPS * 32)
+__global__ void __launch_bounds__(YZ_WARPS * 32, 4)
     yz_plan_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
                    const uint8_t *__restrict__ toomany, int n_events, YzScratch sc, uint32_t *__restrict__ errw) {
     extern __shared__ __align__(16) unsigned char yz_smem[];
@@ -832,10 +833,20 @@ __global__ void __launch_bounds__(YZ_WARPS * 32)
     YzWarp &S = warps[w];
     YzHit *garena = yz_garena(sc, blockIdx.x * YZ_WARPS + w);
 
-    for (long e = (long)blockIdx.x * YZ_WARPS + w; e < n_events; e += (long)gridDim.x * YZ_WARPS) {
+    // planning units (event, YZ_PLAN_CHUNK slots) from a device counter: slots
+    // are independent (one reference thread each), events very uneven
+    const unsigned long long nplan = (unsigned long long)n_events * (OR_NSLOTS / YZ_PLAN_CHUNK);
+    unsigned long long *plan_ctr = reinterpret_cast<unsigned long long *>(sc.counters + 4);
+    for (;;) {
+        unsigned long long pu = 0;
+        if (lane == 0) pu = atomicAdd(plan_ctr, 1ull);
+        pu = __shfl_sync(0xffffffffu, pu, 0);
+        if (pu >= nplan) break;
+        const long e = (long)(pu / (OR_NSLOTS / YZ_PLAN_CHUNK));
+        const int slot0 = (int)(pu % (OR_NSLOTS / YZ_PLAN_CHUNK)) * YZ_PLAN_CHUNK;
         if (toomany[e]) continue;  // K:873-878
-        long budget = YZ_EVENT_INLINE;
-        for (int slot = 0; slot < OR_NSLOTS; ++slot) {
+        long budget = YZ_CHUNK_INLINE;
+        for (int slot = slot0; slot < slot0 + YZ_PLAN_CHUNK; ++slot) {
             const int ntr = min((int)tv.ntracks[e * OR_NSLOTS + slot], OR_SLOTCAP);
             if (ntr == 0) continue;
             const int st3 = 3 + (slot & 1);  // K:884
@@ -1014,7 +1025,7 @@ cudaError_t launch_yz(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_vi
     sc.garena_warps = garena_warps;
     if ((err = cudaMemsetAsync(sc.counters, 0, 256, stream))) return err;
     const long blocks = garena_warps / YZ_WARPS;
-    const long blocks_plan = min((long)(n_events + YZ_WARPS - 1) / YZ_WARPS, blocks);
+    const long blocks_plan = min(((long)n_events * (OR_NSLOTS / YZ_PLAN_CHUNK) + YZ_WARPS - 1) / YZ_WARPS, blocks);
     yz_plan_kernel<<<(unsigned)blocks_plan, YZ_WARPS * 32, smem, stream>>>(d_plane, hv, tv, toomany, n_events, sc,
                                                                            errw);
     if ((err = cudaGetLastError())) return err;
