@@ -21,6 +21,22 @@ cudaError_t launch_pack(const or_hit_record_t *, const int64_t *, int, const flo
                         int);
 cudaError_t launch_collect(or_tracks_view_t, const uint8_t *, int, float, float *, long long, unsigned long long *,
                            cudaStream_t);
+cudaError_t launch_yz_pruned(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
+                             void *, int, int, int, cudaStream_t, int, const int32_t *, const uint8_t *, long);
+cudaError_t launch_rows(const uint16_t *, const uint8_t *, int, int32_t *, cudaStream_t);
+cudaError_t launch_features(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int,
+                            const int32_t *, float *, long, cudaStream_t, int);
+cudaError_t launch_keep(const float *, const int32_t *, int, float, float, uint8_t *, long, cudaStream_t, int);
+cudaError_t launch_mlp_score(const or_mlp_t *, const float *, long, const int32_t *, float *, uint32_t *, cudaStream_t,
+                             int);
+int mlp_train_blocks(int);
+cudaError_t launch_labels(or_tracks_view_t, const uint8_t *, int, const int32_t *, uint8_t *, long, cudaStream_t, int);
+cudaError_t launch_agreement(or_tracks_view_t, or_tracks_view_t, const uint8_t *, int, unsigned long long *,
+                             cudaStream_t, int);
+cudaError_t launch_mlp_train(const or_mlp_t *, const float *, const uint8_t *, const int64_t *, int, float, float *,
+                             float *, float *, cudaStream_t);
+cudaError_t launch_mlp_adam(float *, float *, float *, const float *, int, int, float, float, float, float, or_mlp_t *,
+                            cudaStream_t);
 cudaError_t launch_yz_noalloc(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
                               cudaStream_t, const char **);
 }  // namespace orgpu
@@ -254,6 +270,149 @@ int or_run_batch(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, in
     if ((rc = or_event_reduce(ctx, hits, toomany, n_events, stream))) return rc;
     if ((rc = or_xz(ctx, hits, tracks, ntracklets, toomany, n_events, stream))) return rc;
     if ((rc = or_yz(ctx, hits, tracks, toomany, n_events, stream))) return rc;
+    if ((rc = or_back_clean(ctx, tracks, toomany, n_events, stream))) return rc;
+    return or_global(ctx, hits, tracks, toomany, n_events, stream);
+}
+
+/* ---- learned tracklet scorer ------------------------------------------- */
+
+int or_tracklet_rows(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, int32_t *row_off,
+                     void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany || !row_off) return fail(OR_ERR_ARG, "bad event count, flags or row offsets");
+    if ((rc = check_tracks(tracks))) return rc;
+    cudaError_t e = orgpu::launch_rows(tracks.ntracks, toomany, n_events, row_off, S(stream));
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "tracklet rows");
+}
+
+int or_tracklet_features(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany,
+                         int n_events, const int32_t *row_off, float *features, int64_t max_rows, void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany || !row_off || !features || max_rows < 0)
+        return fail(OR_ERR_ARG, "bad feature arguments");
+    if (!aligned16(features)) return fail(OR_ERR_ARG, "feature rows must be 16-byte aligned");
+    if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
+    cudaError_t e =
+        orgpu::launch_features(ctx->d_plane, hits, tracks, toomany, n_events, row_off, features, (long)max_rows,
+                               S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "tracklet features");
+}
+
+int or_mlp_score(or_ctx_t *ctx, const or_mlp_t *model, const float *features, int64_t n_rows, float *scores,
+                 void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n_rows < 0 || !model || !features || !scores) return fail(OR_ERR_ARG, "bad scorer arguments");
+    if (!aligned16(features)) return fail(OR_ERR_ARG, "feature rows must be 16-byte aligned");
+    cudaError_t e =
+        orgpu::launch_mlp_score(model, features, (long)n_rows, nullptr, scores, ctx->d_errw, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "scorer inference");
+}
+
+int or_keep_mask(or_ctx_t *ctx, const float *scores, const int32_t *row_off, int n_events, float t_keep, float t_unc,
+                 uint8_t *keep, int64_t max_rows, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n_events < 0 || !scores || !row_off || !keep || max_rows < 0)
+        return fail(OR_ERR_ARG, "bad keep-mask arguments");
+    cudaError_t e =
+        orgpu::launch_keep(scores, row_off, n_events, t_keep, t_unc, keep, (long)max_rows, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "keep mask");
+}
+
+int or_yz_pruned(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany, int n_events,
+                 const int32_t *row_off, const uint8_t *keep, int64_t max_rows, void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany || !row_off || !keep || max_rows < 0)
+        return fail(OR_ERR_ARG, "bad pruned-YZ arguments");
+    if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
+    cudaError_t e = orgpu::launch_yz_pruned(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw, ctx->yz_scratch,
+                                            ctx->yz_cap_units, ctx->yz_cap_heavy, ctx->yz_garena_warps, S(stream),
+                                            ctx->sm_count, row_off, keep, (long)max_rows);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "pruned YZ launch");
+}
+
+int or_tracklet_labels(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events,
+                       const int32_t *row_off, uint8_t *labels, int64_t max_rows, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany || !row_off || !labels || max_rows < 0) return fail(OR_ERR_ARG, "bad label arguments");
+    if ((rc = check_tracks(tracks))) return rc;
+    cudaError_t e =
+        orgpu::launch_labels(tracks, toomany, n_events, row_off, labels, (long)max_rows, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "tracklet labels");
+}
+
+int or_track_agreement(or_ctx_t *ctx, or_tracks_view_t tracks_a, or_tracks_view_t tracks_b, const uint8_t *toomany,
+                       int n_events, uint64_t *counts, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany || !counts) return fail(OR_ERR_ARG, "bad agreement arguments");
+    if ((rc = check_tracks(tracks_a)) || (rc = check_tracks(tracks_b))) return rc;
+    cudaError_t e = orgpu::launch_agreement(tracks_a, tracks_b, toomany, n_events,
+                                            reinterpret_cast<unsigned long long *>(counts), S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "track agreement");
+}
+
+int or_mlp_grad_blocks(int batch) { return batch > 0 ? orgpu::mlp_train_blocks(batch) : 0; }
+
+int or_mlp_forward(or_ctx_t *ctx, const or_mlp_t *model, const float *features, const int64_t *idx, int n,
+                   float *prob, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n < 0 || !model || !features || !idx || !prob) return fail(OR_ERR_ARG, "bad forward arguments");
+    cudaError_t e = orgpu::launch_mlp_train(model, features, nullptr, idx, n, 1.f, nullptr, nullptr, prob, S(stream));
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "scorer forward");
+}
+
+int or_mlp_gradient(or_ctx_t *ctx, const or_mlp_t *model, const float *features, const uint8_t *labels,
+                    const int64_t *idx, int batch, float pos_weight, float *grad_part, float *loss_part, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (batch < 0 || !model || !features || !labels || !idx || !grad_part || !loss_part)
+        return fail(OR_ERR_ARG, "bad gradient arguments");
+    cudaError_t e = orgpu::launch_mlp_train(model, features, labels, idx, batch, pos_weight, grad_part, loss_part,
+                                            nullptr, S(stream));
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "scorer gradient");
+}
+
+int or_mlp_adam(or_ctx_t *ctx, float *param, float *m1, float *m2, const float *grad_part, int nblocks, int step,
+                float lr, float beta1, float beta2, float eps, or_mlp_t *model, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (!param || !m1 || !m2 || !grad_part || !model || nblocks < 1 || step < 1)
+        return fail(OR_ERR_ARG, "bad Adam arguments");
+    cudaError_t e =
+        orgpu::launch_mlp_adam(param, m1, m2, grad_part, nblocks, step, lr, beta1, beta2, eps, model, S(stream));
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "scorer Adam step");
+}
+
+int or_run_batch_learned(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, int32_t *ntracklets,
+                         uint8_t *toomany, int n_events, const or_mlp_t *model, float t_keep, float t_unc,
+                         int32_t *row_off, float *features, float *scores, uint8_t *keep, int64_t max_rows,
+                         void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany || !ntracklets || !model || !row_off || !features || !scores || !keep ||
+        max_rows < 0)
+        return fail(OR_ERR_ARG, "bad learned-batch arguments");
+    if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
+    cudaError_t e = cudaMemsetAsync(ntracklets, 0, sizeof(int32_t) * (size_t)n_events, S(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "clear tracklet counts");
+    if ((rc = or_event_reduce(ctx, hits, toomany, n_events, stream))) return rc;
+    if ((rc = or_xz(ctx, hits, tracks, ntracklets, toomany, n_events, stream))) return rc;
+    if ((rc = or_tracklet_rows(ctx, tracks, toomany, n_events, row_off, stream))) return rc;
+    if ((rc = or_tracklet_features(ctx, hits, tracks, toomany, n_events, row_off, features, max_rows, stream)))
+        return rc;
+    // the row count stays on the device: the scorer reads it from row_off[n]
+    cudaError_t e2 = orgpu::launch_mlp_score(model, features, (long)max_rows, row_off + n_events, scores, ctx->d_errw,
+                                             S(stream), ctx->sm_count);
+    if (e2 != cudaSuccess) return cuda_fail(e2, "scorer inference");
+    if ((rc = or_keep_mask(ctx, scores, row_off, n_events, t_keep, t_unc, keep, max_rows, stream))) return rc;
+    if ((rc = or_yz_pruned(ctx, hits, tracks, toomany, n_events, row_off, keep, max_rows, stream))) return rc;
     if ((rc = or_back_clean(ctx, tracks, toomany, n_events, stream))) return rc;
     return or_global(ctx, hits, tracks, toomany, n_events, stream);
 }

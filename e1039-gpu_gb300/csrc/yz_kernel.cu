@@ -91,6 +91,13 @@ struct YzScratch {
     int cap_units, cap_heavy, garena_warps;
 };
 
+// optional pruning: tracklet rows (row_off, as the scorer's) and keep flags
+struct YzPrune {
+    const int32_t *row_off;
+    const uint8_t *keep;  // nullptr: plain
+    long max_rows;
+};
+
 struct PassEntryStore {
     int c;
     float y0, ty, ey0, ety, stpos, stdrift;
@@ -822,7 +829,8 @@ __device__ __forceinline__ YzHit *yz_garena(const YzScratch &sc, int gwarp) {
 
 __global__ void __launch_bounds__(YZ_WARPS * 32, 4)
     yz_plan_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
-                   const uint8_t *__restrict__ toomany, int n_events, YzScratch sc, uint32_t *__restrict__ errw) {
+                   const uint8_t *__restrict__ toomany, int n_events, YzScratch sc, uint32_t *__restrict__ errw,
+                   YzPrune prune) {
     extern __shared__ __align__(16) unsigned char yz_smem[];
     or_plane_t &P = *reinterpret_cast<or_plane_t *>(yz_smem);
     YzWarp *warps = reinterpret_cast<YzWarp *>(yz_smem + ((sizeof(or_plane_t) + 15) & ~size_t(15)));
@@ -846,8 +854,15 @@ __global__ void __launch_bounds__(YZ_WARPS * 32, 4)
         const int slot0 = (int)(pu % (OR_NSLOTS / YZ_PLAN_CHUNK)) * YZ_PLAN_CHUNK;
         if (toomany[e]) continue;  // K:873-878
         long budget = YZ_CHUNK_INLINE;
+        long row = 0;  // scorer row of the next tracklet (slots in order, tracklets in slot order)
+        if (prune.keep) {
+            row = prune.row_off[e];
+            for (int s = 0; s < slot0; ++s) row += min((int)tv.ntracks[e * OR_NSLOTS + s], OR_SLOTCAP);
+        }
         for (int slot = slot0; slot < slot0 + YZ_PLAN_CHUNK; ++slot) {
             const int ntr = min((int)tv.ntracks[e * OR_NSLOTS + slot], OR_SLOTCAP);
+            const long slot_row = row;
+            row += ntr;
             if (ntr == 0) continue;
             const int st3 = 3 + (slot & 1);  // K:884
             YzEvent E;
@@ -865,9 +880,21 @@ __global__ void __launch_bounds__(YZ_WARPS * 32, 4)
                 }
                 const int nu2 = S.np[0], nv2 = S.np[1], nu3 = S.np[2], nv3 = S.np[3];
                 if (nu2 == 0 || nu3 == 0 || nv2 == 0 || nv3 == 0) continue;
-                yz_xhits(S, T, P);
                 const long C2 = (long)nu2 * nv2;
                 const long G = (long)nu3 * nv3;
+                if (prune.keep) {
+                    const long r = slot_row + it;
+                    if (r < prune.max_rows && !prune.keep[r]) {
+                        // pruned: no combination is evaluated, as when none
+                        // passes; the scratch entries still advance over its
+                        // load pattern so later tracklets of the slot see the
+                        // plain state
+                        yz_unit_states(S, base, (int)G, 1, st, nullptr, 0);
+                        __syncwarp();
+                        continue;
+                    }
+                }
+                yz_xhits(S, T, P);
                 const long C = G * C2;
                 bool inline_it = C <= YZ_LIGHT && C <= budget;
                 if (!inline_it) {
@@ -998,9 +1025,9 @@ size_t yz_scratch_bytes(int cap_units, int cap_heavy, int garena_warps) {
     return b + sizeof(YzHit) * YZ_GARENA_HITS * (size_t)garena_warps;
 }
 
-cudaError_t launch_yz(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, const uint8_t *toomany,
-                      int n_events, uint32_t *errw, void *scratch, int cap_units, int cap_heavy, int garena_warps,
-                      cudaStream_t stream, int sm_count) {
+static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
+                                  const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
+                                  int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, YzPrune prune) {
     if (n_events <= 0) return cudaSuccess;
     const size_t smem = yz_smem_bytes();
     cudaError_t err;
@@ -1027,12 +1054,29 @@ cudaError_t launch_yz(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_vi
     const long blocks = garena_warps / YZ_WARPS;
     const long blocks_plan = min(((long)n_events * (OR_NSLOTS / YZ_PLAN_CHUNK) + YZ_WARPS - 1) / YZ_WARPS, blocks);
     yz_plan_kernel<<<(unsigned)blocks_plan, YZ_WARPS * 32, smem, stream>>>(d_plane, hv, tv, toomany, n_events, sc,
-                                                                           errw);
+                                                                           errw, prune);
     if ((err = cudaGetLastError())) return err;
     yz_work_kernel<<<(unsigned)blocks, YZ_WARPS * 32, smem, stream>>>(d_plane, hv, tv, sc);
     if ((err = cudaGetLastError())) return err;
     yz_apply_kernel<<<(unsigned)(sm_count * 4), 128, 0, stream>>>(tv, sc);
     return cudaGetLastError();
+}
+
+cudaError_t launch_yz(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, const uint8_t *toomany,
+                      int n_events, uint32_t *errw, void *scratch, int cap_units, int cap_heavy, int garena_warps,
+                      cudaStream_t stream, int sm_count) {
+    return launch_yz_impl(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
+                          sm_count, YzPrune{nullptr, nullptr, 0});
+}
+
+// YZ with the scorer's keep flags: pruned tracklets are left as tracklets no
+// combination extends; kept ones get the plain result
+cudaError_t launch_yz_pruned(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
+                             const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
+                             int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count,
+                             const int32_t *row_off, const uint8_t *keep, long max_rows) {
+    return launch_yz_impl(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
+                          sm_count, YzPrune{row_off, keep, max_rows});
 }
 
 }  // namespace orgpu

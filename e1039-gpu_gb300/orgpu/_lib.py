@@ -17,7 +17,10 @@ OR_OK, OR_ERR_ARG, OR_ERR_CUDA, OR_ERR_IO, OR_ERR_NOMEM, OR_ERR_CAPACITY, OR_ERR
 EXPORTS = ("or_version", "or_last_error", "or_status_string", "or_geometry_load", "or_create", "or_destroy",
            "or_set_geometry", "or_stream_sync", "or_event_reduce", "or_xz", "or_yz", "or_back_clean", "or_global",
            "or_run_batch", "or_hits_view_from_collection", "or_tracks_view_from_collection", "or_hits_view_bytes",
-           "or_tracks_view_bytes", "or_pack_hits", "or_collect_tracks", "or_yz_noalloc")
+           "or_tracks_view_bytes", "or_pack_hits", "or_collect_tracks", "or_yz_noalloc", "or_tracklet_rows",
+           "or_tracklet_features", "or_mlp_score", "or_keep_mask", "or_yz_pruned", "or_run_batch_learned",
+           "or_tracklet_labels", "or_track_agreement", "or_mlp_grad_blocks", "or_mlp_forward", "or_mlp_gradient",
+           "or_mlp_adam")
 
 OR_YZ_NOALLOC_MAX_EVENTS = 10000
 OR_ERRW_CAPACITY = 2
@@ -68,6 +71,20 @@ def lib():
     lb.or_pack_hits.argtypes = [vp, vp, vp, C.c_int, vp, L.OrHitsView, vp]
     lb.or_collect_tracks.argtypes = [vp, L.OrTracksView, vp, C.c_int, C.c_float, vp, C.c_int64, vp, vp]
     lb.or_yz_noalloc.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, C.c_int, vp, vp]
+    i64, f32, i32 = C.c_int64, C.c_float, C.c_int
+    lb.or_tracklet_rows.argtypes = [vp, L.OrTracksView, vp, i32, vp, vp]
+    lb.or_tracklet_features.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, i32, vp, vp, i64, vp]
+    lb.or_mlp_score.argtypes = [vp, vp, vp, i64, vp, vp]
+    lb.or_keep_mask.argtypes = [vp, vp, vp, i32, f32, f32, vp, i64, vp]
+    lb.or_yz_pruned.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, i32, vp, vp, i64, vp]
+    lb.or_run_batch_learned.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, vp, i32, vp, f32, f32, vp, vp, vp, vp,
+                                        i64, vp]
+    lb.or_tracklet_labels.argtypes = [vp, L.OrTracksView, vp, i32, vp, vp, i64, vp]
+    lb.or_track_agreement.argtypes = [vp, L.OrTracksView, L.OrTracksView, vp, i32, vp, vp]
+    lb.or_mlp_grad_blocks.argtypes = [i32]
+    lb.or_mlp_forward.argtypes = [vp, vp, vp, vp, i32, vp, vp]
+    lb.or_mlp_gradient.argtypes = [vp, vp, vp, vp, vp, i32, f32, vp, vp, vp]
+    lb.or_mlp_adam.argtypes = [vp, vp, vp, vp, vp, i32, i32, f32, f32, f32, f32, vp, vp]
     for name in EXPORTS:
         getattr(lb, name)
     _lib = lb

@@ -78,6 +78,18 @@ class OrTracksView(C.Structure):
     _fields_ = [("ntracks", C.c_void_p), ("tracks", C.c_void_p)]
 
 
+NFEAT, MLP_H = 16, 64
+MLP_NPARAM = MLP_H * NFEAT + MLP_H + MLP_H * MLP_H + MLP_H + MLP_H + 1
+
+
+class OrMlp(C.Structure):
+    """or_mlp_t: the learned scorer's model as the kernels read it."""
+    _fields_ = [("mean", C.c_float * NFEAT), ("inv_std", C.c_float * NFEAT),
+                ("w1", C.c_uint16 * (MLP_H * NFEAT)), ("b1", C.c_float * MLP_H),
+                ("w2", C.c_uint16 * (MLP_H * MLP_H)), ("b2", C.c_float * MLP_H),
+                ("w3", C.c_float * MLP_H), ("b3", C.c_float), ("pad", C.c_float * 3)]
+
+
 HIT_RECORD_DTYPE = np.dtype([("det", "<i2"), ("elem", "<i2"), ("tdc", "<f4"),
                              ("drift", "<f4"), ("flag", "<i4")])
 assert HIT_RECORD_DTYPE.itemsize == 16

@@ -116,6 +116,64 @@ int or_pack_hits(or_ctx_t *ctx, const or_hit_record_t *records, const int64_t *r
 int or_collect_tracks(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, float stid,
                       float *out, int64_t capacity, uint64_t *d_count, void *stream);
 
+/* ---- learned tracklet scorer (no counterpart in the reference) ----------
+ *
+ * A 16-64-64-1 MLP (or_mlp_t, BF16 weights and activations, FP32 sums)
+ * scores every XZ tracklet; the YZ combinatorics of low-scoring tracklets
+ * are skipped.  Rows: tracklet r of event e is row row_off[e] + its rank in
+ * the event (slots in order, tracklets in slot order); flagged events own no
+ * rows; row_off has n_events+1 entries, row_off[n_events] = total rows.
+ * Buffers of max_rows rows: rows past max_rows get no features or scores
+ * and are always kept. */
+int or_tracklet_rows(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, int32_t *row_off,
+                     void *stream);
+/* OR_NFEAT floats per row (16-byte aligned): x0/100, 10 tx, err_x0,
+ * 100 err_tx, log1p(hits in the eight u/v planes), x-hit count, station-3
+ * half, log1p of the windowed and of the accepted u2, v2, u3, v3 hits, and
+ * the sum of the last four logs. */
+int or_tracklet_features(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany,
+                         int n_events, const int32_t *row_off, float *features, int64_t max_rows, void *stream);
+/* Scores (sigmoid outputs) of n_rows feature rows on the tensor cores
+ * (tcgen05, 128 rows per tile). */
+int or_mlp_score(or_ctx_t *ctx, const or_mlp_t *model, const float *features, int64_t n_rows, float *scores,
+                 void *stream);
+/* keep[r] = score >= t_keep, except that an event with any score in
+ * [t_unc, t_keep) keeps all of its rows (it is re-run plain). */
+int or_keep_mask(or_ctx_t *ctx, const float *scores, const int32_t *row_off, int n_events, float t_keep, float t_unc,
+                 uint8_t *keep, int64_t max_rows, void *stream);
+/* or_yz with the keep flags: a pruned tracklet is left as one no
+ * combination extends (stationID 3); kept tracklets get or_yz's result. */
+int or_yz_pruned(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany, int n_events,
+                 const int32_t *row_off, const uint8_t *keep, int64_t max_rows, void *stream);
+/* or_run_batch with the scorer between XZ and YZ; the row count stays on the
+ * device. */
+int or_run_batch_learned(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, int32_t *ntracklets,
+                         uint8_t *toomany, int n_events, const or_mlp_t *model, float t_keep, float t_unc,
+                         int32_t *row_off, float *features, float *scores, uint8_t *keep, int64_t max_rows,
+                         void *stream);
+/* Training labels: 1 for the rows whose tracklet ended as a global track
+ * (stationID 6) in the run that left `tracks`. */
+int or_tracklet_labels(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events,
+                       const int32_t *row_off, uint8_t *labels, int64_t max_rows, void *stream);
+/* Recall of run b against run a on the same events: counts[0] = global
+ * tracks of a, counts[1] = those with the identical record in b, counts[2] =
+ * global tracks of b (device uint64[3]). */
+int or_track_agreement(or_ctx_t *ctx, or_tracks_view_t tracks_a, or_tracks_view_t tracks_b, const uint8_t *toomany,
+                       int n_events, uint64_t *counts, void *stream);
+/* Training (CUDA cores, same rounding points as or_mlp_score): forward of the
+ * rows idx[0..n); per-block partial gradients of the mean weighted binary
+ * cross-entropy over a batch (or_mlp_grad_blocks(batch) blocks of
+ * OR_MLP_NPARAM floats, parameter order w1, b1, w2, b2, w3, b3) and per-block
+ * loss sums; an Adam step on the FP32 parameters that also refreshes the
+ * model's BF16 copies. */
+int or_mlp_grad_blocks(int batch);
+int or_mlp_forward(or_ctx_t *ctx, const or_mlp_t *model, const float *features, const int64_t *idx, int n,
+                   float *prob, void *stream);
+int or_mlp_gradient(or_ctx_t *ctx, const or_mlp_t *model, const float *features, const uint8_t *labels,
+                    const int64_t *idx, int batch, float pos_weight, float *grad_part, float *loss_part, void *stream);
+int or_mlp_adam(or_ctx_t *ctx, float *param, float *m1, float *m2, const float *grad_part, int nblocks, int step,
+                float lr, float beta1, float beta2, float eps, or_mlp_t *model, void *stream);
+
 /* YZ tracklet stage that allocates nothing and needs no context.  This entry
  * point has no counterpart in the reference, whose host code allocates all of
  * its device memory up front (online_reconstruction.cu:738-744).

@@ -57,6 +57,24 @@ extern "C" {
 #define OR_EVT_TRK_FLOATS (OR_TRKMAX * OR_NTRKPARAM) /* 75776 */
 #define OR_MAXHITS_PER_TRACK 18
 
+/* learned tracklet scorer: 16 features per XZ tracklet, MLP 16-64-64-1
+ * (BF16 weights and activations, FP32 accumulation, sigmoid output) */
+#define OR_NFEAT 16
+#define OR_MLP_H 64
+typedef struct or_mlp {
+    float mean[OR_NFEAT];               /* input normalisation: (x - mean) * inv_std */
+    float inv_std[OR_NFEAT];
+    uint16_t w1[OR_MLP_H * OR_NFEAT];   /* bf16 bits, [out][in] */
+    float b1[OR_MLP_H];
+    uint16_t w2[OR_MLP_H * OR_MLP_H];   /* bf16 bits, [out][in] */
+    float b2[OR_MLP_H];
+    float w3[OR_MLP_H];
+    float b3;
+    float pad[3];
+} or_mlp_t;
+/* trainable parameters in FP32, in this order: w1, b1, w2, b2, w3, b3 */
+#define OR_MLP_NPARAM (OR_MLP_H * OR_NFEAT + OR_MLP_H + OR_MLP_H * OR_MLP_H + OR_MLP_H + OR_MLP_H + 1)
+
 /* wire-position table row stride: wire_pos[det*400 + element]
  * (online_reconstruction.cu:191) */
 #define OR_WIREPOS_STRIDE 400

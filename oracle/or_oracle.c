@@ -1704,6 +1704,86 @@ static void global_event(const or_plane_t *P, or_hits_view_t hv, or_tracks_view_
 /* ------------------------------------------------------------------------ */
 /* threaded drivers                                                         */
 /* ------------------------------------------------------------------------ */
+/* ------------------------------------------------------------------------ */
+/* learned-scorer inputs: the 16 features of every XZ tracklet               */
+/* ------------------------------------------------------------------------ */
+/* Rows: tracklets of the accepted events in event, slot, position order.
+ * Windows as YZ builds them (K:1252-1283, H:480-511); accepted = the
+ * calculate_y_uvhit test (H:75-100) with no sign. */
+int64_t orc_tracklet_features(const or_plane_t *P, or_hits_view_t hv, or_tracks_view_t tv, const uint8_t *toomany,
+                              int n_events, int32_t *row_off, float *feat, int64_t max_rows) {
+    int64_t row = 0;
+    for (long e = 0; e < n_events; e++) {
+        row_off[e] = (int32_t)row;
+        if (toomany[e]) continue;
+        for (int slot = 0; slot < OR_NSLOTS; slot++) {
+            const int st3 = 3 + slot % 2;
+            short dl[8];
+            const int stids[4] = {2, 2, st3, st3}, projs[4] = {1, 2, 1, 2};
+            for (int q = 0; q < 4; q++) {
+                int d = detsuperid[stids[q]][projs[q]] * 2;
+                dl[2 * q] = (short)d;
+                dl[2 * q + 1] = (short)(d - 1);
+            }
+            int ntr = tv.ntracks[e * OR_NSLOTS + slot];
+            if (ntr > OR_SLOTCAP) ntr = OR_SLOTCAP;
+            for (int it = 0; it < ntr; it++, row++) {
+                const float *T = trk_rec(tv, e, slot, it);
+                const float x0 = T[OR_TRK_X0], tx = T[OR_TRK_TX], ex0 = T[OR_TRK_ERR_X0], etx = T[OR_TRK_ERR_TX];
+                int nwin[4], nacc[4], nall = 0;
+                for (int q = 0; q < 4; q++) {
+                    const int a = 2 * q;
+                    const float za = P->z[dl[a]], zb = P->z[dl[a + 1]];
+                    const float sp = P->spacing[dl[a]];
+                    const float xmin = fminf((tx - etx) * za, (tx - etx) * zb) + x0 - ex0 - sp;
+                    const float xmax = fmaxf((tx + etx) * za, (tx + etx) * zb) + x0 + ex0 + sp;
+                    int cw = 0, ca = 0;
+                    for (int side = 0; side < 2; side++) {
+                        const int det = dl[a + side];
+                        hitcoll_t h = hits_chamber(hv, e, det);
+                        nall += h.n;
+                        for (int i = 0; i < h.n; i++) {
+                            const int el = (int)hc_chan(h, i);
+                            float p1x, p2x;
+                            if (P->deltapx[det] > 0) {
+                                p1x = x_bep(det, el, P);
+                                p2x = x_tep(det, el, P);
+                            } else {
+                                p1x = x_tep(det, el, P);
+                                p2x = x_bep(det, el, P);
+                            }
+                            if (!((p1x <= xmax) && (p2x >= xmin))) continue;
+                            cw++;
+                            float yy, ey;
+                            if (calculate_y_uvhit(det, el, hc_drift(h, i), 0, x0, tx, P, &yy, &ey)) ca++;
+                        }
+                    }
+                    nwin[q] = cw;
+                    nacc[q] = ca;
+                }
+                if (row < max_rows) {
+                    float *f = feat + row * OR_NFEAT;
+                    f[0] = x0 * 0.01f;
+                    f[1] = tx * 10.f;
+                    f[2] = ex0;
+                    f[3] = etx * 100.f;
+                    f[4] = log1pf((float)nall);
+                    f[5] = T[OR_TRK_NHITS];
+                    f[6] = (float)(slot & 1);
+                    for (int q = 0; q < 4; q++) {
+                        f[7 + q] = log1pf((float)nwin[q]);
+                        f[11 + q] = log1pf((float)nacc[q]);
+                    }
+                    f[15] = log1pf((float)nacc[0]) + log1pf((float)nacc[1]) + log1pf((float)nacc[2]) +
+                            log1pf((float)nacc[3]);
+                }
+            }
+        }
+    }
+    row_off[n_events] = (int32_t)row;
+    return row;
+}
+
 int orc_hardware_threads(void) {
     long n = sysconf(_SC_NPROCESSORS_ONLN);
     return n > 0 ? (int)n : 1;

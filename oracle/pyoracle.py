@@ -62,6 +62,9 @@ def lib():
         _lib.orc_reduce_plane.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         _lib.orc_reduce_plane.restype = C.c_int
         _lib.orc_hardware_threads.restype = C.c_int
+        _lib.orc_tracklet_features.argtypes = [P(L.OrPlane), L.OrHitsView, L.OrTracksView, C.c_void_p, C.c_int,
+                                               C.c_void_p, C.c_void_p, C.c_int64]
+        _lib.orc_tracklet_features.restype = C.c_int64
     return _lib
 
 
@@ -113,6 +116,19 @@ def run_all(plane, hits, tracks, state, n_threads=0, counted=False):
     else:
         lib().orc_run_all(C.byref(plane), hits.view(), tracks.view(), state.ntracklets.ctypes.data,
                           state.toomany.ctypes.data, state.status.ctypes.data, hits.n, n_threads)
+
+
+def tracklet_features(plane, hits, tracks, toomany, max_rows=None):
+    """(row_off [n+1], features [rows, 16]) of the tracklets in `tracks`
+    (the state after XZ)."""
+    n = hits.n
+    cap = int(max_rows if max_rows is not None else n * L.TRKMAX)
+    row_off = np.zeros(n + 1, np.int32)
+    feat = np.zeros((max(cap, 1), L.NFEAT), np.float32)
+    rows = lib().orc_tracklet_features(C.byref(plane), hits.view(), tracks.view(),
+                                       np.ascontiguousarray(toomany, np.uint8).ctypes.data, n, row_off.ctypes.data,
+                                       feat.ctypes.data, cap)
+    return row_off, feat[:min(rows, cap)]
 
 
 def hardware_threads():
