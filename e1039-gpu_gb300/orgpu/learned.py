@@ -242,9 +242,10 @@ class Trainer:
         self.dev = dev
 
     def epoch(self, rng):
+        """One pass over the rows in a random order; returns the mean batch loss."""
         torch = _torch()
         perm = torch.from_numpy(rng.permutation(self.n).astype(np.int64)).to(self.dev)
-        total = 0.0
+        total = torch.zeros((), dtype=torch.float32, device=self.dev)
         nb = 0
         for s in range(0, self.n - self.batch + 1, self.batch):
             idx = perm[s:s + self.batch]
@@ -256,9 +257,9 @@ class Trainer:
             _lib.check(self.lib.or_mlp_adam(self.ctx, self.param.data_ptr(), self.m1.data_ptr(), self.m2.data_ptr(),
                                             self.grad.data_ptr(), self.nblk, self.step_no, float(self.lr), 0.9, 0.999,
                                             1e-8, self.model.ptr(), self.stream), "or_mlp_adam")
-            total += float(self.loss.sum().item()) if (nb % 50 == 0) else 0.0
+            total += self.loss.sum()
             nb += 1
-        return total
+        return float(total.item()) / max(nb, 1)
 
     def result(self):
         return ScorerParams(self.param.cpu().numpy(), self.sp.mean, self.sp.inv_std, self.sp.t_keep, self.sp.t_unc,

@@ -188,3 +188,46 @@ def test_training_reduces_loss(env):
     p, _ = M.forward(res.params, res.mean, res.inv_std, X[:4096])
     acc = np.mean((p > 0.5) == (y[:4096] == 1))
     assert acc > 0.95
+
+
+def _plain_and_learned(env, sp, n, seed, cfg_name="small"):
+    import torch
+    from orgpu import learned, pipeline, synth as S
+    plane, hits0, snap, rc, lr = env
+    from oracle import pyoracle as O
+    from orgpu import GEOMETRY_E906
+    _, wp = O.parse_geometry(GEOMETRY_E906)
+    geo = S.Geometry(plane, wp)
+    cfg = S.config_small(n, seed) if cfg_name == "small" else S.config_uneven(n, seed)
+    rec, off, _ = S.generate(geo, cfg)
+    rec, off = S.cap_records(rec, off)
+    h = S.pack(rec, off, geo.wire_pos_f32())
+    bp = pipeline.DeviceBatch(n)
+    bl = pipeline.DeviceBatch(n)
+    bp.upload_hits(h)
+    bl.upload_hits(h)
+    rc.run_batch(bp)
+    r = learned.TrackletRows(n)
+    lr.run_batch(bl, r, learned.DeviceModel(sp), sp.t_keep, sp.t_unc)
+    rc.sync()
+    return lr.agreement(bp, bl), r
+
+
+def test_learned_batch_keep_all_equals_plain(env):
+    from orgpu import learned
+    sp = learned.ScorerParams.load()
+    sp.t_keep = sp.t_unc = 0.0  # every score >= 0: nothing pruned
+    (n_ref, n_match, n_new), r = _plain_and_learned(env, sp, 600, 77)
+    assert n_ref > 300 and n_match == n_ref == n_new
+    assert int(r.keep[:r.n_rows()].sum()) == r.n_rows()
+
+
+def test_committed_scorer_recall_small_events(env):
+    """The committed model at its own threshold keeps >= 99.5 % of the plain
+    global tracks of one-dimuon events (held-out seed)."""
+    from orgpu import learned
+    sp = learned.ScorerParams.load()
+    (n_ref, n_match, n_new), r = _plain_and_learned(env, sp, 3000, 424242)
+    assert n_ref > 2000
+    assert n_match / n_ref >= 0.995
+    assert int(r.keep[:r.n_rows()].sum()) < r.n_rows()  # something was pruned
