@@ -30,6 +30,8 @@ cudaError_t launch_keep(const float *, const int32_t *, int, float, float, uint8
 cudaError_t launch_mlp_score(const or_mlp_t *, const float *, long, const int32_t *, float *, uint32_t *, cudaStream_t,
                              int);
 int mlp_train_blocks(int);
+cudaError_t launch_select(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, int, int,
+                          cudaStream_t, int);
 cudaError_t launch_labels(or_tracks_view_t, const uint8_t *, int, const int32_t *, uint8_t *, long, cudaStream_t, int);
 cudaError_t launch_agreement(or_tracks_view_t, or_tracks_view_t, const uint8_t *, int, unsigned long long *,
                              cudaStream_t, int);
@@ -272,6 +274,39 @@ int or_run_batch(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, in
     if ((rc = or_yz(ctx, hits, tracks, toomany, n_events, stream))) return rc;
     if ((rc = or_back_clean(ctx, tracks, toomany, n_events, stream))) return rc;
     return or_global(ctx, hits, tracks, toomany, n_events, stream);
+}
+
+/* ---- post-global selection ---------------------------------------------- */
+
+int or_prop_matching(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany,
+                     int n_events, void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
+    if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
+    cudaError_t e = orgpu::launch_select(ctx->d_plane, hits, tracks, toomany, n_events, 1, 0, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "prop segment matching");
+}
+
+int or_global_clean(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
+    if ((rc = check_tracks(tracks))) return rc;
+    or_hits_view_t none;
+    std::memset(&none, 0, sizeof(none));
+    cudaError_t e = orgpu::launch_select(ctx->d_plane, none, tracks, toomany, n_events, 0, 1, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "global track cleaning");
+}
+
+int or_run_selection(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany,
+                     int n_events, void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
+    if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
+    cudaError_t e = orgpu::launch_select(ctx->d_plane, hits, tracks, toomany, n_events, 1, 1, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "post-global selection");
 }
 
 /* ---- learned tracklet scorer ------------------------------------------- */

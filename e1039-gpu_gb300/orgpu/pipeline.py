@@ -149,6 +149,19 @@ class Reconstruction:
         _lib.check(self.lib.or_global(self.ctx, b.hits_view(), b.tracks_view(), b.toomany.data_ptr(), b.n,
                                       self._stream(stream)), "or_global")
 
+    # post-global selection (online_reconstruction.cu:914-933)
+    def prop_segment_matching(self, b, stream=None):
+        _lib.check(self.lib.or_prop_matching(self.ctx, b.hits_view(), b.tracks_view(), b.toomany.data_ptr(), b.n,
+                                             self._stream(stream)), "or_prop_matching")
+
+    def global_track_cleaning(self, b, stream=None):
+        _lib.check(self.lib.or_global_clean(self.ctx, b.tracks_view(), b.toomany.data_ptr(), b.n,
+                                            self._stream(stream)), "or_global_clean")
+
+    def selection(self, b, stream=None):
+        _lib.check(self.lib.or_run_selection(self.ctx, b.hits_view(), b.tracks_view(), b.toomany.data_ptr(), b.n,
+                                             self._stream(stream)), "or_run_selection")
+
     def run_batch(self, b, stream=None):
         _lib.check(self.lib.or_run_batch(self.ctx, b.hits_view(), b.tracks_view(), b.ntracklets.data_ptr(),
                                          b.toomany.data_ptr(), b.n, self._stream(stream)), "or_run_batch")

@@ -90,6 +90,19 @@ int or_global(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const
 int or_run_batch(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, int32_t *ntracklets,
                  uint8_t *toomany, int n_events, void *stream);
 
+/* Post-global selection (online_reconstruction.cu:914-933), after or_global:
+ *   or_prop_matching  <- gKernel_PropSegmentMatching     reconstruction_helper.cuh:1916
+ *                        (every track without an x and a y prop-tube segment
+ *                        agreeing with it gets stationID 5)
+ *   or_global_clean   <- gKernel_GlobalTrackCleaning and ..._crossthreads  :2289, :2333
+ *                        (chi2/ndf and same-charge momentum duplicates)
+ *   or_run_selection  <- both, one launch. */
+int or_prop_matching(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany,
+                     int n_events, void *stream);
+int or_global_clean(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, void *stream);
+int or_run_selection(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany,
+                     int n_events, void *stream);
+
 /* Map the reference's fixed-capacity structs (EstnEvtMax = 10000 events)
  * onto views.  `coll` points at a gEventHitCollections / gEventTrackCollection
  * laid out exactly as reconstruction_classes.cuh:76-87 / :542-544. */

@@ -1705,6 +1705,148 @@ static void global_event(const or_plane_t *P, or_hits_view_t hv, or_tracks_view_
 /* threaded drivers                                                         */
 /* ------------------------------------------------------------------------ */
 /* ------------------------------------------------------------------------ */
+/* post-global selection, H:1916-2380                                        */
+/* ------------------------------------------------------------------------ */
+#define SEL_CHI2DOF_MAX 250.f  /* K0:194 */
+#define SEL_MERGE_THRES 0.015f /* K0:196 */
+
+/* H:1995-2131 (x) and H:2137-2273 (y): is there a prop-tube segment (a hit
+ * of the first station within win1 of the track, one of the second within
+ * win2) whose line agrees with the track?  The reference's loops only set a
+ * flag, so the answer is an existence test over (p1a then p1b) x (p2a then
+ * p2b). */
+static int prop_segment(float x0, float tx, hitcoll_t p1a, float z1a, hitcoll_t p1b, float z1b, hitcoll_t p2a,
+                        float z2a, hitcoll_t p2b, float z2b, float win1, float win2, float slope_max,
+                        float inter_max) {
+    const float cut = 0.03f; /* H:1992, H:2000 */
+    for (int s1 = 0; s1 < 2; s1++) {
+        hitcoll_t h1 = s1 ? p1b : p1a;
+        const float z1 = s1 ? z1b : z1a;
+        for (int n = 0; n < h1.n; n++) {
+            const float ipos1 = hc_pos(h1, n);
+            if (!(fabsf(ipos1 - (tx * z1 + x0)) < win1)) continue;
+            for (int s2 = 0; s2 < 2; s2++) {
+                hitcoll_t h2 = s2 ? p2b : p2a;
+                const float z2 = s2 ? z2b : z2a;
+                for (int m = 0; m < h2.n; m++) {
+                    const float ipos2 = hc_pos(h2, m);
+                    if (fabsf(ipos2 - (tx * z2 + x0)) > win2) continue;
+                    const float a = (ipos2 - ipos1) / (z2 - z1);
+                    if (fabsf(a) > slope_max) continue;
+                    if (fabsf(a - tx) > cut) continue;
+                    const float b = ipos1 - a * z1;
+                    if (fabsf(b) > inter_max) continue;
+                    if (fabsf((tx * 2028.19f + x0) - (a * 2028.19f + b)) > 3.0f) continue;
+                    return 1;
+                }
+            }
+        }
+    }
+    return 0;
+}
+
+/* gKernel_PropSegmentMatching, H:1916-2277: every track of the slot (any
+ * stationID) without an x and a y prop-tube segment gets stationID 5 */
+static void prop_match_event(const or_plane_t *P, or_hits_view_t hv, or_tracks_view_t tv, long e,
+                             const uint8_t *toomany) {
+    if (toomany[e]) return;
+    const int px1 = detsuperid[5][0] * 2, px2 = detsuperid[6][0] * 2; /* 50/49, 52/51 */
+    const int py1 = detsuperid[5][1] * 2, py2 = detsuperid[6][1] * 2; /* 48/47, 54/53 */
+    hitcoll_t p1x1 = hits_prop(hv, e, px1), p1x2 = hits_prop(hv, e, px1 - 1);
+    hitcoll_t p2x1 = hits_prop(hv, e, px2), p2x2 = hits_prop(hv, e, px2 - 1);
+    hitcoll_t p1y1 = hits_prop(hv, e, py1), p1y2 = hits_prop(hv, e, py1 - 1);
+    hitcoll_t p2y1 = hits_prop(hv, e, py2), p2y2 = hits_prop(hv, e, py2 - 1);
+    for (int slot = 0; slot < OR_NSLOTS; slot++) {
+        const int n = tv.ntracks[e * OR_NSLOTS + slot];
+        for (int i = 0; i < n; i++) {
+            float *T = trk_rec(tv, e, slot, i);
+            const float x0 = T[OR_TRK_X0], y0 = T[OR_TRK_Y0], tx = T[OR_TRK_TX], ty = T[OR_TRK_TY];
+            if (!prop_segment(x0, tx, p1x1, P->z[px1], p1x2, P->z[px1 - 1], p2x1, P->z[px2], p2x2, P->z[px2 - 1],
+                              5.08f, 7.62f, TX_MAX, X0_MAX)) {
+                T[OR_TRK_STID] = 5.f;
+                continue;
+            }
+            if (!prop_segment(y0, ty, p1y1, P->z[py1], p1y2, P->z[py1 - 1], p2y1, P->z[py2], p2y2, P->z[py2 - 1],
+                              5.08f, 10.16f, TY_MAX, Y0_MAX))
+                T[OR_TRK_STID] = 5.f;
+        }
+    }
+}
+
+/* gKernel_GlobalTrackCleaning, H:2289-2331, each slot on its own.  The else
+ * branch compares invP(i) with itself (H:2323), so it demotes i whenever the
+ * charges agree. */
+static void gclean_event(or_tracks_view_t tv, long e, const uint8_t *toomany) {
+    if (toomany[e]) return;
+    for (int s = 0; s < OR_NSLOTS; s++) {
+        const int n = tv.ntracks[e * OR_NSLOTS + s];
+        for (int i = 0; i < n; i++) {
+            float *Ti = trk_rec(tv, e, s, i);
+            if (Ti[OR_TRK_STID] < 6) continue;
+            if (Ti[OR_TRK_CHI2] / (Ti[OR_TRK_NHITS] - 5) > SEL_CHI2DOF_MAX) {
+                Ti[OR_TRK_STID] = 5.f;
+                continue;
+            }
+            for (int j = i + 1; j < n; j++) {
+                float *Tj = trk_rec(tv, e, s, j);
+                if (Tj[OR_TRK_STID] < 6) continue;
+                if (Ti[OR_TRK_CHI2] / (Ti[OR_TRK_NHITS] - 5) < Tj[OR_TRK_CHI2] / (Tj[OR_TRK_NHITS] - 5)) {
+                    if ((Ti[OR_TRK_INVP] - Tj[OR_TRK_INVP]) / Ti[OR_TRK_INVP] < SEL_MERGE_THRES &&
+                        Ti[OR_TRK_CHARGE] * Tj[OR_TRK_CHARGE] > 0)
+                        Tj[OR_TRK_STID] = 5.f;
+                } else {
+                    if ((Ti[OR_TRK_INVP] - Ti[OR_TRK_INVP]) / Tj[OR_TRK_INVP] < SEL_MERGE_THRES &&
+                        Ti[OR_TRK_CHARGE] * Tj[OR_TRK_CHARGE] > 0)
+                        Ti[OR_TRK_STID] = 5.f;
+                }
+            }
+        }
+    }
+}
+
+/* gKernel_GlobalTrackCleaning_crossthreads, H:2333-2380, the block's 32
+ * threads in lockstep as in clean_cross_event: at each step (i_trd, i, j)
+ * the demotions (stationID = 5) land after every thread has decided. */
+static void gclean_cross_event(or_tracks_view_t tv, long e, const uint8_t *toomany) {
+    if (toomany[e]) return;
+    int nt[OR_NSLOTS], maxn = 0;
+    for (int t = 0; t < OR_NSLOTS; t++) {
+        nt[t] = tv.ntracks[e * OR_NSLOTS + t];
+        if (nt[t] > maxn) maxn = nt[t];
+    }
+    for (int u = 0; u < OR_NSLOTS; u++) {
+        const int m = nt[u];
+        for (int i = 0; i < maxn; i++) {
+            int act[OR_NSLOTS];
+            for (int t = 0; t < OR_NSLOTS; t++)
+                act[t] = t != u && i < nt[t] && trk_rec(tv, e, t, i)[OR_TRK_STID] >= 6;
+            for (int j = 0; j < m; j++) {
+                float *Tj = trk_rec(tv, e, u, j);
+                if (Tj[OR_TRK_STID] < 6) continue;
+                int demote_j = 0, demote_i[OR_NSLOTS];
+                for (int t = 0; t < OR_NSLOTS; t++) {
+                    demote_i[t] = 0;
+                    if (!act[t]) continue;
+                    const float *Ti = trk_rec(tv, e, t, i);
+                    if (Ti[OR_TRK_CHI2] / (Ti[OR_TRK_NHITS] - 5) < Tj[OR_TRK_CHI2] / (Tj[OR_TRK_NHITS] - 5)) {
+                        if ((Ti[OR_TRK_INVP] - Tj[OR_TRK_INVP]) / Ti[OR_TRK_INVP] < SEL_MERGE_THRES &&
+                            Ti[OR_TRK_CHARGE] * Tj[OR_TRK_CHARGE] > 0)
+                            demote_j = 1;
+                    } else {
+                        if ((Ti[OR_TRK_INVP] - Tj[OR_TRK_INVP]) / Tj[OR_TRK_INVP] < SEL_MERGE_THRES &&
+                            Ti[OR_TRK_CHARGE] * Tj[OR_TRK_CHARGE] > 0)
+                            demote_i[t] = 1;
+                    }
+                }
+                if (demote_j) Tj[OR_TRK_STID] = 5.f;
+                for (int t = 0; t < OR_NSLOTS; t++)
+                    if (demote_i[t]) trk_rec(tv, e, t, i)[OR_TRK_STID] = 5.f;
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* learned-scorer inputs: the 16 features of every XZ tracklet               */
 /* ------------------------------------------------------------------------ */
 /* Rows: tracklets of the accepted events in event, slot, position order.
@@ -1789,7 +1931,7 @@ int orc_hardware_threads(void) {
     return n > 0 ? (int)n : 1;
 }
 
-enum { ST_ER, ST_XZ, ST_YZ, ST_CLEAN, ST_CLEANX, ST_GLOBAL, ST_ALL };
+enum { ST_ER, ST_XZ, ST_YZ, ST_CLEAN, ST_CLEANX, ST_GLOBAL, ST_ALL, ST_PROP, ST_GCLEAN, ST_GCLEANX };
 
 typedef struct {
     int stage;
@@ -1823,6 +1965,9 @@ static void *worker(void *arg) {
         case ST_CLEAN: clean_event(j->t, e, j->toomany); break;
         case ST_CLEANX: clean_cross_event(j->t, e, j->toomany); break;
         case ST_GLOBAL: global_event(j->P, j->h, j->t, e, j->toomany, ps, c); break;
+        case ST_PROP: prop_match_event(j->P, j->h, j->t, e, j->toomany); break;
+        case ST_GCLEAN: gclean_event(j->t, e, j->toomany); break;
+        case ST_GCLEANX: gclean_cross_event(j->t, e, j->toomany); break;
         case ST_ALL:
             er_event(j->h, e, j->toomany, j->status);
             xz_event(j->P, j->h, j->t, e, j->ntkl, j->toomany, j->status, xs, c);
@@ -1893,6 +2038,18 @@ void orc_global(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, const
                 int n_threads) {
     run_stage(ST_GLOBAL, p, h, t, NULL, (uint8_t *)toomany, NULL, NULL, n_events, n_threads);
 }
+void orc_prop_matching(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, const uint8_t *toomany,
+                       int n_events, int n_threads) {
+    run_stage(ST_PROP, p, h, t, NULL, (uint8_t *)toomany, NULL, NULL, n_events, n_threads);
+}
+
+void orc_global_clean(or_tracks_view_t t, const uint8_t *toomany, int n_events, int n_threads) {
+    or_hits_view_t h;
+    memset(&h, 0, sizeof(h));
+    run_stage(ST_GCLEAN, NULL, h, t, NULL, (uint8_t *)toomany, NULL, NULL, n_events, n_threads);
+    run_stage(ST_GCLEANX, NULL, h, t, NULL, (uint8_t *)toomany, NULL, NULL, n_events, n_threads);
+}
+
 void orc_run_all(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, int32_t *ntracklets, uint8_t *toomany,
                  uint32_t *status, int n_events, int n_threads) {
     run_stage(ST_ALL, p, h, t, ntracklets, toomany, status, NULL, n_events, n_threads);

@@ -69,6 +69,13 @@ void orc_fit_2d_drift(int n, const float *x, const float *drift, const short *si
 void orc_matinv_2x2(const float *a, float *ainv);
 int orc_reduce_plane(const float *slot, int n, int detid, short *hitflag);
 
+/* post-global selection (online_reconstruction.cu:914-933):
+ * gKernel_PropSegmentMatching (reconstruction_helper.cuh:1916-2277), then
+ * gKernel_GlobalTrackCleaning and ..._crossthreads (:2289-2380) */
+void orc_prop_matching(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, const uint8_t *toomany,
+                       int n_events, int n_threads);
+void orc_global_clean(or_tracks_view_t t, const uint8_t *toomany, int n_events, int n_threads);
+
 /* the learned scorer's 16 features per XZ tracklet (row order of
  * or_tracklet_rows); returns the row count */
 int64_t orc_tracklet_features(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, const uint8_t *toomany,

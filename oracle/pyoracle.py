@@ -62,6 +62,8 @@ def lib():
         _lib.orc_reduce_plane.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         _lib.orc_reduce_plane.restype = C.c_int
         _lib.orc_hardware_threads.restype = C.c_int
+        _lib.orc_prop_matching.argtypes = [P(L.OrPlane), L.OrHitsView, L.OrTracksView, C.c_void_p, C.c_int, C.c_int]
+        _lib.orc_global_clean.argtypes = [L.OrTracksView, C.c_void_p, C.c_int, C.c_int]
         _lib.orc_tracklet_features.argtypes = [P(L.OrPlane), L.OrHitsView, L.OrTracksView, C.c_void_p, C.c_int,
                                                C.c_void_p, C.c_void_p, C.c_int64]
         _lib.orc_tracklet_features.restype = C.c_int64
@@ -106,6 +108,14 @@ def back_clean(tracks, state, n_threads=0):
 
 def global_tracking(plane, hits, tracks, state, n_threads=0):
     lib().orc_global(C.byref(plane), hits.view(), tracks.view(), state.toomany.ctypes.data, hits.n, n_threads)
+
+
+def prop_matching(plane, hits, tracks, state, n_threads=0):
+    lib().orc_prop_matching(C.byref(plane), hits.view(), tracks.view(), state.toomany.ctypes.data, hits.n, n_threads)
+
+
+def global_clean(tracks, state, n_threads=0):
+    lib().orc_global_clean(tracks.view(), state.toomany.ctypes.data, tracks.n, n_threads)
 
 
 def run_all(plane, hits, tracks, state, n_threads=0, counted=False):

@@ -37,6 +37,9 @@ KERNELS = {
     "clean": "_Z25gKernel_BackTrackCleaningP21gEventTrackCollectionPKb",
     "clean_x": "_Z38gKernel_BackTrackCleaning_crossthreadsP21gEventTrackCollectionPKb",
     "global": "_Z23gKernel_Global_trackingP20gEventHitCollectionsP21gEventTrackCollectionPK6gPlanePb",
+    "prop": "_Z27gKernel_PropSegmentMatchingP20gEventHitCollectionsP21gEventTrackCollectionPKfPKb",
+    "gclean": "_Z27gKernel_GlobalTrackCleaningP21gEventTrackCollectionPKb",
+    "gclean_x": "_Z40gKernel_GlobalTrackCleaning_crossthreadsP21gEventTrackCollectionPKb",
 }
 
 # byte offsets of the members of gEventHitCollections (4-byte members, no padding)
@@ -148,6 +151,14 @@ class RefKernels:
     def back_clean(self, n):
         self._launch("clean", n, 32, self.tracks.data_ptr(), self.flags.data_ptr())
         self._launch("clean_x", n, 32, self.tracks.data_ptr(), self.flags.data_ptr())
+
+    def selection(self, n):
+        """PropSegmentMatching (z = the plane's z array, its first member),
+        then GlobalTrackCleaning and ..._crossthreads (M:914-933)."""
+        self._launch("prop", n, 32, self.hits.data_ptr(), self.tracks.data_ptr(), self.plane.data_ptr(),
+                     self.flags.data_ptr())
+        self._launch("gclean", n, 32, self.tracks.data_ptr(), self.flags.data_ptr())
+        self._launch("gclean_x", n, 32, self.tracks.data_ptr(), self.flags.data_ptr())
 
     def global_tracking(self, n):
         self._launch("global", n, 32, self.hits.data_ptr(), self.tracks.data_ptr(), self.plane.data_ptr(),

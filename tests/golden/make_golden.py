@@ -12,6 +12,8 @@ the oracle's:
   YZ      gKernel_YZ_tracking on the oracle's XZ tracklets
   clean   gKernel_BackTrackCleaning + ..._crossthreads on the oracle's YZ output
   global  gKernel_Global_tracking on the oracle's cleaned tracks
+  sel     gKernel_PropSegmentMatching + gKernel_GlobalTrackCleaning{,_crossthreads}
+          on the oracle's global tracks
 
 The reference XZ kernel is not run (barriers in divergent code).  Events
 are first checked against the reference's array bounds with the oracle's
@@ -75,6 +77,10 @@ class Snap:
         self.tracks_clean = t.copy()
         O.global_tracking(plane, self.hits_er, t, st)
         self.tracks_global = t
+        ts = t.copy()
+        O.prop_matching(plane, self.hits_er, ts, st)
+        O.global_clean(ts, st)
+        self.tracks_sel = ts
         # domain counters from a counted run of the whole chain
         h2, t2, st2 = hits0.copy(), L.HostTracks(n), O.OracleState(n)
         O.run_all(plane, h2, t2, st2, counted=True)
@@ -128,6 +134,10 @@ def run_reference(rk, plane, snap, n):
     rk.global_tracking(n)
     out["t_global"] = time.time() - t0
     out["tracks_global"] = rk.get_tracks(n)
+    # post-global selection
+    rk.put_tracks(snap.tracks_global)
+    rk.selection(n)
+    out["tracks_sel"] = rk.get_tracks(n)
     return out
 
 
@@ -140,7 +150,8 @@ def compare(snap, ref, rtol):
     rep["er_flags"] = {"accepted_by_oracle": int((snap.toomany_er == 0).sum()),
                        "recomputed_vs_oracle_mismatch": int((flags_re != snap.toomany_er).sum()),
                        "reference_raw_vs_oracle_mismatch": int((flags_ref != snap.toomany_er).sum())}
-    for stage, want in (("yz", snap.tracks_yz), ("clean", snap.tracks_clean), ("global", snap.tracks_global)):
+    for stage, want in (("yz", snap.tracks_yz), ("clean", snap.tracks_clean), ("global", snap.tracks_global),
+                        ("sel", snap.tracks_sel)):
         a = G.compact_tracks(ref["tracks_" + stage], snap.toomany_xz)
         b = G.compact_tracks(want, snap.toomany_xz)
         r = G.compare_tracks(a, b, rtol)
@@ -211,7 +222,7 @@ def _subset(ref, idx):
     h = _take_hits(ref["hits_er"], idx)
     out["er_counts"], out["er_hits"] = G.compact_hits(h)
     out["er_flags"] = ref["flags_er"][idx]
-    for stage in ("yz", "clean", "global"):
+    for stage in ("yz", "clean", "global", "sel"):
         t = _take_tracks(ref["tracks_" + stage], idx)
         nt, w, r = G.compact_tracks(t)
         out[f"{stage}_ntracks"], out[f"{stage}_where"], out[f"{stage}_records"] = nt, w, r
@@ -242,7 +253,7 @@ def _summary(report):
                                 "flags_recomputed": r["er_flags"]["recomputed_vs_oracle_mismatch"],
                                 **{st: [r[st]["n_count_mismatch"], r[st]["n_discrete_mismatch"],
                                         r[st]["n_value_mismatch"], r[st]["max_rel_fit"]]
-                                   for st in ("yz", "clean", "global")}}
+                                   for st in ("yz", "clean", "global", "sel")}}
     return s
 
 

@@ -47,6 +47,11 @@ class Snapshots:
         self.tracks_clean = t.copy()
         O.global_tracking(plane, self.hits_er, t, self.state, n_threads)
         self.tracks_global = t
+        # post-global selection on a copy
+        ts = t.copy()
+        O.prop_matching(plane, self.hits_er, ts, self.state, n_threads)
+        O.global_clean(ts, self.state, n_threads)
+        self.tracks_sel = ts
 
 
 def hit_mismatches(a, b, max_report=10):

@@ -58,7 +58,8 @@ def test_fixture_covers_every_stage(golden):
     G, M, data = golden
     z, snap = data["small"]
     for v in ("fmad0", "fmad1"):
-        for key in ("er_counts", "er_hits", "er_flags", "yz_records", "clean_records", "global_records"):
+        for key in ("er_counts", "er_hits", "er_flags", "yz_records", "clean_records", "global_records",
+                    "sel_records"):
             assert f"small/{v}/{key}" in z
     assert snap.hits0.n >= 16
     assert int(z["small/fmad0/global_records"][:, 0].astype(int).tolist().count(6)) > 0
@@ -87,13 +88,14 @@ def test_event_reducer_flags_from_reference_counts(golden, name):
     np.testing.assert_array_equal(M.recomputed_flags(h), snap.toomany_er)
 
 
-@pytest.mark.parametrize("stage", ["yz", "clean", "global"])
+@pytest.mark.parametrize("stage", ["yz", "clean", "global", "sel"])
 @pytest.mark.parametrize("name", CONFIGS)
 def test_tracking_stages_bit_exact_fmad0(golden, name, stage):
     G, M, data = golden
     z, snap = data[name]
     ref = tuple(z[f"{name}/fmad0/{stage}_{k}"] for k in ("ntracks", "where", "records"))
-    want = {"yz": snap.tracks_yz, "clean": snap.tracks_clean, "global": snap.tracks_global}[stage]
+    want = {"yz": snap.tracks_yz, "clean": snap.tracks_clean, "global": snap.tracks_global,
+            "sel": snap.tracks_sel}[stage]
     r = G.compare_tracks(_masked(ref, snap.toomany_xz), G.compact_tracks(want, snap.toomany_xz), 0.0)
     assert r["count_mismatch"] == [] and r["value_mismatch"] == [], r
 
@@ -106,7 +108,8 @@ def test_tracking_stages_fmad1_band(golden, name):
     differing where contraction changed a chi2 ordering or a cut."""
     G, M, data = golden
     z, snap = data[name]
-    for stage, want in (("yz", snap.tracks_yz), ("clean", snap.tracks_clean), ("global", snap.tracks_global)):
+    for stage, want in (("yz", snap.tracks_yz), ("clean", snap.tracks_clean), ("global", snap.tracks_global),
+                        ("sel", snap.tracks_sel)):
         ref = tuple(z[f"{name}/fmad1/{stage}_{k}"] for k in ("ntracks", "where", "records"))
         r = G.compare_tracks(_masked(ref, snap.toomany_xz), G.compact_tracks(want, snap.toomany_xz), 1e-2,
                              resid_atol=0.02)

@@ -99,6 +99,27 @@ def test_global(setup):
     assert count_tracks(snap.tracks_global, 6) > 0
 
 
+def test_post_global_selection(setup):
+    import torch
+    from orgpu import pipeline
+    plane, geo, rec, off, hits0, snap, rc = setup
+    b = _batch(rc, hits0.n, pipeline)
+    b.upload_hits(snap.hits_er)
+    b.toomany.copy_(torch.from_numpy(snap.toomany_xz))
+    b.upload_tracks(snap.tracks_global)
+    rc.prop_segment_matching(b)
+    rc.global_track_cleaning(b)
+    rc.sync()
+    assert track_mismatches(b.download_tracks(), snap.tracks_sel, snap.toomany_xz) == []
+    # the fused launch gives the same
+    b.upload_tracks(snap.tracks_global)
+    rc.selection(b)
+    rc.sync()
+    assert track_mismatches(b.download_tracks(), snap.tracks_sel, snap.toomany_xz) == []
+    n6_before, n6_after = count_tracks(snap.tracks_global, 6), count_tracks(snap.tracks_sel, 6)
+    assert 0 < n6_after < n6_before
+
+
 def test_end_to_end(setup):
     from orgpu import pipeline
     plane, geo, rec, off, hits0, snap, rc = setup
