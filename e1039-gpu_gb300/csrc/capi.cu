@@ -71,7 +71,10 @@ inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 
 int check_ctx(or_ctx_t *ctx, bool need_geom) {
     if (!ctx) return fail(OR_ERR_ARG, "null context");
     if (need_geom && !ctx->has_geom) return fail(OR_ERR_NOGEOM, "no geometry set (or_set_geometry)");
-    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(OR_ERR_CUDA, "cudaSetDevice failed");
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) return fail(OR_ERR_CUDA, "cudaGetDevice failed");
+    if (cur != ctx->device && cudaSetDevice(ctx->device) != cudaSuccess)
+        return fail(OR_ERR_CUDA, "cudaSetDevice failed");
     return OR_OK;
 }
 int check_hits(const or_hits_view_t &h) {

@@ -489,7 +489,7 @@ cudaError_t launch_global(const or_plane_t *d_plane, or_hits_view_t hv, or_track
                           int sm_count) {
     if (n_events <= 0) return cudaSuccess;
     const size_t smem = global_smem_bytes();
-    cudaError_t err = cudaFuncSetAttribute(global_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t err = smem_attr_once((const void *)global_kernel, (int)smem);
     if (err != cudaSuccess) return err;
     if ((err = cudaMemsetAsync(sched, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return err;
     long blocks = ((long)n_events * (OR_NSLOTS / GL_CHUNK) + GL_WARPS - 1) / GL_WARPS;

@@ -398,7 +398,7 @@ cudaError_t launch_mlp_score(const or_mlp_t *model, const float *feat, long n_ro
                              float *score, uint32_t *errw, cudaStream_t stream, int sm_count) {
     if (n_rows <= 0) return cudaSuccess;
     const size_t smem = mlp_score_smem();
-    cudaError_t err = cudaFuncSetAttribute(mlp_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t err = smem_attr_once((const void *)mlp_score_kernel, (int)smem);
     if (err != cudaSuccess) return err;
     const long ntiles = (n_rows + MS_ROWS - 1) / MS_ROWS;
     long blocks = ntiles;
@@ -415,7 +415,7 @@ cudaError_t launch_mlp_train(const or_mlp_t *model, const float *feat, const uin
                              cudaStream_t stream) {
     if (batch <= 0) return cudaSuccess;
     const size_t smem = mlp_train_smem();
-    cudaError_t err = cudaFuncSetAttribute(mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t err = smem_attr_once((const void *)mlp_train_kernel, (int)smem);
     if (err != cudaSuccess) return err;
     mlp_train_kernel<<<(unsigned)mlp_train_blocks(batch), TR_ROWS, smem, stream>>>(model, feat, label, idx, batch,
                                                                                   pos_weight, grad_part, loss_part,

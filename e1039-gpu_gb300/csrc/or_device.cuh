@@ -12,6 +12,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <mutex>
 #include <stdint.h>
 
 #include "../../include/or_layout.h"
@@ -380,6 +381,25 @@ __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
 // highest set lane index of m, or -1
 __device__ __forceinline__ int last_lane(unsigned m) { return m ? 31 - __clz(m) : -1; }
+
+// Raise a kernel's dynamic shared-memory limit once per device; the
+// attribute persists, so later launches -- also those recorded into a CUDA
+// graph by stream capture -- make no further runtime calls for it.
+inline cudaError_t smem_attr_once(const void *func, int bytes) {
+    static std::mutex mu;
+    static const void *fn[64][32];
+    static int nfn[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    std::lock_guard<std::mutex> lock(mu);
+    for (int i = 0; i < nfn[dev]; ++i)
+        if (fn[dev][i] == func) return cudaSuccess;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess && nfn[dev] < 32) fn[dev][nfn[dev]++] = func;
+    return e;
+}
 
 // Error words the kernels raise (bounded waits, capacity overruns).
 enum : uint32_t {

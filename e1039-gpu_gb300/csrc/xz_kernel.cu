@@ -390,7 +390,7 @@ cudaError_t launch_xz(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_vi
                       uint8_t *toomany, int n_events, cudaStream_t stream, int sm_count) {
     if (n_events <= 0) return cudaSuccess;
     const size_t smem = xz_smem_bytes();
-    cudaError_t err = cudaFuncSetAttribute(xz_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t err = smem_attr_once((const void *)xz_kernel, (int)smem);
     if (err != cudaSuccess) return err;
     long blocks = (n_events + XZ_WARPS - 1) / XZ_WARPS;
     const long cap = (long)sm_count * 8;

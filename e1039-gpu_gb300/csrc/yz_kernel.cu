@@ -1031,9 +1031,9 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
     if (n_events <= 0) return cudaSuccess;
     const size_t smem = yz_smem_bytes();
     cudaError_t err;
-    if ((err = cudaFuncSetAttribute(yz_plan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+    if ((err = smem_attr_once((const void *)yz_plan_kernel, (int)smem)))
         return err;
-    if ((err = cudaFuncSetAttribute(yz_work_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+    if ((err = smem_attr_once((const void *)yz_work_kernel, (int)smem)))
         return err;
     char *p = static_cast<char *>(scratch);
     YzScratch sc;
