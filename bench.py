@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=906002)
     ap.add_argument("--cpu-sample", type=int, default=0, help="events in the CPU-baseline sample (0 = auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     return ap.parse_args()
 
 
@@ -315,6 +317,8 @@ def main():
         cpu = {"value": ns / dt, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": "first %d events of the workload, one pass, all host threads" % ns}
 
+    learned_res = None if args.no_learned else learned_leg(args, rc, b, rec, off, d_rec, d_off, d_wp, value, dev)
+    serving_res = None if args.no_serving else serving_leg(plane, wp)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no dataset)", "config": cj,
@@ -322,10 +326,92 @@ def main():
                     "h2d_bytes_per_step": int(rec.nbytes + off.nbytes),
                     "d2h_bytes_per_step": int(statistics.mean(d2h_bytes)) if d2h_bytes else 0},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-            "gpu_launches": len(stages) * args.steps,
+            "gpu_launches": LAUNCHES_PER_STEP * args.steps,
             "stage_ms": stage_ms,
-            "events_rejected_frac": float(toomany.mean()), "global_tracks_last_step": ntrk}
+            "events_rejected_frac": float(toomany.mean()), "global_tracks_last_step": ntrk,
+            "learned": learned_res, "serving": serving_res}
     print(json.dumps(line))
+
+
+# kernels one step launches: pack, event reducer, XZ, YZ plan/work/apply,
+# cleaning, global tracking
+LAUNCHES_PER_STEP = 8
+
+
+def learned_leg(args, rc, b_plain, rec, off, d_rec, d_off, d_wp, plain_value, dev):
+    """The learned path (scorer + pruned YZ) on the same batch: events/s,
+    and recall against the plain run of the last timed step."""
+    import torch
+    from orgpu import learned, pipeline
+    n = b_plain.n
+    sp = learned.ScorerParams.load()
+    lrn = learned.Learned(rc)
+    model = learned.DeviceModel(sp, dev.index)
+    r = learned.TrackletRows(n, device=dev.index)
+    bl = pipeline.DeviceBatch(n, dev.index)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        rc.pack(bl, d_rec, d_off, d_wp)
+        lrn.run_batch(bl, r, model, sp.t_keep, sp.t_unc)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    n_ref, n_match, n_new = lrn.agreement(b_plain, bl)
+    nr = r.n_rows()
+    rc.sync()
+    return {"value": n / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms, "plain_value": plain_value,
+            "ratio_vs_plain": (n / (ms / 1000.0)) / plain_value,
+            "recall": n_match / n_ref if n_ref else 1.0, "plain_global_tracks": n_ref,
+            "reproduced": n_match, "learned_global_tracks": n_new,
+            "kept_share": float(r.keep[:nr].float().mean().item()) if nr else 1.0,
+            "model": "e1039-gpu_gb300/data/scorer_e906.npz", "t_keep": sp.t_keep, "t_unc": sp.t_unc}
+
+
+def serving_leg(plane, wp, pool_events=40000, burst_s=4.0, seed=906005):
+    """Spill-structured Poisson arrivals of batches of U(1, 10000) one-dimuon
+    events (the learned-scorer / small-batch distribution) at three offered
+    loads, through the continuous-batching server: p50/p99 latency and
+    sustained events/s per load.  Each 4 s burst starts on an idle server:
+    the 56 s gap between spills is the drain."""
+    from orgpu import serving, synth as S
+    geo = S.Geometry(plane, wp)
+    rec, off, _ = S.generate(geo, S.config_small(pool_events, seed))
+    rec, off = S.cap_records(rec, off)
+    srv = serving.Server(plane, wp, slot_events=10000, max_slots=4, rec_per_event=400)
+    rng = np.random.default_rng(seed)
+
+    def take(n):
+        e0 = int(rng.integers(0, pool_events - n + 1))
+        r0 = off[e0]
+        return rec[r0:off[e0 + n]], (off[e0:e0 + n + 1] - r0).astype(np.int64)
+
+    # capacity: a saturating queue of full-size batches
+    cal = srv.serve([(0.0,) + take(10000) for _ in range(12)])
+    cap = serving.latency_stats(cal)["events_per_s"]
+    loads = {}
+    for frac in (0.5, 0.8, 1.1):
+        rate = frac * cap / 5000.5  # batches per second (mean batch 5000.5 events)
+        sched, t = [], 0.0
+        while True:
+            t += float(rng.exponential(1.0 / rate))
+            if t > burst_s:
+                break
+            sched.append((t,) + take(int(rng.integers(1, 10001))))
+        done = srv.serve(sched)
+        st = serving.latency_stats(done) if done else {}
+        st["offered_events_per_s"] = frac * cap
+        loads["%.1fx" % frac] = st
+    return {"slots": len(srv.slots), "slot_events": 10000, "graphs": True, "burst_s": burst_s,
+            "capacity_events_per_s": cap, "workload": "one dimuon + Poisson(150) noise per event", "loads": loads}
 
 
 if __name__ == "__main__":

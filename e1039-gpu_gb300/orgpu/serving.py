@@ -294,16 +294,16 @@ class Server:
         t0 = time.perf_counter()
         todo = collections.deque(sorted(schedule, key=lambda x: x[0]))
         out = []
-        while todo or self.step():
+        while True:
             now = time.perf_counter() - t0
             while todo and todo[0][0] <= now:
                 a, rec, off = todo.popleft()
                 out.append(self.submit(rec, off, arrival=t0 + a))
-            if not todo:
-                continue
-            if not any(s.stage is not None for s in self.slots) and not self.pending:
+            busy = self.step()
+            if not busy:
+                if not todo:
+                    break
                 time.sleep(max(0.0, min(todo[0][0] - now, 0.001)))
-        self.drain()
         return out
 
 
