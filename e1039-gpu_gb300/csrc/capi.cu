@@ -8,30 +8,32 @@
 #include "or_device.cuh"
 
 namespace orgpu {
-cudaError_t launch_event_reduce(or_hits_view_t, uint8_t *, int, uint32_t *, cudaStream_t, int);
+cudaError_t launch_event_reduce(or_hits_view_t, uint8_t *, int, uint32_t *, cudaStream_t, int, int);
 cudaError_t launch_xz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, int32_t *, uint8_t *, int, cudaStream_t,
-                      int);
+                      int, int);
+cudaError_t launch_yz_tuned(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
+                            void *, int, int, int, cudaStream_t, int, int);
 cudaError_t launch_yz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *, void *,
                       int, int, int, cudaStream_t, int);
 size_t yz_scratch_bytes(int, int, int);
-cudaError_t launch_back_clean(or_tracks_view_t, const uint8_t *, int, cudaStream_t, int);
+cudaError_t launch_back_clean(or_tracks_view_t, const uint8_t *, int, cudaStream_t, int, int);
 cudaError_t launch_global(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
-                          unsigned long long *, cudaStream_t, int);
+                          unsigned long long *, cudaStream_t, int, int);
 cudaError_t launch_pack(const or_hit_record_t *, const int64_t *, int, const float *, or_hits_view_t, cudaStream_t,
                         int);
 cudaError_t launch_collect(or_tracks_view_t, const uint8_t *, int, float, float *, long long, unsigned long long *,
                            cudaStream_t);
 cudaError_t launch_yz_pruned(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
-                             void *, int, int, int, cudaStream_t, int, const int32_t *, const uint8_t *, long);
+                             void *, int, int, int, cudaStream_t, int, const int32_t *, const uint8_t *, long, int);
 cudaError_t launch_rows(const uint16_t *, const uint8_t *, int, int32_t *, cudaStream_t);
 cudaError_t launch_features(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int,
-                            const int32_t *, float *, long, cudaStream_t, int);
+                            const int32_t *, float *, long, cudaStream_t, int, int);
 cudaError_t launch_keep(const float *, const int32_t *, int, float, float, uint8_t *, long, cudaStream_t, int);
 cudaError_t launch_mlp_score(const or_mlp_t *, const float *, long, const int32_t *, float *, uint32_t *, cudaStream_t,
                              int);
 int mlp_train_blocks(int);
 cudaError_t launch_select(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, int, int,
-                          cudaStream_t, int);
+                          cudaStream_t, int, int);
 cudaError_t launch_labels(or_tracks_view_t, const uint8_t *, int, const int32_t *, uint8_t *, long, cudaStream_t, int);
 cudaError_t launch_agreement(or_tracks_view_t, or_tracks_view_t, const uint8_t *, int, unsigned long long *,
                              cudaStream_t, int);
@@ -53,6 +55,7 @@ struct or_ctx {
     // YZ work queue: units of heavy tracklets, their best records, overflow arenas
     void *yz_scratch;
     int yz_cap_units, yz_cap_heavy, yz_garena_warps;
+    int warps[OR_K_COUNT];  // events (work units) per CTA of each tunable kernel
 };
 
 namespace {
@@ -120,6 +123,7 @@ int or_create(int device, or_ctx_t **out) {
     or_ctx_t *c = new or_ctx_t();
     c->device = device;
     c->has_geom = false;
+    for (int k = 0; k < OR_K_COUNT; ++k) c->warps[k] = 4;
     if ((e = cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) {
         delete c;
         return cuda_fail(e, "cudaDeviceGetAttribute");
@@ -153,6 +157,22 @@ int or_create(int device, or_ctx_t **out) {
     }
     *out = c;
     return OR_OK;
+}
+
+int or_set_launch(or_ctx_t *ctx, int kernel, int events_per_cta) {
+    if (!ctx) return fail(OR_ERR_ARG, "null context");
+    if (kernel < 0 || kernel >= OR_K_COUNT) return fail(OR_ERR_ARG, "unknown kernel id");
+    const int w = events_per_cta;
+    if (w != 1 && w != 2 && w != 4 && w != 8 && w != 16)
+        return fail(OR_ERR_ARG, "events per CTA must be 1, 2, 4, 8 or 16");
+    if (kernel == OR_K_XZ && w > 8) return fail(OR_ERR_ARG, "XZ takes at most 8 events per CTA (shared memory)");
+    ctx->warps[kernel] = w;
+    return OR_OK;
+}
+
+int or_get_launch(or_ctx_t *ctx, int kernel) {
+    if (!ctx || kernel < 0 || kernel >= OR_K_COUNT) return -1;
+    return ctx->warps[kernel];
 }
 
 int or_destroy(or_ctx_t *ctx) {
@@ -198,7 +218,8 @@ int or_event_reduce(or_ctx_t *ctx, or_hits_view_t hits, uint8_t *toomany, int n_
     if (rc) return rc;
     if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
     if ((rc = check_hits(hits))) return rc;
-    cudaError_t e = orgpu::launch_event_reduce(hits, toomany, n_events, ctx->d_errw, S(stream), ctx->sm_count);
+    cudaError_t e = orgpu::launch_event_reduce(hits, toomany, n_events, ctx->d_errw, S(stream), ctx->sm_count,
+                                               ctx->warps[OR_K_EVENT_REDUCE]);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "event reducer launch");
 }
 
@@ -209,7 +230,8 @@ int or_xz(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, int32_t *
     if (n_events < 0 || !toomany || !ntracklets) return fail(OR_ERR_ARG, "bad event count or output arrays");
     if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
     cudaError_t e =
-        orgpu::launch_xz(ctx->d_plane, hits, tracks, ntracklets, toomany, n_events, S(stream), ctx->sm_count);
+        orgpu::launch_xz(ctx->d_plane, hits, tracks, ntracklets, toomany, n_events, S(stream), ctx->sm_count,
+                         ctx->warps[OR_K_XZ]);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "XZ launch");
 }
 
@@ -219,9 +241,9 @@ int or_yz(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uin
     if (rc) return rc;
     if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
     if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
-    cudaError_t e = orgpu::launch_yz(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw, ctx->yz_scratch,
-                                     ctx->yz_cap_units, ctx->yz_cap_heavy, ctx->yz_garena_warps, S(stream),
-                                     ctx->sm_count);
+    cudaError_t e = orgpu::launch_yz_tuned(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw,
+                                           ctx->yz_scratch, ctx->yz_cap_units, ctx->yz_cap_heavy,
+                                           ctx->yz_garena_warps, S(stream), ctx->sm_count, ctx->warps[OR_K_YZ]);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "YZ launch");
 }
 
@@ -248,7 +270,8 @@ int or_back_clean(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany
     if (rc) return rc;
     if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
     if ((rc = check_tracks(tracks))) return rc;
-    cudaError_t e = orgpu::launch_back_clean(tracks, toomany, n_events, S(stream), ctx->sm_count);
+    cudaError_t e =
+        orgpu::launch_back_clean(tracks, toomany, n_events, S(stream), ctx->sm_count, ctx->warps[OR_K_BACK_CLEAN]);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "cleaning launch");
 }
 
@@ -260,7 +283,7 @@ int or_global(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const
     if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
     cudaError_t e =
         orgpu::launch_global(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw, ctx->d_sched, S(stream),
-                             ctx->sm_count);
+                             ctx->sm_count, ctx->warps[OR_K_GLOBAL]);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "global tracking launch");
 }
 
@@ -287,7 +310,8 @@ int or_prop_matching(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks
     if (rc) return rc;
     if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
     if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
-    cudaError_t e = orgpu::launch_select(ctx->d_plane, hits, tracks, toomany, n_events, 1, 0, S(stream), ctx->sm_count);
+    cudaError_t e = orgpu::launch_select(ctx->d_plane, hits, tracks, toomany, n_events, 1, 0, S(stream), ctx->sm_count,
+                                         ctx->warps[OR_K_SELECT]);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "prop segment matching");
 }
 
@@ -298,7 +322,8 @@ int or_global_clean(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *tooma
     if ((rc = check_tracks(tracks))) return rc;
     or_hits_view_t none;
     std::memset(&none, 0, sizeof(none));
-    cudaError_t e = orgpu::launch_select(ctx->d_plane, none, tracks, toomany, n_events, 0, 1, S(stream), ctx->sm_count);
+    cudaError_t e = orgpu::launch_select(ctx->d_plane, none, tracks, toomany, n_events, 0, 1, S(stream), ctx->sm_count,
+                                         ctx->warps[OR_K_SELECT]);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "global track cleaning");
 }
 
@@ -308,7 +333,8 @@ int or_run_selection(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks
     if (rc) return rc;
     if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
     if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
-    cudaError_t e = orgpu::launch_select(ctx->d_plane, hits, tracks, toomany, n_events, 1, 1, S(stream), ctx->sm_count);
+    cudaError_t e = orgpu::launch_select(ctx->d_plane, hits, tracks, toomany, n_events, 1, 1, S(stream), ctx->sm_count,
+                                         ctx->warps[OR_K_SELECT]);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "post-global selection");
 }
 
@@ -334,7 +360,7 @@ int or_tracklet_features(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tr
     if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
     cudaError_t e =
         orgpu::launch_features(ctx->d_plane, hits, tracks, toomany, n_events, row_off, features, (long)max_rows,
-                               S(stream), ctx->sm_count);
+                               S(stream), ctx->sm_count, ctx->warps[OR_K_FEATURES]);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "tracklet features");
 }
 
@@ -369,7 +395,7 @@ int or_yz_pruned(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, co
     if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
     cudaError_t e = orgpu::launch_yz_pruned(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw, ctx->yz_scratch,
                                             ctx->yz_cap_units, ctx->yz_cap_heavy, ctx->yz_garena_warps, S(stream),
-                                            ctx->sm_count, row_off, keep, (long)max_rows);
+                                            ctx->sm_count, row_off, keep, (long)max_rows, ctx->warps[OR_K_YZ]);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "pruned YZ launch");
 }
 

@@ -22,8 +22,6 @@
 
 namespace orgpu {
 
-constexpr int CL_WARPS = 4;
-
 // shared (detector, element) hits of A's hits found among B's, H:1810-1817
 __device__ __forceinline__ int common_hits(const float *A, int na, const float *B, int nb) {
     int acc = 0;
@@ -46,11 +44,12 @@ __device__ __forceinline__ int clean_decide(const float *Ti, int ni, const float
     return ((float)nc > (float)nj * 0.3333f) ? 2 : 0;
 }
 
-__global__ void __launch_bounds__(CL_WARPS * 32)
+template <int W>
+__global__ void __launch_bounds__(W * 32)
     clean_kernel(or_tracks_view_t tv, const uint8_t *__restrict__ toomany, int n_events) {
     const int w = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    for (long e = (long)blockIdx.x * CL_WARPS + w; e < n_events; e += (long)gridDim.x * CL_WARPS) {
+    for (long e = (long)blockIdx.x * W + w; e < n_events; e += (long)gridDim.x * W) {
         if (toomany[e]) continue;
         const int n_own = min((int)tv.ntracks[e * OR_NSLOTS + lane], OR_SLOTCAP);
         // --- pass 1: the lane's own slot (H:1789-1843) ------------------------
@@ -100,14 +99,26 @@ __global__ void __launch_bounds__(CL_WARPS * 32)
     }
 }
 
-cudaError_t launch_back_clean(or_tracks_view_t tv, const uint8_t *toomany, int n_events, cudaStream_t stream,
-                              int sm_count) {
-    if (n_events <= 0) return cudaSuccess;
-    long blocks = (n_events + CL_WARPS - 1) / CL_WARPS;
-    const long cap = (long)sm_count * 16;
+template <int W>
+static cudaError_t clean_launch(or_tracks_view_t tv, const uint8_t *toomany, int n_events, cudaStream_t stream,
+                                int sm_count) {
+    long blocks = (n_events + W - 1) / W;
+    const long cap = (long)sm_count * (64 / W);
     if (blocks > cap) blocks = cap;
-    clean_kernel<<<(unsigned)blocks, CL_WARPS * 32, 0, stream>>>(tv, toomany, n_events);
+    clean_kernel<W><<<(unsigned)blocks, W * 32, 0, stream>>>(tv, toomany, n_events);
     return cudaGetLastError();
+}
+
+cudaError_t launch_back_clean(or_tracks_view_t tv, const uint8_t *toomany, int n_events, cudaStream_t stream,
+                              int sm_count, int warps) {
+    if (n_events <= 0) return cudaSuccess;
+    switch (warps) {
+    case 1: return clean_launch<1>(tv, toomany, n_events, stream, sm_count);
+    case 2: return clean_launch<2>(tv, toomany, n_events, stream, sm_count);
+    case 8: return clean_launch<8>(tv, toomany, n_events, stream, sm_count);
+    case 16: return clean_launch<16>(tv, toomany, n_events, stream, sm_count);
+    default: return clean_launch<4>(tv, toomany, n_events, stream, sm_count);
+    }
 }
 
 }  // namespace orgpu

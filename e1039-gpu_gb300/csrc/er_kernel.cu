@@ -17,7 +17,6 @@
 
 namespace orgpu {
 
-constexpr int ER_WARPS = 4;
 constexpr int ER_BUF_FLOATS = 2048;                 // 8 KB staging buffer per warp
 constexpr int ER_MAX_STAGED_HITS = ER_BUF_FLOATS / 5 + 8;
 constexpr int ER_NPLANES = 48;
@@ -157,9 +156,11 @@ static __device__ int er_reduce_plane(const float *h, int n, int det, uint8_t *k
     return nred;
 }
 
-__global__ void __launch_bounds__(ER_WARPS * 32) er_kernel(or_hits_view_t hv, uint8_t *__restrict__ toomany,
-                                                           int n_events, uint32_t *__restrict__ errw) {
-    __shared__ ErWarp sm[ER_WARPS];
+template <int W>
+__global__ void __launch_bounds__(W * 32) er_kernel(or_hits_view_t hv, uint8_t *__restrict__ toomany, int n_events,
+                                                    uint32_t *__restrict__ errw) {
+    extern __shared__ __align__(16) unsigned char er_smem[];
+    ErWarp *sm = reinterpret_cast<ErWarp *>(er_smem);
     const int w = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     ErWarp &S = sm[w];
@@ -167,7 +168,7 @@ __global__ void __launch_bounds__(ER_WARPS * 32) er_kernel(or_hits_view_t hv, ui
     __syncwarp();
     uint32_t phase = 0;
 
-    for (long e = (long)blockIdx.x * ER_WARPS + w; e < n_events; e += (long)gridDim.x * ER_WARPS) {
+    for (long e = (long)blockIdx.x * W + w; e < n_events; e += (long)gridDim.x * W) {
         for (int p = lane; p < ER_NPLANES; p += 32) {
             const PlaneRef r = er_plane(hv, e, c_er_det[p]);
             const int n = (int)*r.count;
@@ -242,14 +243,30 @@ __global__ void __launch_bounds__(ER_WARPS * 32) er_kernel(or_hits_view_t hv, ui
 }
 
 // Host launcher.
-cudaError_t launch_event_reduce(or_hits_view_t hv, uint8_t *toomany, int n_events, uint32_t *errw,
-                                cudaStream_t stream, int sm_count) {
-    if (n_events <= 0) return cudaSuccess;
-    long blocks = (n_events + ER_WARPS - 1) / ER_WARPS;
-    const long cap = (long)sm_count * 12;
+template <int W>
+static cudaError_t er_launch(or_hits_view_t hv, uint8_t *toomany, int n_events, uint32_t *errw, cudaStream_t stream,
+                             int sm_count) {
+    const size_t smem = sizeof(ErWarp) * W;
+    cudaError_t e = smem_attr_once((const void *)er_kernel<W>, (int)smem);
+    if (e != cudaSuccess) return e;
+    long blocks = (n_events + W - 1) / W;
+    const long cap = (long)sm_count * (48 / W > 0 ? 48 / W : 1);  // up to 48 resident warps per SM
     if (blocks > cap) blocks = cap;
-    er_kernel<<<(unsigned)blocks, ER_WARPS * 32, 0, stream>>>(hv, toomany, n_events, errw);
+    er_kernel<W><<<(unsigned)blocks, W * 32, smem, stream>>>(hv, toomany, n_events, errw);
     return cudaGetLastError();
+}
+
+// Host launcher; `warps` = events per CTA (1, 2, 4, 8 or 16).
+cudaError_t launch_event_reduce(or_hits_view_t hv, uint8_t *toomany, int n_events, uint32_t *errw,
+                                cudaStream_t stream, int sm_count, int warps) {
+    if (n_events <= 0) return cudaSuccess;
+    switch (warps) {
+    case 1: return er_launch<1>(hv, toomany, n_events, errw, stream, sm_count);
+    case 2: return er_launch<2>(hv, toomany, n_events, errw, stream, sm_count);
+    case 8: return er_launch<8>(hv, toomany, n_events, errw, stream, sm_count);
+    case 16: return er_launch<16>(hv, toomany, n_events, errw, stream, sm_count);
+    default: return er_launch<4>(hv, toomany, n_events, errw, stream, sm_count);
+    }
 }
 
 }  // namespace orgpu

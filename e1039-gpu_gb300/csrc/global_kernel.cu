@@ -20,7 +20,6 @@
 
 namespace orgpu {
 
-constexpr int GL_WARPS = 4;
 constexpr int GL_PAIRCAP = 128;
 constexpr int GL_NST = 7;  // scratch entries tracked for stale reads: 0..6
 
@@ -82,7 +81,8 @@ static __device__ void sagitta_st1(float x0, float tx, float y0, float ty, int d
 // finish early keep taking units instead of idling behind a heavy event.
 constexpr int GL_CHUNK = 8;
 
-__global__ void __launch_bounds__(GL_WARPS * 32)
+template <int W>
+__global__ void __launch_bounds__(W * 32)
     global_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
                   const uint8_t *__restrict__ toomany, int n_events, uint32_t *__restrict__ errw,
                   unsigned long long *__restrict__ sched) {
@@ -482,22 +482,37 @@ __global__ void __launch_bounds__(GL_WARPS * 32)
     }
 }
 
-size_t global_smem_bytes() { return ((sizeof(or_plane_t) + 15) & ~size_t(15)) + sizeof(GlWarp) * GL_WARPS; }
+size_t global_smem_bytes(int warps) {
+    return ((sizeof(or_plane_t) + 15) & ~size_t(15)) + sizeof(GlWarp) * (size_t)warps;
+}
 
-cudaError_t launch_global(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, const uint8_t *toomany,
-                          int n_events, uint32_t *errw, unsigned long long *sched, cudaStream_t stream,
-                          int sm_count) {
-    if (n_events <= 0) return cudaSuccess;
-    const size_t smem = global_smem_bytes();
-    cudaError_t err = smem_attr_once((const void *)global_kernel, (int)smem);
+template <int W>
+static cudaError_t global_launch(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
+                                 const uint8_t *toomany, int n_events, uint32_t *errw, unsigned long long *sched,
+                                 cudaStream_t stream, int sm_count) {
+    const size_t smem = global_smem_bytes(W);
+    cudaError_t err = smem_attr_once((const void *)global_kernel<W>, (int)smem);
     if (err != cudaSuccess) return err;
     if ((err = cudaMemsetAsync(sched, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return err;
-    long blocks = ((long)n_events * (OR_NSLOTS / GL_CHUNK) + GL_WARPS - 1) / GL_WARPS;
-    const long cap = (long)sm_count * 8;
+    long blocks = ((long)n_events * (OR_NSLOTS / GL_CHUNK) + W - 1) / W;
+    const long cap = (long)sm_count * (32 / W > 0 ? 32 / W : 1);
     if (blocks > cap) blocks = cap;
-    global_kernel<<<(unsigned)blocks, GL_WARPS * 32, smem, stream>>>(d_plane, hv, tv, toomany, n_events, errw,
-                                                                      sched);
+    global_kernel<W><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, toomany, n_events, errw, sched);
     return cudaGetLastError();
+}
+
+// `warps` = work units (event, 8 slots) in flight per CTA: 1, 2, 4, 8 or 16
+cudaError_t launch_global(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, const uint8_t *toomany,
+                          int n_events, uint32_t *errw, unsigned long long *sched, cudaStream_t stream,
+                          int sm_count, int warps) {
+    if (n_events <= 0) return cudaSuccess;
+    switch (warps) {
+    case 1: return global_launch<1>(d_plane, hv, tv, toomany, n_events, errw, sched, stream, sm_count);
+    case 2: return global_launch<2>(d_plane, hv, tv, toomany, n_events, errw, sched, stream, sm_count);
+    case 8: return global_launch<8>(d_plane, hv, tv, toomany, n_events, errw, sched, stream, sm_count);
+    case 16: return global_launch<16>(d_plane, hv, tv, toomany, n_events, errw, sched, stream, sm_count);
+    default: return global_launch<4>(d_plane, hv, tv, toomany, n_events, errw, sched, stream, sm_count);
+    }
 }
 
 }  // namespace orgpu

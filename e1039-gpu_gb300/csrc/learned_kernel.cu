@@ -74,9 +74,9 @@ __global__ void __launch_bounds__(RW_THREADS)
     if (t == RW_THREADS - 1) row_off[n_events] = warp_sum[RW_THREADS / 32 - 1];
 }
 
-constexpr int FT_WARPS = 4;
 
-__global__ void __launch_bounds__(FT_WARPS * 32)
+template <int W>
+__global__ void __launch_bounds__(W * 32)
     features_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
                     const uint8_t *__restrict__ toomany, int n_events, const int32_t *__restrict__ row_off,
                     float *__restrict__ feat, long max_rows) {
@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(FT_WARPS * 32)
     load_plane_smem(&P, gplane);
     __syncthreads();
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (long e = (long)blockIdx.x * FT_WARPS + w; e < n_events; e += (long)gridDim.x * FT_WARPS) {
+    for (long e = (long)blockIdx.x * W + w; e < n_events; e += (long)gridDim.x * W) {
         if (toomany[e]) continue;
         // first row of every slot
         const int nslot = min((int)tv.ntracks[e * OR_NSLOTS + lane], OR_SLOTCAP);
@@ -258,16 +258,29 @@ cudaError_t launch_rows(const uint16_t *ntracks, const uint8_t *toomany, int n_e
     return cudaGetLastError();
 }
 
+template <int W>
+static cudaError_t features_launch(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
+                                   const uint8_t *toomany, int n_events, const int32_t *row_off, float *feat,
+                                   long max_rows, cudaStream_t stream, int sm_count) {
+    long blocks = (n_events + W - 1) / W;
+    const long cap = (long)sm_count * (64 / W);
+    if (blocks > cap) blocks = cap;
+    features_kernel<W><<<(unsigned)blocks, W * 32, 0, stream>>>(d_plane, hv, tv, toomany, n_events, row_off, feat,
+                                                               max_rows);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_features(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, const uint8_t *toomany,
                             int n_events, const int32_t *row_off, float *feat, long max_rows, cudaStream_t stream,
-                            int sm_count) {
+                            int sm_count, int warps) {
     if (n_events <= 0) return cudaSuccess;
-    long blocks = (n_events + FT_WARPS - 1) / FT_WARPS;
-    const long cap = (long)sm_count * 16;
-    if (blocks > cap) blocks = cap;
-    features_kernel<<<(unsigned)blocks, FT_WARPS * 32, 0, stream>>>(d_plane, hv, tv, toomany, n_events, row_off,
-                                                                    feat, max_rows);
-    return cudaGetLastError();
+    switch (warps) {
+    case 1: return features_launch<1>(d_plane, hv, tv, toomany, n_events, row_off, feat, max_rows, stream, sm_count);
+    case 2: return features_launch<2>(d_plane, hv, tv, toomany, n_events, row_off, feat, max_rows, stream, sm_count);
+    case 8: return features_launch<8>(d_plane, hv, tv, toomany, n_events, row_off, feat, max_rows, stream, sm_count);
+    case 16: return features_launch<16>(d_plane, hv, tv, toomany, n_events, row_off, feat, max_rows, stream, sm_count);
+    default: return features_launch<4>(d_plane, hv, tv, toomany, n_events, row_off, feat, max_rows, stream, sm_count);
+    }
 }
 
 cudaError_t launch_keep(const float *score, const int32_t *row_off, int n_events, float t_keep, float t_unc,

@@ -23,7 +23,6 @@
 
 namespace orgpu {
 
-constexpr int SL_WARPS = 4;
 constexpr float SEL_CHI2DOF_MAX = 250.f;  // reconstruction_constants.h:194
 constexpr float SEL_MERGE_THRES = 0.015f; // :196
 
@@ -59,7 +58,8 @@ __device__ __forceinline__ bool prop_segment(float x0, float tx, const HitPlane 
 
 __device__ __forceinline__ float chi2dof(const float *T) { return T[OR_TRK_CHI2] / (T[OR_TRK_NHITS] - 5); }
 
-__global__ void __launch_bounds__(SL_WARPS * 32)
+template <int W>
+__global__ void __launch_bounds__(W * 32)
     select_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
                   const uint8_t *__restrict__ toomany, int n_events, int do_prop, int do_clean) {
     __shared__ float zs[OR_NDET];
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(SL_WARPS * 32)
     // prop-tube planes: x 50/49 and 52/51, y 48/47 and 54/53
     const int px1 = c_detsuperid[5][0] * 2, px2 = c_detsuperid[6][0] * 2;
     const int py1 = c_detsuperid[5][1] * 2, py2 = c_detsuperid[6][1] * 2;
-    for (long e = (long)blockIdx.x * SL_WARPS + w; e < n_events; e += (long)gridDim.x * SL_WARPS) {
+    for (long e = (long)blockIdx.x * W + w; e < n_events; e += (long)gridDim.x * W) {
         if (toomany[e]) continue;
         const int n_own = min((int)tv.ntracks[e * OR_NSLOTS + lane], OR_SLOTCAP);
         if (do_prop) {
@@ -142,15 +142,27 @@ __global__ void __launch_bounds__(SL_WARPS * 32)
     }
 }
 
-cudaError_t launch_select(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, const uint8_t *toomany,
-                          int n_events, int do_prop, int do_clean, cudaStream_t stream, int sm_count) {
-    if (n_events <= 0) return cudaSuccess;
-    long blocks = (n_events + SL_WARPS - 1) / SL_WARPS;
-    const long cap = (long)sm_count * 16;
+template <int W>
+static cudaError_t select_launch(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
+                                 const uint8_t *toomany, int n_events, int do_prop, int do_clean, cudaStream_t stream,
+                                 int sm_count) {
+    long blocks = (n_events + W - 1) / W;
+    const long cap = (long)sm_count * (64 / W);
     if (blocks > cap) blocks = cap;
-    select_kernel<<<(unsigned)blocks, SL_WARPS * 32, 0, stream>>>(d_plane, hv, tv, toomany, n_events, do_prop,
-                                                                  do_clean);
+    select_kernel<W><<<(unsigned)blocks, W * 32, 0, stream>>>(d_plane, hv, tv, toomany, n_events, do_prop, do_clean);
     return cudaGetLastError();
+}
+
+cudaError_t launch_select(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, const uint8_t *toomany,
+                          int n_events, int do_prop, int do_clean, cudaStream_t stream, int sm_count, int warps) {
+    if (n_events <= 0) return cudaSuccess;
+    switch (warps) {
+    case 1: return select_launch<1>(d_plane, hv, tv, toomany, n_events, do_prop, do_clean, stream, sm_count);
+    case 2: return select_launch<2>(d_plane, hv, tv, toomany, n_events, do_prop, do_clean, stream, sm_count);
+    case 8: return select_launch<8>(d_plane, hv, tv, toomany, n_events, do_prop, do_clean, stream, sm_count);
+    case 16: return select_launch<16>(d_plane, hv, tv, toomany, n_events, do_prop, do_clean, stream, sm_count);
+    default: return select_launch<4>(d_plane, hv, tv, toomany, n_events, do_prop, do_clean, stream, sm_count);
+    }
 }
 
 }  // namespace orgpu

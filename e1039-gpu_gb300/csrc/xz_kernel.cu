@@ -29,7 +29,6 @@
 
 namespace orgpu {
 
-constexpr int XZ_WARPS = 4;
 constexpr int XZ_NCELLS = 32 * 49;
 constexpr int XZ_MAXPLANEHITS = 200;
 
@@ -113,7 +112,8 @@ struct XHit {
     float X, Z, drift, tdc, w;
 };
 
-__global__ void __launch_bounds__(XZ_WARPS * 32)
+template <int W>
+__global__ void __launch_bounds__(W * 32)
     xz_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
               int32_t *__restrict__ ntracklets, uint8_t *__restrict__ toomany, int n_events) {
     extern __shared__ __align__(16) unsigned char xz_smem[];
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(XZ_WARPS * 32)
     const int lane = threadIdx.x & 31;
     XzWarp &S = warps[w];
 
-    for (long e = (long)blockIdx.x * XZ_WARPS + w; e < n_events; e += (long)gridDim.x * XZ_WARPS) {
+    for (long e = (long)blockIdx.x * W + w; e < n_events; e += (long)gridDim.x * W) {
         uint16_t *nt = tv.ntracks + e * OR_NSLOTS;
         if (toomany[e]) {  // K:195-200
             nt[lane] = 0;
@@ -382,21 +382,33 @@ __global__ void __launch_bounds__(XZ_WARPS * 32)
     }
 }
 
-size_t xz_smem_bytes() {
-    return ((sizeof(or_plane_t) + 15) & ~size_t(15)) + sizeof(XzWarp) * XZ_WARPS;
+size_t xz_smem_bytes(int warps) {
+    return ((sizeof(or_plane_t) + 15) & ~size_t(15)) + sizeof(XzWarp) * (size_t)warps;
 }
 
-cudaError_t launch_xz(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, int32_t *ntracklets,
-                      uint8_t *toomany, int n_events, cudaStream_t stream, int sm_count) {
-    if (n_events <= 0) return cudaSuccess;
-    const size_t smem = xz_smem_bytes();
-    cudaError_t err = smem_attr_once((const void *)xz_kernel, (int)smem);
+template <int W>
+static cudaError_t xz_launch(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, int32_t *ntracklets,
+                             uint8_t *toomany, int n_events, cudaStream_t stream, int sm_count) {
+    const size_t smem = xz_smem_bytes(W);
+    cudaError_t err = smem_attr_once((const void *)xz_kernel<W>, (int)smem);
     if (err != cudaSuccess) return err;
-    long blocks = (n_events + XZ_WARPS - 1) / XZ_WARPS;
-    const long cap = (long)sm_count * 8;
+    long blocks = (n_events + W - 1) / W;
+    const long cap = (long)sm_count * (32 / W > 0 ? 32 / W : 1);
     if (blocks > cap) blocks = cap;
-    xz_kernel<<<(unsigned)blocks, XZ_WARPS * 32, smem, stream>>>(d_plane, hv, tv, ntracklets, toomany, n_events);
+    xz_kernel<W><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, ntracklets, toomany, n_events);
     return cudaGetLastError();
+}
+
+// `warps` = events per CTA: 1, 2, 4 or 8 (the per-warp scratch is too large for 16)
+cudaError_t launch_xz(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, int32_t *ntracklets,
+                      uint8_t *toomany, int n_events, cudaStream_t stream, int sm_count, int warps) {
+    if (n_events <= 0) return cudaSuccess;
+    switch (warps) {
+    case 1: return xz_launch<1>(d_plane, hv, tv, ntracklets, toomany, n_events, stream, sm_count);
+    case 2: return xz_launch<2>(d_plane, hv, tv, ntracklets, toomany, n_events, stream, sm_count);
+    case 8: return xz_launch<8>(d_plane, hv, tv, ntracklets, toomany, n_events, stream, sm_count);
+    default: return xz_launch<4>(d_plane, hv, tv, ntracklets, toomany, n_events, stream, sm_count);
+    }
 }
 
 }  // namespace orgpu

@@ -37,7 +37,6 @@
 
 namespace orgpu {
 
-constexpr int YZ_WARPS = 4;
 constexpr int YZ_MAXWIN = 100;          // windowed hits per plane (the reference's hitidx arrays)
 constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's hitpairs arrays)
 constexpr int YZ_ARENA_HITS = 192;      // windowed hits kept in shared memory per warp
@@ -827,7 +826,8 @@ __device__ __forceinline__ YzHit *yz_garena(const YzScratch &sc, int gwarp) {
     return sc.garena + (long)(gwarp % sc.garena_warps) * YZ_GARENA_HITS;
 }
 
-__global__ void __launch_bounds__(YZ_WARPS * 32, 4)
+template <int W>
+__global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
     yz_plan_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
                    const uint8_t *__restrict__ toomany, int n_events, YzScratch sc, uint32_t *__restrict__ errw,
                    YzPrune prune) {
@@ -839,7 +839,7 @@ __global__ void __launch_bounds__(YZ_WARPS * 32, 4)
     const int w = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     YzWarp &S = warps[w];
-    YzHit *garena = yz_garena(sc, blockIdx.x * YZ_WARPS + w);
+    YzHit *garena = yz_garena(sc, blockIdx.x * W + w);
 
     // planning units (event, YZ_PLAN_CHUNK slots) from a device counter: slots
     // are independent (one reference thread each), events very uneven
@@ -940,7 +940,8 @@ __global__ void __launch_bounds__(YZ_WARPS * 32, 4)
 }
 
 // persistent warps drain the unit queue
-__global__ void __launch_bounds__(YZ_WARPS * 32)
+template <int W>
+__global__ void __launch_bounds__(W * 32)
     yz_work_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv, YzScratch sc) {
     extern __shared__ __align__(16) unsigned char yz_smem[];
     or_plane_t &P = *reinterpret_cast<or_plane_t *>(yz_smem);
@@ -950,7 +951,7 @@ __global__ void __launch_bounds__(YZ_WARPS * 32)
     const int w = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     YzWarp &S = warps[w];
-    YzHit *garena = yz_garena(sc, blockIdx.x * YZ_WARPS + w);
+    YzHit *garena = yz_garena(sc, blockIdx.x * W + w);
     const int nunits = min((int)sc.counters[0], sc.cap_units);
     for (;;) {
         int u = 0;
@@ -1015,7 +1016,9 @@ __global__ void __launch_bounds__(128) yz_apply_kernel(or_tracks_view_t tv, YzSc
     }
 }
 
-size_t yz_smem_bytes() { return ((sizeof(or_plane_t) + 15) & ~size_t(15)) + sizeof(YzWarp) * YZ_WARPS; }
+size_t yz_smem_bytes(int warps) {
+    return ((sizeof(or_plane_t) + 15) & ~size_t(15)) + sizeof(YzWarp) * (size_t)warps;
+}
 
 // Scratch the YZ stage needs: queue of units, per-unit best records, heavy
 // tracklets, per-warp overflow arenas.
@@ -1025,15 +1028,16 @@ size_t yz_scratch_bytes(int cap_units, int cap_heavy, int garena_warps) {
     return b + sizeof(YzHit) * YZ_GARENA_HITS * (size_t)garena_warps;
 }
 
+template <int W>
 static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
                                   const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
                                   int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, YzPrune prune) {
     if (n_events <= 0) return cudaSuccess;
-    const size_t smem = yz_smem_bytes();
+    const size_t smem = yz_smem_bytes(W);
     cudaError_t err;
-    if ((err = smem_attr_once((const void *)yz_plan_kernel, (int)smem)))
+    if ((err = smem_attr_once((const void *)yz_plan_kernel<W>, (int)smem)))
         return err;
-    if ((err = smem_attr_once((const void *)yz_work_kernel, (int)smem)))
+    if ((err = smem_attr_once((const void *)yz_work_kernel<W>, (int)smem)))
         return err;
     char *p = static_cast<char *>(scratch);
     YzScratch sc;
@@ -1051,22 +1055,48 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
     sc.cap_heavy = cap_heavy;
     sc.garena_warps = garena_warps;
     if ((err = cudaMemsetAsync(sc.counters, 0, 256, stream))) return err;
-    const long blocks = garena_warps / YZ_WARPS;
-    const long blocks_plan = min(((long)n_events * (OR_NSLOTS / YZ_PLAN_CHUNK) + YZ_WARPS - 1) / YZ_WARPS, blocks);
-    yz_plan_kernel<<<(unsigned)blocks_plan, YZ_WARPS * 32, smem, stream>>>(d_plane, hv, tv, toomany, n_events, sc,
-                                                                           errw, prune);
+    const long blocks = garena_warps / W;
+    const long blocks_plan = min(((long)n_events * (OR_NSLOTS / YZ_PLAN_CHUNK) + W - 1) / W, blocks);
+    yz_plan_kernel<W><<<(unsigned)blocks_plan, W * 32, smem, stream>>>(d_plane, hv, tv, toomany, n_events, sc, errw,
+                                                                       prune);
     if ((err = cudaGetLastError())) return err;
-    yz_work_kernel<<<(unsigned)blocks, YZ_WARPS * 32, smem, stream>>>(d_plane, hv, tv, sc);
+    yz_work_kernel<W><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, sc);
     if ((err = cudaGetLastError())) return err;
     yz_apply_kernel<<<(unsigned)(sm_count * 4), 128, 0, stream>>>(tv, sc);
     return cudaGetLastError();
 }
 
+static cudaError_t launch_yz_w(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
+                               const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
+                               int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, YzPrune prune,
+                               int warps) {
+    switch (warps) {
+    case 1: return launch_yz_impl<1>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
+                                     garena_warps, stream, sm_count, prune);
+    case 2: return launch_yz_impl<2>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
+                                     garena_warps, stream, sm_count, prune);
+    case 8: return launch_yz_impl<8>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
+                                     garena_warps, stream, sm_count, prune);
+    case 16: return launch_yz_impl<16>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
+                                       garena_warps, stream, sm_count, prune);
+    default: return launch_yz_impl<4>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
+                                      garena_warps, stream, sm_count, prune);
+    }
+}
+
 cudaError_t launch_yz(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, const uint8_t *toomany,
                       int n_events, uint32_t *errw, void *scratch, int cap_units, int cap_heavy, int garena_warps,
                       cudaStream_t stream, int sm_count) {
-    return launch_yz_impl(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
-                          sm_count, YzPrune{nullptr, nullptr, 0});
+    return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
+                       sm_count, YzPrune{nullptr, nullptr, 0}, 4);
+}
+
+// with `warps` events (work units) per CTA: 1, 2, 4, 8 or 16
+cudaError_t launch_yz_tuned(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
+                            const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
+                            int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, int warps) {
+    return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
+                       sm_count, YzPrune{nullptr, nullptr, 0}, warps);
 }
 
 // YZ with the scorer's keep flags: pruned tracklets are left as tracklets no
@@ -1074,9 +1104,9 @@ cudaError_t launch_yz(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_vi
 cudaError_t launch_yz_pruned(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
                              const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
                              int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count,
-                             const int32_t *row_off, const uint8_t *keep, long max_rows) {
-    return launch_yz_impl(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
-                          sm_count, YzPrune{row_off, keep, max_rows});
+                             const int32_t *row_off, const uint8_t *keep, long max_rows, int warps) {
+    return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
+                       sm_count, YzPrune{row_off, keep, max_rows}, warps);
 }
 
 }  // namespace orgpu

@@ -20,7 +20,11 @@ EXPORTS = ("or_version", "or_last_error", "or_status_string", "or_geometry_load"
            "or_tracks_view_bytes", "or_pack_hits", "or_collect_tracks", "or_yz_noalloc", "or_tracklet_rows",
            "or_tracklet_features", "or_mlp_score", "or_keep_mask", "or_yz_pruned", "or_run_batch_learned",
            "or_tracklet_labels", "or_track_agreement", "or_mlp_grad_blocks", "or_mlp_forward", "or_mlp_gradient",
-           "or_mlp_adam", "or_prop_matching", "or_global_clean", "or_run_selection")
+           "or_mlp_adam", "or_prop_matching", "or_global_clean", "or_run_selection", "or_set_launch",
+           "or_get_launch")
+
+# tunable kernels (or_kernel_id_t)
+KERNELS = {"event_reduce": 0, "xz": 1, "yz": 2, "back_clean": 3, "global": 4, "select": 5, "features": 6}
 
 OR_YZ_NOALLOC_MAX_EVENTS = 10000
 OR_ERRW_CAPACITY = 2
@@ -85,6 +89,8 @@ def lib():
     lb.or_mlp_forward.argtypes = [vp, vp, vp, vp, i32, vp, vp]
     lb.or_mlp_gradient.argtypes = [vp, vp, vp, vp, vp, i32, f32, vp, vp, vp]
     lb.or_mlp_adam.argtypes = [vp, vp, vp, vp, vp, i32, i32, f32, f32, f32, f32, vp, vp]
+    lb.or_set_launch.argtypes = [vp, i32, i32]
+    lb.or_get_launch.argtypes = [vp, i32]
     lb.or_prop_matching.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, i32, vp]
     lb.or_global_clean.argtypes = [vp, L.OrTracksView, vp, i32, vp]
     lb.or_run_selection.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, i32, vp]

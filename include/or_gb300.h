@@ -52,6 +52,20 @@ typedef enum or_status {
 
 typedef struct or_ctx or_ctx_t;
 
+/* Tunable launch shapes (or_set_launch): events -- or, for the dynamically
+ * scheduled YZ and global kernels, work units -- per CTA, one warp each,
+ * so CTAs of 32 to 512 threads.  Results do not depend on them. */
+typedef enum or_kernel_id {
+    OR_K_EVENT_REDUCE = 0,
+    OR_K_XZ = 1, /* at most 8 */
+    OR_K_YZ = 2,
+    OR_K_BACK_CLEAN = 3,
+    OR_K_GLOBAL = 4,
+    OR_K_SELECT = 5,
+    OR_K_FEATURES = 6,
+    OR_K_COUNT = 7
+} or_kernel_id_t;
+
 /* Library version string and the CUDA arch it was built for. */
 const char *or_version(void);
 /* Text of the most recent error on this thread. */
@@ -67,6 +81,10 @@ int or_geometry_load(const char *path, or_plane_t *plane, double *wire_pos);
  * context's small device state, and records a copy of nothing else. */
 int or_create(int device, or_ctx_t **out);
 int or_destroy(or_ctx_t *ctx);
+/* Events per CTA of `kernel` (1, 2, 4, 8 or 16; default 4), e.g. as chosen by
+ * the autotuner (orgpu/autotune.py); or_get_launch returns the current one. */
+int or_set_launch(or_ctx_t *ctx, int kernel, int events_per_cta);
+int or_get_launch(or_ctx_t *ctx, int kernel);
 /* Copy a host or_plane_t to the device (online_reconstruction.cu:754). */
 int or_set_geometry(or_ctx_t *ctx, const or_plane_t *plane);
 /* Wait for `stream` and report the device-side error words raised since the
