@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     return ap.parse_args()
 
 
@@ -172,6 +173,14 @@ def main():
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
     rc = pipeline.Reconstruction(plane, local)
+    tuned = None
+    if not args.no_autotune:
+        # launch shapes for this workload, tuned on a sample of its events
+        from orgpu import autotune
+        ns = min(n, 16000)
+        sample = S.pack(rec[:off[ns]], off[:ns + 1], S.Geometry(plane, wp).wire_pos_f32())
+        tuned = autotune.tune(rc, sample, candidates=(1, 2, 4, 8, 16), repeats=2, device=local)
+        del sample
     b = pipeline.DeviceBatch(n, local)
     stream = torch.cuda.current_stream(dev)
     d_rec = torch.from_numpy(rec.view(np.uint8)).to(dev)
@@ -318,7 +327,7 @@ def main():
                "sample": "first %d events of the workload, one pass, all host threads" % ns}
 
     learned_res = None if args.no_learned else learned_leg(args, rc, b, rec, off, d_rec, d_off, d_wp, value, dev)
-    serving_res = None if args.no_serving else serving_leg(plane, wp)
+    serving_res = None if args.no_serving else serving_leg(plane, wp, tuned)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no dataset)", "config": cj,
@@ -329,7 +338,9 @@ def main():
             "gpu_launches": LAUNCHES_PER_STEP * args.steps,
             "stage_ms": stage_ms,
             "events_rejected_frac": float(toomany.mean()), "global_tracks_last_step": ntrk,
-            "learned": learned_res, "serving": serving_res}
+            "learned": learned_res, "serving": serving_res,
+            "autotune": None if tuned is None else {"events_per_cta": tuned["best"], "sample_events": tuned["events"],
+                                                    "stage_ms_by_shape": tuned["ms"]}}
     print(json.dumps(line))
 
 
@@ -376,7 +387,7 @@ def learned_leg(args, rc, b_plain, rec, off, d_rec, d_off, d_wp, plain_value, de
             "model": "e1039-gpu_gb300/data/scorer_e906.npz", "t_keep": sp.t_keep, "t_unc": sp.t_unc}
 
 
-def serving_leg(plane, wp, pool_events=40000, burst_s=4.0, seed=906005):
+def serving_leg(plane, wp, tuned=None, pool_events=40000, burst_s=4.0, seed=906005):
     """Spill-structured Poisson arrivals of batches of U(1, 10000) one-dimuon
     events (the learned-scorer / small-batch distribution) at three offered
     loads, through the continuous-batching server: p50/p99 latency and
@@ -386,7 +397,7 @@ def serving_leg(plane, wp, pool_events=40000, burst_s=4.0, seed=906005):
     geo = S.Geometry(plane, wp)
     rec, off, _ = S.generate(geo, S.config_small(pool_events, seed))
     rec, off = S.cap_records(rec, off)
-    srv = serving.Server(plane, wp, slot_events=10000, max_slots=4, rec_per_event=400)
+    srv = serving.Server(plane, wp, slot_events=10000, max_slots=4, rec_per_event=400, launch_config=tuned)
     rng = np.random.default_rng(seed)
 
     def take(n):

@@ -204,7 +204,7 @@ class Server:
     keeping `reserve_bytes` free."""
 
     def __init__(self, plane, wire_pos, slot_events=10000, max_slots=4, rec_per_event=400, device=0, scorer=None,
-                 graphs=True, reserve_bytes=8 << 30):
+                 graphs=True, reserve_bytes=8 << 30, launch_config=None):
         torch = _torch()
         self.device = device
         wp = torch.from_numpy(np.asarray(wire_pos, np.float32).reshape(-1)).cuda(device)
@@ -218,6 +218,9 @@ class Server:
         if not self.slots:
             raise _lib.OrError(_lib.OR_ERR_NOMEM, "no slot fits in the free device memory")
         for s in self.slots:
+            if launch_config is not None:  # autotune.tune() result: shapes before the graphs are captured
+                from . import autotune
+                autotune.apply(s.rc, launch_config)
             s.capture()
         self.slot_events = slot_events
         self.pending = collections.deque()
