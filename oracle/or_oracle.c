@@ -300,14 +300,23 @@ static void calculate_xz_fy(int d, int elid, float drift, short hitsign, float y
     *z = zz;
 }
 
+/* Arithmetic type of the fits, residuals and chi2 sums.  float restates the
+ * reference; building with -DORC_FIT_T=double gives the FP64 oracle the
+ * FP32 fit errors are measured against (inputs and stored results stay
+ * float, as the reference's records are). */
+#ifndef ORC_FIT_T
+#define ORC_FIT_T float
+#endif
+typedef ORC_FIT_T fit_t;
+
 /* FT:3-82 (Gauss-Jordan with partial pivoting; operations.h:39-62) */
-void orc_matinv_2x2(const float *A, float *Ainv) {
+static void matinv_2x2_t(const fit_t *A, fit_t *Ainv) {
     int perm0 = 0, perm1 = 1, icol0, icol1, i;
-    float AA00 = A[0], AA10 = A[1], AA01 = A[2], AA11 = A[3], tmp, t, pp;
+    fit_t AA00 = A[0], AA10 = A[1], AA01 = A[2], AA11 = A[3], tmp, t, pp;
     int pvt;
-    pp = fabsf(AA00);
+    pp = (fit_t)fabs(AA00);
     pvt = 0;
-    t = fabsf(AA10);
+    t = (fit_t)fabs(AA10);
     if (t > pp) {
         pp = t;
         pvt = 1;
@@ -317,14 +326,14 @@ void orc_matinv_2x2(const float *A, float *Ainv) {
         tmp = AA01; AA01 = AA11; AA11 = tmp;
         i = perm0; perm0 = perm1; perm1 = i;
     }
-    tmp = 1.0f / AA00;
+    tmp = (fit_t)1.0f / AA00;
     icol0 = perm0;
     AA00 = tmp;
     AA01 = tmp * AA01;
     tmp = AA10;
     AA10 = (-tmp) * AA00;
     AA11 = -(tmp * AA01) + AA11;
-    tmp = 1.0f / AA11;
+    tmp = (fit_t)1.0f / AA11;
     icol1 = perm1;
     AA10 = tmp * AA10;
     AA11 = tmp;
@@ -337,43 +346,53 @@ void orc_matinv_2x2(const float *A, float *Ainv) {
     Ainv[1 * 2 + icol1] = AA11;
 }
 
+void orc_matinv_2x2(const float *A, float *Ainv) {
+    fit_t a[4] = {A[0], A[1], A[2], A[3]}, r[4];
+    matinv_2x2_t(a, r);
+    for (int k = 0; k < 4; k++) Ainv[k] = (float)r[k];
+}
+
 /* AM:32-74; the returned "chi2" of the reference is never read by the hot
  * path (each caller overwrites it), so it is not computed */
 void orc_fit_2d(int n, const float *x, const float *z, const float *w, float *par, float *err) {
-    float A[4] = {0, 0, 0, 0}, Ainv[4] = {0, 0, 0, 0}, B[2] = {0, 0};
+    fit_t A[4] = {0, 0, 0, 0}, Ainv[4] = {0, 0, 0, 0}, B[2] = {0, 0};
     for (int i = 0; i < n; i++) {
-        B[0] += w[i] * x[i];
-        B[1] += w[i] * x[i] * z[i];
-        A[0] += w[i];
-        A[1] += w[i] * z[i];
-        A[2] += w[i] * z[i];
-        A[3] += w[i] * z[i] * z[i];
+        const fit_t wi = w[i], xi = x[i], zi = z[i];
+        B[0] += wi * xi;
+        B[1] += wi * xi * zi;
+        A[0] += wi;
+        A[1] += wi * zi;
+        A[2] += wi * zi;
+        A[3] += wi * zi * zi;
     }
-    orc_matinv_2x2(A, Ainv);
+    matinv_2x2_t(A, Ainv);
     for (int j = 0; j < 2; j++) {
-        par[j] = 0.0f;
-        err[j] = sqrtf(fabsf(Ainv[j * 2 + j]));
-        for (int k = 0; k < 2; k++) par[j] += Ainv[j * 2 + k] * B[k];
+        fit_t pj = 0;
+        err[j] = (float)sqrt((double)(fit_t)fabs(Ainv[j * 2 + j]));
+        for (int k = 0; k < 2; k++) pj += Ainv[j * 2 + k] * B[k];
+        par[j] = (float)pj;
     }
 }
 
 /* AM:78-119 */
 void orc_fit_2d_drift(int n, const float *x, const float *drift, const short *sign, const float *z, const float *w,
                       float *par, float *err) {
-    float A[4] = {0, 0, 0, 0}, Ainv[4] = {0, 0, 0, 0}, B[2] = {0, 0};
+    fit_t A[4] = {0, 0, 0, 0}, Ainv[4] = {0, 0, 0, 0}, B[2] = {0, 0};
     for (int i = 0; i < n; i++) {
-        B[0] += w[i] * (x[i] + drift[i] * (float)sign[i]);
-        B[1] += w[i] * (x[i] + drift[i] * (float)sign[i]) * z[i];
-        A[0] += w[i];
-        A[1] += w[i] * z[i];
-        A[2] += w[i] * z[i];
-        A[3] += w[i] * z[i] * z[i];
+        const fit_t wi = w[i], zi = z[i], xd = (fit_t)x[i] + (fit_t)drift[i] * (fit_t)sign[i];
+        B[0] += wi * xd;
+        B[1] += wi * xd * zi;
+        A[0] += wi;
+        A[1] += wi * zi;
+        A[2] += wi * zi;
+        A[3] += wi * zi * zi;
     }
-    orc_matinv_2x2(A, Ainv);
+    matinv_2x2_t(A, Ainv);
     for (int j = 0; j < 2; j++) {
-        par[j] = 0.0f;
-        err[j] = sqrtf(fabsf(Ainv[j * 2 + j]));
-        for (int k = 0; k < 2; k++) par[j] += Ainv[j * 2 + k] * B[k];
+        fit_t pj = 0;
+        err[j] = (float)sqrt((double)(fit_t)fabs(Ainv[j * 2 + j]));
+        for (int k = 0; k < 2; k++) pj += Ainv[j * 2 + k] * B[k];
+        par[j] = (float)pj;
     }
 }
 
@@ -531,33 +550,37 @@ static int match_track_XZ_to_hodo(int stid, int detid, int nhits, hitcoll_t hits
 }
 
 /* H:1149-1165 */
-static float residual(short d, short elid, float drift, short sign, const or_plane_t *p, float x0, float y0, float tx,
-                      float ty) {
-    float p1x = x_bep(d, elid, p), p1y = y_bep(d, elid, p), p1z = z_bep(d, elid, p);
-    float deltapx = p->deltapx[d], deltapy = p->deltapy[d], deltapz = p->deltapz[d];
-    float den2 = deltapy * deltapy * (1 + tx * tx) + deltapx * deltapx * (1 + ty * ty) -
-                 2 * (ty * deltapx * deltapz + ty * deltapy * deltapz + tx * ty * deltapx * deltapy);
-    float dca = ((ty * deltapz - deltapy) * (p1x - x0) + (deltapx - tx * deltapz) * (p1y - y0) +
-                 p1z * (tx * deltapy - ty * deltapx)) /
-                sqrtf(den2);
-    return drift * (float)sign - dca;
+static float residual(short d, short elid, float drift, short sign, const or_plane_t *p, float x0_, float y0_,
+                      float tx_, float ty_) {
+    const fit_t x0 = x0_, y0 = y0_, tx = tx_, ty = ty_;
+    const fit_t p1x = x_bep(d, elid, p), p1y = y_bep(d, elid, p), p1z = z_bep(d, elid, p);
+    const fit_t deltapx = p->deltapx[d], deltapy = p->deltapy[d], deltapz = p->deltapz[d];
+    const fit_t den2 = deltapy * deltapy * (1 + tx * tx) + deltapx * deltapx * (1 + ty * ty) -
+                       2 * (ty * deltapx * deltapz + ty * deltapy * deltapz + tx * ty * deltapx * deltapy);
+    const fit_t dca = ((ty * deltapz - deltapy) * (p1x - x0) + (deltapx - tx * deltapz) * (p1y - y0) +
+                       p1z * (tx * deltapy - ty * deltapx)) /
+                      (fit_t)sqrt((double)den2);
+    return (float)((fit_t)drift * (fit_t)sign - dca);
 }
 
 /* H:1182-1204 */
 static float chi2_track(int n, float *residuals, const float *driftdist, const short *sign, const float *resol,
                         const float *p1x, const float *p1y, const float *p1z, const float *dpx, const float *dpy,
                         const float *dpz, float x0, float y0, float tx, float ty) {
-    float chi2 = 0;
+    fit_t chi2 = 0;
+    const fit_t X0 = x0, Y0 = y0, TX = tx, TY = ty;
     for (int i = 0; i < n; i++) {
-        float den2 = dpy[i] * dpy[i] * (1 + tx * tx) + dpx[i] * dpx[i] * (1 + ty * ty) -
-                     2 * (ty * dpx[i] * dpz[i] + ty * dpy[i] * dpz[i] + tx * ty * dpx[i] * dpy[i]);
-        float dca = ((ty * dpz[i] - dpy[i]) * (p1x[i] - x0) + (dpx[i] - tx * dpz[i]) * (p1y[i] - y0) +
-                     p1z[i] * (tx * dpy[i] - ty * dpx[i])) /
-                    sqrtf(den2);
-        residuals[i] = driftdist[i] * (float)sign[i] - dca;
-        chi2 += residuals[i] * residuals[i] / resol[i] / resol[i];
+        const fit_t px = dpx[i], py = dpy[i], pz = dpz[i];
+        const fit_t den2 = py * py * (1 + TX * TX) + px * px * (1 + TY * TY) -
+                           2 * (TY * px * pz + TY * py * pz + TX * TY * px * py);
+        const fit_t dca = ((TY * pz - py) * ((fit_t)p1x[i] - X0) + (px - TX * pz) * ((fit_t)p1y[i] - Y0) +
+                           (fit_t)p1z[i] * (TX * py - TY * px)) /
+                          (fit_t)sqrt((double)den2);
+        const fit_t r = (fit_t)driftdist[i] * (fit_t)sign[i] - dca;
+        residuals[i] = (float)r;
+        chi2 += r * r / (fit_t)resol[i] / (fit_t)resol[i];
     }
-    return chi2;
+    return (float)chi2;
 }
 
 /* H:556-613 */

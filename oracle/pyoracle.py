@@ -17,33 +17,56 @@ sys.path.insert(0, os.path.join(REPO, "e1039-gpu_gb300"))
 from orgpu import layout as L  # noqa: E402
 
 LIB_PATH = os.path.join(HERE, "liborc.so")
+LIB64_PATH = os.path.join(HERE, "liborc64.so")  # the same code with FP64 fits, residuals and chi2 sums
 SOURCES = [os.path.join(HERE, "or_oracle.c")]
 
 ST_TOOMANY_ER, ST_TOOMANY_XZBIN, ST_TOOMANY_TKL = 1, 2, 4
 NCOUNTS = 8
 
 
-def build(force=False):
-    """Compile the oracle with one rounding per float operation."""
-    if not force and os.path.exists(LIB_PATH) and all(
-            os.path.getmtime(LIB_PATH) >= os.path.getmtime(s) for s in SOURCES + [
+def _build_one(path, extra, force):
+    if not force and os.path.exists(path) and all(
+            os.path.getmtime(path) >= os.path.getmtime(s) for s in SOURCES + [
                 os.path.join(HERE, "or_oracle.h"), os.path.join(REPO, "include", "or_layout.h")]):
-        return LIB_PATH
+        return path
     cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-           "-pthread", "-o", LIB_PATH + ".tmp"] + SOURCES + ["-lm"]
+           "-pthread"] + extra + ["-o", path + ".tmp"] + SOURCES + ["-lm"]
     subprocess.check_call(cmd)
-    os.replace(LIB_PATH + ".tmp", LIB_PATH)
-    return LIB_PATH
+    os.replace(path + ".tmp", path)
+    return path
+
+
+def build(force=False):
+    """Compile the oracle with one rounding per float operation, and its FP64
+    instance (fits, residuals and chi2 sums in double)."""
+    _build_one(LIB64_PATH, ["-DORC_FIT_T=double"], force)
+    return _build_one(LIB_PATH, [], force)
 
 
 _lib = None
+_lib64 = None
 
 
 def lib():
     global _lib
     if _lib is None:
         build()
-        _lib = C.CDLL(LIB_PATH)
+        _lib = _load(LIB_PATH)
+    return _lib
+
+
+def lib64():
+    """The FP64 instance (same entry points)."""
+    global _lib64
+    if _lib64 is None:
+        build()
+        _lib64 = _load(LIB64_PATH)
+    return _lib64
+
+
+def _load(path):
+    _lib = C.CDLL(path)
+    if True:
         P = C.POINTER
         _lib.orc_parse_geometry.argtypes = [C.c_char_p, P(L.OrPlane), C.c_void_p]
         _lib.orc_event_reduce.argtypes = [L.OrHitsView, C.c_void_p, C.c_void_p, C.c_int, C.c_int]
@@ -118,14 +141,15 @@ def global_clean(tracks, state, n_threads=0):
     lib().orc_global_clean(tracks.view(), state.toomany.ctypes.data, tracks.n, n_threads)
 
 
-def run_all(plane, hits, tracks, state, n_threads=0, counted=False):
+def run_all(plane, hits, tracks, state, n_threads=0, counted=False, fp64=False):
+    lb = lib64() if fp64 else lib()
     if counted:
-        lib().orc_run_all_counted(C.byref(plane), hits.view(), tracks.view(), state.ntracklets.ctypes.data,
+        lb.orc_run_all_counted(C.byref(plane), hits.view(), tracks.view(), state.ntracklets.ctypes.data,
                                   state.toomany.ctypes.data, state.status.ctypes.data, state.counts.ctypes.data,
                                   hits.n, n_threads)
     else:
-        lib().orc_run_all(C.byref(plane), hits.view(), tracks.view(), state.ntracklets.ctypes.data,
-                          state.toomany.ctypes.data, state.status.ctypes.data, hits.n, n_threads)
+        lb.orc_run_all(C.byref(plane), hits.view(), tracks.view(), state.ntracklets.ctypes.data,
+                       state.toomany.ctypes.data, state.status.ctypes.data, hits.n, n_threads)
 
 
 def tracklet_features(plane, hits, tracks, toomany, max_rows=None):
