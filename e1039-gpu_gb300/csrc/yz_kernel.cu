@@ -486,6 +486,73 @@ __device__ __forceinline__ int yz_gather(const YzWarp &S, const YzHit *base, int
 // scratch-entry scan.  Survivors (about 6% on the uneven batch) go to a
 // shared-memory queue in order.  Phase 2 (survivors, 32 at a time): sign
 // state, left/right walk, prop and hodoscope gates, chi2 (K:1613-1799).
+//
+// Outer iterations (iu3, iv3) whose u3 pair or v3 pair gives no accepted hit
+// are skipped whole: the reference leaves such an iteration before any
+// station-2 load (K:1326-1390), so it neither writes a scratch entry past a
+// count of 4 nor yields a candidate, and jumping over it changes nothing.
+
+// Pairs of lists 2 (u3) and 3 (v3) with an accepted hit, as 128-bit masks
+// (at most YZ_MAXPAIR = 100 pairs per list).
+struct YzAlive {
+    unsigned u[4], v[4];
+};
+
+__device__ __forceinline__ YzAlive yz_alive(const YzWarp &S, const YzHit *base) {
+    const int lane = lane_id();
+    const YzHit *l4 = yz_list(S, base, 4), *l5 = yz_list(S, base, 5);
+    const YzHit *l6 = yz_list(S, base, 6), *l7 = yz_list(S, base, 7);
+    YzAlive m;
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        const int i = w * 32 + lane;
+        bool a = false, b = false;
+        if (i < S.np[2]) {
+            const short2 p = S.pair[2][i];
+            a = (p.x >= 0 && l4[p.x].acc) || (p.y >= 0 && l5[p.y].acc);
+        }
+        if (i < S.np[3]) {
+            const short2 p = S.pair[3][i];
+            b = (p.x >= 0 && l6[p.x].acc) || (p.y >= 0 && l7[p.y].acc);
+        }
+        m.u[w] = __ballot_sync(0xffffffffu, a);
+        m.v[w] = __ballot_sync(0xffffffffu, b);
+    }
+    return m;
+}
+
+__device__ __forceinline__ int bits128(const unsigned m[4]) {
+    return __popc(m[0]) + __popc(m[1]) + __popc(m[2]) + __popc(m[3]);
+}
+
+__device__ __forceinline__ bool bit128(const unsigned m[4], int i) {
+    const unsigned w = i < 32 ? m[0] : (i < 64 ? m[1] : (i < 96 ? m[2] : m[3]));
+    return (w >> (i & 31)) & 1u;
+}
+
+// first set bit at index >= p (0 <= p), or -1
+__device__ __forceinline__ int next_bit128(const unsigned m[4], int p) {
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        if (w < (p >> 5)) continue;
+        unsigned v = m[w];
+        if (w == (p >> 5)) v &= ~0u << (p & 31);
+        if (v) return w * 32 + __ffs(v) - 1;
+    }
+    return -1;
+}
+
+// first outer iteration after (iu, iv), u fastest, with both pairs alive; -1 if none
+__device__ __forceinline__ int next_alive_outer(const YzAlive &m, int nu3, int iu, int iv) {
+    if (bit128(m.v, iv)) {
+        const int u = next_bit128(m.u, iu + 1);
+        if (u >= 0) return u + iv * nu3;
+    }
+    const int v = next_bit128(m.v, iv + 1);
+    const int u = next_bit128(m.u, 0);
+    return (v < 0 || u < 0) ? -1 : u + v * nu3;
+}
+
 __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l, long c1l, Stale st[4],
                                        const or_plane_t &P) {
     const int lane = lane_id();
@@ -651,19 +718,23 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
     // nu3, nv3) -- the reference's index order (u2 fastest) -- advanced by 32
     // per chunk with carries instead of divisions.
     int d0, d1, d2, d3, s0, s1, s2, s3;
-    {
-        const int c = c0 + lane;
+    auto set_digits = [&](int cb) {
+        const int c = cb + lane;
         const int g = c / C2, r = c - g * C2;
         d0 = r % nu2;
         d1 = r / nu2;
         d2 = g % nu3;
         d3 = g / nu3;
+    };
+    set_digits(c0);
+    {
         const int sg = 32 / C2, sr = 32 - sg * C2;
         s0 = sr % nu2;
         s1 = sr / nu2;
         s2 = sg % nu3;
         s3 = sg / nu3;
     }
+    const YzAlive alive = yz_alive(S, base);
     // station-3 part of the lane's current outer iteration (iu3, iv3): the
     // fit sums over its accepted hits in the reference order, their count,
     // and whether both u3 and v3 gave one (K:1326-1390); recomputed only
@@ -673,6 +744,18 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
     bool alive3 = false, need3 = true;
     int basec = c0;
     for (;;) {
+        if (basec < c1) {
+            // the chunk's first combination in a dead outer iteration: jump
+            // to the next live one (every combination in between is dead)
+            const int g = basec / C2;
+            const int iv = g / nu3, iu = g - iv * nu3;
+            if (!(bit128(alive.u, iu) && bit128(alive.v, iv))) {
+                const int gn = next_alive_outer(alive, nu3, iu, iv);
+                basec = gn < 0 ? c1 : min(gn * C2, c1);
+                if (basec < c1) set_digits(basec);
+                need3 = true;
+            }
+        }
         const bool more = basec < c1;
         if (!more && qn == 0) break;
         if (more) {
@@ -894,12 +977,16 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
                         continue;
                     }
                 }
+                const YzAlive al = yz_alive(S, base);
+                const long Ga = (long)bits128(al.u) * bits128(al.v);  // live outer iterations
+                if (Ga == 0) continue;  // no candidate and no scratch entry past 3 written
                 yz_xhits(S, T, P);
                 const long C = G * C2;
-                bool inline_it = C <= YZ_LIGHT && C <= budget;
+                const long Cl = Ga * C2 + G;  // live combinations, plus one step per outer iteration
+                bool inline_it = Cl <= YZ_LIGHT && Cl <= budget;
                 if (!inline_it) {
-                    // whole outer iterations per unit
-                    const long gper = max(1L, YZ_UNIT / C2);
+                    // whole outer iterations per unit, about YZ_UNIT live combinations each
+                    const long gper = max(1L, min(G, (YZ_UNIT * G) / (Ga * C2)));
                     const int nunits = (int)((G + gper - 1) / gper);
                     int hid = 0, u0 = 0;
                     if (lane == 0) {
@@ -928,7 +1015,7 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
                     }
                 }
                 if (inline_it) {
-                    budget -= C;
+                    budget -= Cl;
                     const unsigned long long bk = yz_range(S, E, base, 0, C, st, P);
                     __syncwarp();
                     if (bk != ~0ull) yz_store(T, S.b, S.nhx);

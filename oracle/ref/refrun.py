@@ -82,6 +82,9 @@ class RefKernels:
         self.tracks = torch.zeros(TRACKS_BYTES, dtype=torch.uint8, device=dev)
         self.plane = torch.zeros(C.sizeof(L.OrPlane), dtype=torch.uint8, device=dev)
         self.flags = torch.zeros(E, dtype=torch.uint8, device=dev)
+        # when a dict: device milliseconds of every launch, accumulated by
+        # kernel key (CUDA events on the launching stream around the launch)
+        self.timing = None
 
     def _chk(self, rc, what):
         if rc != 0:
@@ -96,6 +99,25 @@ class RefKernels:
             self.mod = C.c_void_p()
 
     # -- struct I/O ------------------------------------------------------------
+    def view(self, name, n):
+        """Typed device view of the first n events of one member: a hit
+        section by name ("nhits_cham", "hits_cham", ...), "ntracks",
+        "tracks" or "flags" -- for device-to-device copies and comparisons
+        against the library's DeviceBatch buffers, which use the same layout."""
+        t = self.torch
+        assert n <= E
+        if name == "flags":
+            return self.flags[:n]
+        if name == "ntracks":
+            return self.tracks[:2 * n * L.NSLOTS].view(t.int16)
+        if name == "tracks":
+            return self.tracks[_TRK_OFF:_TRK_OFF + 4 * n * L.EVT_TRK_FLOATS].view(t.float32)
+        per = {"nhits_cham": L.NCHAM, "hits_cham": L.EVT_CHAM_FLOATS, "nhits_hodo": L.NHODO,
+               "hits_hodo": L.EVT_HODO_FLOATS, "nhits_prop": L.NPROP, "hits_prop": L.EVT_PROP_FLOATS}[name]
+        off = {nm: o for nm, o, _ in _HIT_SECTIONS}[name]
+        v = self.hits[off:off + 4 * n * per]
+        return v.view(t.int32) if name.startswith("nhits") else v.view(t.float32)
+
     def set_plane(self, plane):
         self.plane.copy_(self.torch.frombuffer(bytearray(plane.to_bytes()), dtype=self.torch.uint8))
 
@@ -136,10 +158,17 @@ class RefKernels:
         vals = [C.c_void_p(p) for p in ptrs]
         args = (C.c_void_p * len(vals))(*[C.cast(C.byref(v), C.c_void_p) for v in vals])
         stream = C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+        if self.timing is not None:
+            ev = [self.torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record()
         self._chk(self.cu.cuLaunchKernel(self.fn[key], n, 1, 1, threads, 1, 1, 0, stream, args, None),
                   f"launch {key}")
+        if self.timing is not None:
+            ev[1].record()
         self.torch.cuda.synchronize()
         self._chk(self.cu.cuCtxSynchronize(), f"after {key}")
+        if self.timing is not None:
+            self.timing[key] = self.timing.get(key, 0.0) + ev[0].elapsed_time(ev[1])
 
     def event_reduce(self, n):
         self._launch("er", n, 8, self.hits.data_ptr(), self.flags.data_ptr())
