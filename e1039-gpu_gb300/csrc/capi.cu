@@ -16,6 +16,11 @@ cudaError_t launch_yz_tuned(const or_plane_t *, or_hits_view_t, or_tracks_view_t
 cudaError_t launch_yz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *, void *,
                       int, int, int, cudaStream_t, int);
 size_t yz_scratch_bytes(int, int, int);
+cudaError_t launch_vertexing(const or_plane_t *, or_tracks_view_t, const uint8_t *, int, cudaStream_t, int);
+cudaError_t launch_dimuons(const or_plane_t *, or_tracks_view_t, or_dimuons_view_t, const uint8_t *, int,
+                           cudaStream_t, int);
+cudaError_t launch_histograms(or_tracks_view_t, or_dimuons_view_t, const int32_t *, const uint8_t *, or_hists_t *,
+                              int, cudaStream_t, int);
 cudaError_t launch_back_clean(or_tracks_view_t, const uint8_t *, int, cudaStream_t, int, int);
 cudaError_t launch_global(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
                           unsigned long long *, cudaStream_t, int, int);
@@ -336,6 +341,73 @@ int or_run_selection(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks
     cudaError_t e = orgpu::launch_select(ctx->d_plane, hits, tracks, toomany, n_events, 1, 1, S(stream), ctx->sm_count,
                                          ctx->warps[OR_K_SELECT]);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "post-global selection");
+}
+
+/* ---- vertexing, dimuons, histograms ------------------------------------ */
+
+static int check_dimuons(or_dimuons_view_t d) {
+    if (!d.ndimuons || !d.dimuons) return fail(OR_ERR_ARG, "null dimuon view pointer");
+    return OR_OK;
+}
+
+int or_vertexing(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
+    if ((rc = check_tracks(tracks))) return rc;
+    cudaError_t e = orgpu::launch_vertexing(ctx->d_plane, tracks, toomany, n_events, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "vertexing");
+}
+
+int or_dimuons(or_ctx_t *ctx, or_tracks_view_t tracks, or_dimuons_view_t dimuons, const uint8_t *toomany,
+               int n_events, void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
+    if ((rc = check_tracks(tracks)) || (rc = check_dimuons(dimuons))) return rc;
+    cudaError_t e = orgpu::launch_dimuons(ctx->d_plane, tracks, dimuons, toomany, n_events, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "dimuon building");
+}
+
+int or_fill_histograms(or_ctx_t *ctx, or_tracks_view_t tracks, or_dimuons_view_t dimuons,
+                       const int32_t *trigger_bits, const uint8_t *toomany, or_hists_t *d_hists, int n_events,
+                       void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany || !d_hists) return fail(OR_ERR_ARG, "bad event count, flags or histogram table");
+    if ((rc = check_tracks(tracks)) || (rc = check_dimuons(dimuons))) return rc;
+    cudaError_t e = orgpu::launch_histograms(tracks, dimuons, trigger_bits, toomany, d_hists, n_events, S(stream),
+                                             ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "histogram fill");
+}
+
+void or_hist_table_init(or_hists_t *h) {
+    /* histotools binning (reconstruction_constants.h:225-266) in the order of
+     * online_reconstruction.cu:670-694; centres as M:718 computes them */
+    static const short nb[OR_HIST_NVARS] = {100, 100, 100, 100, 100, 200, 50, 50, 50, 50, 50, 50,
+                                            100, 100, 100, 100, 100, 200};
+    static const float lo[OR_HIST_NVARS] = {-20.f, -20.f, 0.f, -20.f, -20.f, -500.f, 0.f, 0.f, 0.f, 0.f, 0.f,
+                                            -3.141592654f, -20.f, -20.f, 0.f, -20.f, -20.f, -500.f};
+    static const float hi[OR_HIST_NVARS] = {20.f, 20.f, 120.f, 20.f, 20.f, 500.f, 10.f, 1.f, 1.f, 0.5f, 5.f,
+                                            3.141592654f, 20.f, 20.f, 120.f, 20.f, 20.f, 500.f};
+    if (!h) return;
+    std::memset(h, 0, sizeof(*h));
+    for (int t = 0; t < OR_HIST_NTRIGGERS; ++t)
+        for (int k = 0; k < OR_HIST_NVARS; ++k) {
+            const int i = t * OR_HIST_NVARS + k;
+            h->nbins[i] = nb[k];
+            h->pts_hw[i] = (hi[k] - lo[k]) * 0.5f / nb[k];
+            for (int l = 0; l < nb[k]; ++l) h->xpts[i * OR_HIST_NBINS_MAX + l] = lo[k] + h->pts_hw[k] * (2.f * l + 1.f);
+        }
+}
+
+int or_run_physics(or_ctx_t *ctx, or_tracks_view_t tracks, or_dimuons_view_t dimuons, const int32_t *trigger_bits,
+                   const uint8_t *toomany, or_hists_t *d_hists, int n_events, void *stream) {
+    int rc = or_vertexing(ctx, tracks, toomany, n_events, stream);
+    if (rc) return rc;
+    if ((rc = or_dimuons(ctx, tracks, dimuons, toomany, n_events, stream))) return rc;
+    if (!d_hists) return OR_OK;
+    return or_fill_histograms(ctx, tracks, dimuons, trigger_bits, toomany, d_hists, n_events, stream);
 }
 
 /* ---- learned tracklet scorer ------------------------------------------- */

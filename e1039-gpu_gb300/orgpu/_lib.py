@@ -21,7 +21,8 @@ EXPORTS = ("or_version", "or_last_error", "or_status_string", "or_geometry_load"
            "or_tracklet_features", "or_mlp_score", "or_keep_mask", "or_yz_pruned", "or_run_batch_learned",
            "or_tracklet_labels", "or_track_agreement", "or_mlp_grad_blocks", "or_mlp_forward", "or_mlp_gradient",
            "or_mlp_adam", "or_prop_matching", "or_global_clean", "or_run_selection", "or_set_launch",
-           "or_get_launch")
+           "or_get_launch", "or_vertexing", "or_dimuons", "or_fill_histograms", "or_hist_table_init",
+           "or_run_physics")
 
 # tunable kernels (or_kernel_id_t)
 KERNELS = {"event_reduce": 0, "xz": 1, "yz": 2, "back_clean": 3, "global": 4, "select": 5, "features": 6}
@@ -94,6 +95,12 @@ def lib():
     lb.or_prop_matching.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, i32, vp]
     lb.or_global_clean.argtypes = [vp, L.OrTracksView, vp, i32, vp]
     lb.or_run_selection.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, i32, vp]
+    lb.or_vertexing.argtypes = [vp, L.OrTracksView, vp, i32, vp]
+    lb.or_dimuons.argtypes = [vp, L.OrTracksView, L.OrDimuonsView, vp, i32, vp]
+    lb.or_fill_histograms.argtypes = [vp, L.OrTracksView, L.OrDimuonsView, vp, vp, vp, i32, vp]
+    lb.or_hist_table_init.argtypes = [C.POINTER(L.OrHists)]
+    lb.or_hist_table_init.restype = None
+    lb.or_run_physics.argtypes = [vp, L.OrTracksView, L.OrDimuonsView, vp, vp, vp, i32, vp]
     for name in EXPORTS:
         getattr(lb, name)
     _lib = lb

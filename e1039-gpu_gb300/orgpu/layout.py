@@ -29,6 +29,21 @@ TRK_ERR_TX, TRK_ERR_TY, TRK_ERR_X0, TRK_ERR_Y0, TRK_ERR_INVP, TRK_CHARGE = 10, 1
 TRK_HIT_DETID, TRK_HIT_CHAN, TRK_HIT_POS, TRK_HIT_DRIFT = 22, 40, 58, 76
 TRK_HIT_SIGN, TRK_HIT_TDC, TRK_HIT_RESID = 94, 112, 130
 
+TRK_VX, TRK_PX = 16, 19  # vertex position and momentum, written by vertexing
+
+# dimuon collections (reconstruction_classes.cuh:870-936, reconstruction_constants.h:183-184)
+DIMUON_MAX, NDIMUONPARAM = 16, 36
+EVT_DIM_FLOATS = DIMUON_MAX * NDIMUONPARAM
+DIM_MASS, DIM_PT, DIM_XF, DIM_X1, DIM_X2, DIM_COSTHETA, DIM_PHI = 0, 1, 2, 3, 4, 5, 6
+DIM_MASS_SINGLE, DIM_CHI2_SINGLE, DIM_VTX, DIM_POS_VTX, DIM_NEG_VTX = 7, 8, 9, 12, 15
+DIM_POS_P, DIM_NEG_P, DIM_POS_P_SINGLE, DIM_NEG_P_SINGLE = 18, 22, 26, 30
+DIM_CHI2_VTX, DIM_CHI2_KF = 34, 35
+# fields the reference never computes (stored as 0 here)
+DIM_UNSET_FIELDS = (DIM_MASS_SINGLE, DIM_CHI2_SINGLE, DIM_CHI2_VTX, DIM_CHI2_KF)
+
+# monitoring histograms (reconstruction_classes.cuh:938-944, reconstruction_constants.h:216-266)
+HIST_NTRIGGERS, HIST_NVARS, HIST_NVARS_TRACKS, HIST_NBINS_MAX = 11, 18, 6, 256
+
 # the 24 chamber planes the E1039 configuration reads (reconstruction_constants.h:60)
 EFF_DETID_CHAMBERS = (1, 2, 3, 4, 5, 6, 13, 14, 15, 16, 17, 18,
                       19, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30)
@@ -156,6 +171,50 @@ class HostHits:
         n = int(cnt[e * per + k])
         base = e * stride + NHITSPARAM * cap * k
         return n, data[base:base + NHITSPARAM * n].reshape(NHITSPARAM, n)
+
+
+class OrDimuonsView(C.Structure):
+    _fields_ = [("ndimuons", C.c_void_p), ("dimuons", C.c_void_p)]
+
+
+class OrHists(C.Structure):
+    """or_hists_t == the reference's gHistsArrays."""
+    _fields_ = [("nbins", C.c_int16 * (HIST_NTRIGGERS * HIST_NVARS)),
+                ("pts_hw", C.c_float * (HIST_NTRIGGERS * HIST_NVARS)),
+                ("xpts", C.c_float * (HIST_NTRIGGERS * HIST_NVARS * HIST_NBINS_MAX)),
+                ("values", C.c_float * (HIST_NTRIGGERS * HIST_NVARS * HIST_NBINS_MAX))]
+
+    def values_array(self):
+        """values as [trigger, variable, bin] (a copy)."""
+        return np.ctypeslib.as_array(self.values).reshape(HIST_NTRIGGERS, HIST_NVARS, HIST_NBINS_MAX).copy()
+
+    def to_bytes(self):
+        return bytes(C.string_at(C.addressof(self), C.sizeof(self)))
+
+    @classmethod
+    def from_bytes(cls, b):
+        h = cls()
+        C.memmove(C.addressof(h), bytes(b), C.sizeof(cls))
+        return h
+
+
+class HostDimuons:
+    """Dimuon collections of n events."""
+
+    def __init__(self, n_events):
+        self.n = n_events
+        self.ndimuons = np.zeros(n_events, np.uint16)
+        self.dimuons = np.zeros(n_events * EVT_DIM_FLOATS, np.float32)
+
+    def view(self):
+        v = OrDimuonsView()
+        v.ndimuons = self.ndimuons.ctypes.data
+        v.dimuons = self.dimuons.ctypes.data
+        return v
+
+    def records(self, e):
+        n = min(int(self.ndimuons[e]), DIMUON_MAX)
+        return self.dimuons[e * EVT_DIM_FLOATS:e * EVT_DIM_FLOATS + n * NDIMUONPARAM].reshape(n, NDIMUONPARAM)
 
 
 class HostTracks:

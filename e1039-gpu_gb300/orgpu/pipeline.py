@@ -99,6 +99,52 @@ class DeviceBatch:
         return t
 
 
+class DeviceDimuons:
+    """Device dimuon collections of n events (reference layout)."""
+
+    def __init__(self, n_events, device=0):
+        torch = _torch()
+        dev = torch.device("cuda", device)
+        self.n = int(n_events)
+        self.ndimuons = torch.zeros(self.n, dtype=torch.int16, device=dev)
+        self.dimuons = torch.zeros(self.n * L.EVT_DIM_FLOATS, dtype=torch.float32, device=dev)
+
+    def view(self):
+        v = L.OrDimuonsView()
+        v.ndimuons = self.ndimuons.data_ptr()
+        v.dimuons = self.dimuons.data_ptr()
+        return v
+
+    def download(self):
+        d = L.HostDimuons.__new__(L.HostDimuons)
+        d.n = self.n
+        d.ndimuons = self.ndimuons.cpu().numpy().view(np.uint16)
+        d.dimuons = self.dimuons.cpu().numpy()
+        return d
+
+
+class DeviceHists:
+    """The histogram tables (or_hists_t) in device memory, initialised with
+    the reference's binning (or_hist_table_init) and zero counts."""
+
+    def __init__(self, device=0):
+        torch = _torch()
+        h = L.OrHists()
+        _lib.lib().or_hist_table_init(C.byref(h))
+        raw = np.frombuffer(h.to_bytes(), np.uint8).copy()
+        self.buf = torch.from_numpy(raw).to(torch.device("cuda", device))
+
+    def ptr(self):
+        return self.buf.data_ptr()
+
+    def zero_counts(self):
+        off = L.OrHists.values.offset
+        self.buf[off:].zero_()
+
+    def download(self):
+        return L.OrHists.from_bytes(self.buf.cpu().numpy().tobytes())
+
+
 class Reconstruction:
     """One library context (one device) with its geometry."""
 
@@ -161,6 +207,28 @@ class Reconstruction:
     def selection(self, b, stream=None):
         _lib.check(self.lib.or_run_selection(self.ctx, b.hits_view(), b.tracks_view(), b.toomany.data_ptr(), b.n,
                                              self._stream(stream)), "or_run_selection")
+
+    # after the selection (online_reconstruction.cu:939-983)
+    def vertexing(self, b, stream=None):
+        _lib.check(self.lib.or_vertexing(self.ctx, b.tracks_view(), b.toomany.data_ptr(), b.n, self._stream(stream)),
+                   "or_vertexing")
+
+    def dimuons(self, b, d, stream=None):
+        _lib.check(self.lib.or_dimuons(self.ctx, b.tracks_view(), d.view(), b.toomany.data_ptr(), b.n,
+                                       self._stream(stream)), "or_dimuons")
+
+    def fill_histograms(self, b, d, hists, trigger_bits=None, stream=None):
+        """Add this batch's counts into hists (DeviceHists); trigger_bits: a
+        device int32 tensor of b.n entries or None."""
+        tb = None if trigger_bits is None else trigger_bits.data_ptr()
+        _lib.check(self.lib.or_fill_histograms(self.ctx, b.tracks_view(), d.view(), tb, b.toomany.data_ptr(),
+                                               hists.ptr(), b.n, self._stream(stream)), "or_fill_histograms")
+
+    def run_physics(self, b, d, hists=None, trigger_bits=None, stream=None):
+        tb = None if trigger_bits is None else trigger_bits.data_ptr()
+        _lib.check(self.lib.or_run_physics(self.ctx, b.tracks_view(), d.view(), tb, b.toomany.data_ptr(),
+                                           None if hists is None else hists.ptr(), b.n, self._stream(stream)),
+                   "or_run_physics")
 
     def run_batch(self, b, stream=None):
         _lib.check(self.lib.or_run_batch(self.ctx, b.hits_view(), b.tracks_view(), b.ntracklets.data_ptr(),

@@ -260,6 +260,13 @@ def generate(geo, cfg):
     return rec, offsets, truth
 
 
+def trigger_bits(n_events, seed=906010):
+    """Per-event trigger words (int32): the reference reads them from the raw
+    event (gEvent::TriggerBits, online_reconstruction.cu:346); here ten
+    seeded independent bits, each set with probability 1/2."""
+    return np.random.default_rng(seed).integers(0, 1 << 10, n_events).astype(np.int32)
+
+
 def cap_records(records, offsets):
     """Drop hits beyond each plane's slot capacity (the reference host writes
     past the slot otherwise, online_reconstruction.cu:406-417)."""

@@ -121,6 +121,31 @@ int or_global_clean(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *tooma
 int or_run_selection(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany,
                      int n_events, void *stream);
 
+/* After the selection (online_reconstruction.cu:939-983), reconstruction_kernels.cuh:
+ *   or_vertexing        <- gKernel_Vertexing (tracks, z, flags)                     :2542
+ *                          stationID >= 6 tracks swum back through FMag in double:
+ *                          stationID 7, vertex position and momentum
+ *   or_dimuons          <- gKernel_DimuonBuilding (tracks, dimuons, z, flags)       :2820
+ *                          opposite-charge pairs of vertexed tracks, closest
+ *                          approach, kinematics, cuts; ndimuons written for every
+ *                          accepted event
+ *   or_fill_histograms  <- gKernel_fill_display_histograms (tracks, dimuons,
+ *                          hists, trigger bits, flags)                             :3100
+ *                          adds exact counts into d_hists->values (device
+ *                          memory); trigger_bits may be NULL (all zero)
+ *   or_hist_table_init     the host's table setup (online_reconstruction.cu:670-723)
+ *                          into host memory, values zeroed
+ *   or_run_physics         the three kernels in order; d_hists may be NULL. */
+int or_vertexing(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, void *stream);
+int or_dimuons(or_ctx_t *ctx, or_tracks_view_t tracks, or_dimuons_view_t dimuons, const uint8_t *toomany,
+               int n_events, void *stream);
+int or_fill_histograms(or_ctx_t *ctx, or_tracks_view_t tracks, or_dimuons_view_t dimuons,
+                       const int32_t *trigger_bits, const uint8_t *toomany, or_hists_t *d_hists, int n_events,
+                       void *stream);
+void or_hist_table_init(or_hists_t *host_table);
+int or_run_physics(or_ctx_t *ctx, or_tracks_view_t tracks, or_dimuons_view_t dimuons, const int32_t *trigger_bits,
+                   const uint8_t *toomany, or_hists_t *d_hists, int n_events, void *stream);
+
 /* Map the reference's fixed-capacity structs (EstnEvtMax = 10000 events)
  * onto views.  `coll` points at a gEventHitCollections / gEventTrackCollection
  * laid out exactly as reconstruction_classes.cuh:76-87 / :542-544. */

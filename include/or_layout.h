@@ -164,6 +164,53 @@ typedef struct or_tracks_view {
     float *tracks;     /* [n_events*512*148] */
 } or_tracks_view_t;
 
+/* Dimuon collections (gEventDimuonCollection, reconstruction_classes.cuh:
+ * 870-936): per event a count and 16 records of 36 floats, written by
+ * or_dimuons (gKernel_DimuonBuilding, reconstruction_kernels.cuh:2820-3090). */
+#define OR_DIMUON_MAX 16     /* datasizes::DimuonSizeMax, reconstruction_constants.h:184 */
+#define OR_NDIMUONPARAM 36   /* datasizes::NDimuonParam, :183 */
+#define OR_EVT_DIM_FLOATS (OR_DIMUON_MAX * OR_NDIMUONPARAM)
+enum {
+    OR_DIM_MASS = 0,
+    OR_DIM_PT = 1,
+    OR_DIM_XF = 2,
+    OR_DIM_X1 = 3,
+    OR_DIM_X2 = 4,
+    OR_DIM_COSTHETA = 5,
+    OR_DIM_PHI = 6,
+    OR_DIM_MASS_SINGLE = 7, /* never computed by the reference: 0 here */
+    OR_DIM_CHI2_SINGLE = 8, /* never computed by the reference: 0 here */
+    OR_DIM_VTX = 9,         /* 3 floats */
+    OR_DIM_POS_VTX = 12,    /* 3 */
+    OR_DIM_NEG_VTX = 15,    /* 3 */
+    OR_DIM_POS_P = 18,      /* px, py, pz, E */
+    OR_DIM_NEG_P = 22,
+    OR_DIM_POS_P_SINGLE = 26,
+    OR_DIM_NEG_P_SINGLE = 30,
+    OR_DIM_CHI2_VTX = 34, /* never computed by the reference: 0 here */
+    OR_DIM_CHI2_KF = 35   /* never computed by the reference: 0 here */
+};
+
+typedef struct or_dimuons_view {
+    uint16_t *ndimuons; /* [n_events] */
+    float *dimuons;     /* [n_events*16*36] */
+} or_dimuons_view_t;
+
+/* Monitoring histograms (gHistsArrays, reconstruction_classes.cuh:938-944):
+ * 11 trigger classes x 18 variables (6 per track, 12 per dimuon), each a
+ * table of at most 256 bins given by centre and half width.  Same byte
+ * layout as the reference struct. */
+#define OR_HIST_NTRIGGERS 11   /* histotools::ntriggers, reconstruction_constants.h:217 */
+#define OR_HIST_NVARS 18       /* histotools::nvars_total, :223 */
+#define OR_HIST_NVARS_TRACKS 6 /* :220 */
+#define OR_HIST_NBINS_MAX 256  /* :218 */
+typedef struct or_hists {
+    int16_t nbins[OR_HIST_NTRIGGERS * OR_HIST_NVARS];
+    float pts_hw[OR_HIST_NTRIGGERS * OR_HIST_NVARS];
+    float xpts[OR_HIST_NTRIGGERS * OR_HIST_NVARS * OR_HIST_NBINS_MAX];
+    float values[OR_HIST_NTRIGGERS * OR_HIST_NVARS * OR_HIST_NBINS_MAX];
+} or_hists_t;
+
 /* Compact hit record, the raw-event format of the reference's input
  * (OnlineReconstruction/LoadInput.h:10-20: detectorID, elementID, tdcTime,
  * driftDistance, plus the in-time flag bit the host packer turns into

@@ -81,6 +81,18 @@ void orc_global_clean(or_tracks_view_t t, const uint8_t *toomany, int n_events, 
 int64_t orc_tracklet_features(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, const uint8_t *toomany,
                               int n_events, int32_t *row_off, float *feat, int64_t max_rows);
 
+/* after global tracking (or_physics.c): vertexing (gKernel_Vertexing,
+ * reconstruction_kernels.cuh:2542-2810), dimuons (gKernel_DimuonBuilding,
+ * :2820-3090), the histogram table (online_reconstruction.cu:670-723) and the
+ * histogram fill (gKernel_fill_display_histograms, :3100-3195); trigger_bits
+ * may be NULL (all zero) */
+void orc_vertexing(const or_plane_t *p, or_tracks_view_t t, const uint8_t *toomany, int n_events, int n_threads);
+void orc_dimuons(const or_plane_t *p, or_tracks_view_t t, or_dimuons_view_t d, const uint8_t *toomany, int n_events,
+                 int n_threads);
+void orc_hist_table(or_hists_t *h);
+void orc_fill_histograms(or_tracks_view_t t, or_dimuons_view_t d, or_hists_t *h, const int32_t *trigger_bits,
+                         const uint8_t *toomany, int n_events);
+
 int orc_hardware_threads(void);
 
 #ifdef __cplusplus

@@ -18,7 +18,7 @@ from orgpu import layout as L  # noqa: E402
 
 LIB_PATH = os.path.join(HERE, "liborc.so")
 LIB64_PATH = os.path.join(HERE, "liborc64.so")  # the same code with FP64 fits, residuals and chi2 sums
-SOURCES = [os.path.join(HERE, "or_oracle.c")]
+SOURCES = [os.path.join(HERE, "or_oracle.c"), os.path.join(HERE, "or_physics.c")]
 
 ST_TOOMANY_ER, ST_TOOMANY_XZBIN, ST_TOOMANY_TKL = 1, 2, 4
 NCOUNTS = 8
@@ -90,6 +90,11 @@ def _load(path):
         _lib.orc_tracklet_features.argtypes = [P(L.OrPlane), L.OrHitsView, L.OrTracksView, C.c_void_p, C.c_int,
                                                C.c_void_p, C.c_void_p, C.c_int64]
         _lib.orc_tracklet_features.restype = C.c_int64
+        _lib.orc_vertexing.argtypes = [P(L.OrPlane), L.OrTracksView, C.c_void_p, C.c_int, C.c_int]
+        _lib.orc_dimuons.argtypes = [P(L.OrPlane), L.OrTracksView, L.OrDimuonsView, C.c_void_p, C.c_int, C.c_int]
+        _lib.orc_hist_table.argtypes = [P(L.OrHists)]
+        _lib.orc_fill_histograms.argtypes = [L.OrTracksView, L.OrDimuonsView, P(L.OrHists), C.c_void_p, C.c_void_p,
+                                             C.c_int]
     return _lib
 
 
@@ -163,6 +168,26 @@ def tracklet_features(plane, hits, tracks, toomany, max_rows=None):
                                        np.ascontiguousarray(toomany, np.uint8).ctypes.data, n, row_off.ctypes.data,
                                        feat.ctypes.data, cap)
     return row_off, feat[:min(rows, cap)]
+
+
+def vertexing(plane, tracks, state, n_threads=0):
+    lib().orc_vertexing(C.byref(plane), tracks.view(), state.toomany.ctypes.data, tracks.n, n_threads)
+
+
+def dimuons(plane, tracks, dims, state, n_threads=0):
+    lib().orc_dimuons(C.byref(plane), tracks.view(), dims.view(), state.toomany.ctypes.data, tracks.n, n_threads)
+
+
+def hist_table():
+    h = L.OrHists()
+    lib().orc_hist_table(C.byref(h))
+    return h
+
+
+def fill_histograms(tracks, dims, hists, trigger_bits, state):
+    tb = None if trigger_bits is None else np.ascontiguousarray(trigger_bits, np.int32)
+    lib().orc_fill_histograms(tracks.view(), dims.view(), C.byref(hists), None if tb is None else tb.ctypes.data,
+                              state.toomany.ctypes.data, tracks.n)
 
 
 def hardware_threads():

@@ -40,7 +40,14 @@ KERNELS = {
     "prop": "_Z27gKernel_PropSegmentMatchingP20gEventHitCollectionsP21gEventTrackCollectionPKfPKb",
     "gclean": "_Z27gKernel_GlobalTrackCleaningP21gEventTrackCollectionPKb",
     "gclean_x": "_Z40gKernel_GlobalTrackCleaning_crossthreadsP21gEventTrackCollectionPKb",
+    "vertexing": "_Z17gKernel_VertexingP21gEventTrackCollectionPKfPb",
+    "dimuons": "_Z22gKernel_DimuonBuildingP21gEventTrackCollectionP22gEventDimuonCollectionPKfPKb",
+    "hists": "_Z31gKernel_fill_display_histogramsP21gEventTrackCollectionP22gEventDimuonCollectionP12gHistsArraysPKiPKb",
 }
+# gEventDimuonCollection (reconstruction_classes.cuh:870-872): unsigned short
+# NDimuons[E], then float DimuonsRawData[E*16*36] (4-byte aligned after 2*E bytes)
+DIM_DATA_OFF = 2 * E
+DIMS_BYTES = DIM_DATA_OFF + 4 * E * L.EVT_DIM_FLOATS
 
 # byte offsets of the members of gEventHitCollections (4-byte members, no padding)
 _HIT_SECTIONS = []
@@ -82,6 +89,10 @@ class RefKernels:
         self.tracks = torch.zeros(TRACKS_BYTES, dtype=torch.uint8, device=dev)
         self.plane = torch.zeros(C.sizeof(L.OrPlane), dtype=torch.uint8, device=dev)
         self.flags = torch.zeros(E, dtype=torch.uint8, device=dev)
+        self.dims = torch.zeros(DIMS_BYTES, dtype=torch.uint8, device=dev)
+        self.hists = torch.zeros(C.sizeof(L.OrHists), dtype=torch.uint8, device=dev)
+        self.trig = torch.zeros(E, dtype=torch.int32, device=dev)
+        self.flags_hist = torch.zeros(E, dtype=torch.uint8, device=dev)
         # when a dict: device milliseconds of every launch, accumulated by
         # kernel key (CUDA events on the launching stream around the launch)
         self.timing = None
@@ -188,6 +199,45 @@ class RefKernels:
                      self.flags.data_ptr())
         self._launch("gclean", n, 32, self.tracks.data_ptr(), self.flags.data_ptr())
         self._launch("gclean_x", n, 32, self.tracks.data_ptr(), self.flags.data_ptr())
+
+    def vertexing(self, n):
+        """gKernel_Vertexing<<<n, 32>>>(tracks, plane z, flags) (M:939-945)."""
+        self._launch("vertexing", n, 32, self.tracks.data_ptr(), self.plane.data_ptr(), self.flags.data_ptr())
+
+    def dimuons(self, n):
+        """gKernel_DimuonBuilding<<<n, 1>>>(tracks, dimuons, plane z, flags) (M:962-968)."""
+        self._launch("dimuons", n, 1, self.tracks.data_ptr(), self.dims.data_ptr(), self.plane.data_ptr(),
+                     self.flags.data_ptr())
+
+    def histograms(self, events, table, trigger_bits):
+        """gKernel_fill_display_histograms<<<., 1>>> (M:983) on the given
+        events, one event per launch: the kernel adds with a plain "+=" from
+        every block, so concurrent blocks would lose counts.  The kernel
+        indexes every per-event array with blockIdx.x, so event e runs as
+        block e of a grid of e+1 blocks whose other blocks see the "too many
+        hits" flag and return at once.  `table` is an OrHists with the binning
+        and the starting counts; returns the OrHists after the fills."""
+        self.hists.copy_(self.torch.frombuffer(bytearray(table.to_bytes()), dtype=self.torch.uint8))
+        n = len(trigger_bits)
+        self.trig[:n].copy_(self.torch.from_numpy(np.ascontiguousarray(trigger_bits, np.int32)))
+        for e in events:
+            e = int(e)
+            self.flags_hist[:e].fill_(1)
+            self.flags_hist[e] = self.flags[e]
+            self._launch("hists", e + 1, 1, self.tracks.data_ptr(), self.dims.data_ptr(), self.hists.data_ptr(),
+                         self.trig.data_ptr(), self.flags_hist.data_ptr())
+        return L.OrHists.from_bytes(self.hists.cpu().numpy().tobytes())
+
+    def put_dimuons(self, d):
+        assert d.n <= E
+        self.dims[:d.ndimuons.nbytes].copy_(self.torch.from_numpy(d.ndimuons.view(np.uint8)))
+        self.dims[DIM_DATA_OFF:DIM_DATA_OFF + d.dimuons.nbytes].copy_(self.torch.from_numpy(d.dimuons.view(np.uint8)))
+
+    def get_dimuons(self, n):
+        d = L.HostDimuons(n)
+        d.ndimuons[:] = self.dims[:2 * n].cpu().numpy().view(np.uint16)
+        d.dimuons[:] = self.dims[DIM_DATA_OFF:DIM_DATA_OFF + 4 * n * L.EVT_DIM_FLOATS].cpu().numpy().view(np.float32)
+        return d
 
     def global_tracking(self, n):
         self._launch("global", n, 32, self.hits.data_ptr(), self.tracks.data_ptr(), self.plane.data_ptr(),

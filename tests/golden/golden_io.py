@@ -118,6 +118,67 @@ def compare_tracks(a, b, rtol=0.0, resid_atol=None):
     return res
 
 
+def compact_dimuons(d, toomany=None):
+    """(ndimuons uint16 [n], records float32 [m, 36]) with the fields the
+    reference never computes set to 0."""
+    nd = d.ndimuons[:d.n].astype(np.uint16).copy()
+    if toomany is not None:
+        nd[np.asarray(toomany, bool)] = 0
+    nd = np.minimum(nd, L.DIMUON_MAX)
+    recs = [d.dimuons[e * L.EVT_DIM_FLOATS:e * L.EVT_DIM_FLOATS + int(nd[e]) * L.NDIMUONPARAM]
+            for e in range(d.n)]
+    r = (np.concatenate(recs) if recs else np.zeros(0, np.float32)).reshape(-1, L.NDIMUONPARAM).copy()
+    r[:, list(L.DIM_UNSET_FIELDS)] = 0.0
+    return nd, r
+
+
+def compare_dimuons(a, b, rtol=0.0, phi_ulps=0):
+    """Events whose dimuon counts differ, and records that differ: every
+    field bit for bit (rtol == 0) or within rtol relative (1e-6 absolute
+    near zero); phi within phi_ulps units in the last place (atan2f differs
+    by a few ulps between the C library and CUDA)."""
+    nda, ra = a
+    ndb, rb = b
+    res = {"events": int(nda.shape[0]), "dimuons": int(ra.shape[0]), "count_mismatch": [], "value_mismatch": []}
+    res["count_mismatch"] = [int(e) for e in np.nonzero(nda != ndb)[0]]
+    if res["count_mismatch"] or ra.shape != rb.shape:
+        return res
+    fields = np.ones(L.NDIMUONPARAM, bool)
+    if phi_ulps:
+        fields[L.DIM_PHI] = False
+        ua, ub = ra[:, L.DIM_PHI].view(np.int32).astype(np.int64), rb[:, L.DIM_PHI].view(np.int32).astype(np.int64)
+        phi_bad = np.abs(ua - ub) > phi_ulps
+    else:
+        phi_bad = np.zeros(len(ra), bool)
+    if rtol == 0.0:
+        bad = (ra[:, fields].view(np.uint32) != rb[:, fields].view(np.uint32)).any(axis=1) | phi_bad
+    else:
+        err = np.abs(ra.astype(np.float64) - rb.astype(np.float64))[:, fields]
+        tol = np.maximum(rtol * np.maximum(np.abs(ra), np.abs(rb))[:, fields], 1e-6)
+        both_nan = (np.isnan(ra) & np.isnan(rb))[:, fields]
+        bad = ((err > tol) & ~both_nan).any(axis=1) | phi_bad
+    res["value_mismatch"] = [int(i) for i in np.nonzero(bad)[0]]
+    return res
+
+
+def compare_hists(a, b, phi_slack=0):
+    """Histogram counts [trigger, variable, bin]: every table equal, except
+    that the dimuon phi table (variable 11) may move up to phi_slack counts
+    between neighbouring bins (a last-place difference in phi at a bin edge).
+    Returns the (trigger, variable) tables that differ."""
+    va, vb = a.values_array(), b.values_array()
+    out = []
+    for t in range(L.HIST_NTRIGGERS):
+        for k in range(L.HIST_NVARS):
+            x, y = va[t, k], vb[t, k]
+            if k == 11 and phi_slack:
+                if x.sum() != y.sum() or np.abs(x - y).sum() > 2 * phi_slack:
+                    out.append((t, k))
+            elif not np.array_equal(x, y):
+                out.append((t, k))
+    return out
+
+
 def select_events(rec, off, idx):
     """Records and offsets of the events `idx` (in that order)."""
     idx = np.asarray(idx, np.int64)

@@ -14,6 +14,11 @@ the oracle's:
   global  gKernel_Global_tracking on the oracle's cleaned tracks
   sel     gKernel_PropSegmentMatching + gKernel_GlobalTrackCleaning{,_crossthreads}
           on the oracle's global tracks
+  vtx     gKernel_Vertexing on the oracle's selected tracks
+  dim     gKernel_DimuonBuilding on the oracle's vertexed tracks
+  hist    gKernel_fill_display_histograms on the oracle's tracks and dimuons,
+          with seeded trigger words, one event per launch (its "+=" from
+          concurrent blocks would lose counts)
 
 The reference XZ kernel is not run (barriers in divergent code).  Events
 are first checked against the reference's array bounds with the oracle's
@@ -60,7 +65,7 @@ CONFIGS = [
 class Snap:
     """Oracle state after every stage, plus the per-event domain counters."""
 
-    def __init__(self, plane, hits0):
+    def __init__(self, plane, hits0, trig=None):
         n = hits0.n
         st = O.OracleState(n)
         self.hits0 = hits0
@@ -81,6 +86,14 @@ class Snap:
         O.prop_matching(plane, self.hits_er, ts, st)
         O.global_clean(ts, st)
         self.tracks_sel = ts
+        tv = ts.copy()
+        O.vertexing(plane, tv, st)
+        self.tracks_vtx = tv
+        self.dims = L.HostDimuons(n)
+        O.dimuons(plane, tv, self.dims, st)
+        self.trig = S.trigger_bits(n) if trig is None else np.asarray(trig, np.int32)
+        self.hists = O.hist_table()
+        O.fill_histograms(tv, self.dims, self.hists, self.trig, st)
         # domain counters from a counted run of the whole chain
         h2, t2, st2 = hits0.copy(), L.HostTracks(n), O.OracleState(n)
         O.run_all(plane, h2, t2, st2, counted=True)
@@ -90,7 +103,11 @@ class Snap:
 def in_domain(hits0, snap):
     n = hits0.n
     raw = hits0.nhits_cham.reshape(n, L.NCHAM).max(axis=1)
-    return (raw <= MAX_CHAM_RAW) & (snap.counts[:, 6] <= MAX_WINDOW) & (snap.counts[:, 7] <= MAX_WINDOW)
+    # the reference's dimuon kernel stores a 17th dimuon past its event's 16
+    # records (K:3059), beyond its buffer for the last event: keep events the
+    # oracle gives fewer than 16
+    return ((raw <= MAX_CHAM_RAW) & (snap.counts[:, 6] <= MAX_WINDOW) & (snap.counts[:, 7] <= MAX_WINDOW) &
+            (snap.dims.ndimuons < L.DIMUON_MAX))
 
 
 def recomputed_flags(h):
@@ -138,6 +155,17 @@ def run_reference(rk, plane, snap, n):
     rk.put_tracks(snap.tracks_global)
     rk.selection(n)
     out["tracks_sel"] = rk.get_tracks(n)
+    # vertexing, dimuons (M:939-968)
+    rk.put_tracks(snap.tracks_sel)
+    rk.vertexing(n)
+    out["tracks_vtx"] = rk.get_tracks(n)
+    rk.put_tracks(snap.tracks_vtx)
+    rk.put_dimuons(L.HostDimuons(n))
+    rk.dimuons(n)
+    out["dims"] = rk.get_dimuons(n)
+    # histograms (M:983) on the oracle's tracks and dimuons
+    rk.put_dimuons(snap.dims)
+    out["hists"] = rk.histograms(np.nonzero(snap.toomany_xz == 0)[0], O.hist_table(), snap.trig)
     return out
 
 
@@ -159,6 +187,20 @@ def compare(snap, ref, rtol):
             r["n_" + k] = len(r[k])
             r[k] = r[k][:20]
         rep[stage] = r
+    r = G.compare_tracks(G.compact_tracks(ref["tracks_vtx"], snap.toomany_xz),
+                         G.compact_tracks(snap.tracks_vtx, snap.toomany_xz), rtol)
+    for k in ("count_mismatch", "discrete_mismatch", "value_mismatch"):
+        r["n_" + k] = len(r[k])
+        r[k] = r[k][:20]
+    rep["vtx"] = r
+    r = G.compare_dimuons(G.compact_dimuons(ref["dims"], snap.toomany_xz),
+                          G.compact_dimuons(snap.dims, snap.toomany_xz), rtol, phi_ulps=4)
+    for k in ("count_mismatch", "value_mismatch"):
+        r["n_" + k] = len(r[k])
+        r[k] = r[k][:20]
+    rep["dim"] = r
+    rep["hist"] = {"differing_tables": G.compare_hists(ref["hists"], snap.hists, phi_slack=2),
+                   "counts": float(snap.hists.values_array().sum())}
     rep["seconds"] = {k: ref[k] for k in ("t_er", "t_yz", "t_global")}
     return rep
 
@@ -200,12 +242,19 @@ def main():
         rec_f, off_f = G.select_events(rec_k, off_k, fix)
         fixture[f"{name}/records"] = rec_f.view(np.uint8).reshape(-1, L.HIT_RECORD_DTYPE.itemsize)
         fixture[f"{name}/offsets"] = off_f
+        fixture[f"{name}/trigger_bits"] = snap.trig[fix]
         for v, rk in images.items():
             ref = run_reference(rk, plane, snap, n)
             crep[v] = compare(snap, ref, 0.0 if v == "fmad0" else 1e-5)
             sub = _subset(ref, fix)
             for key, arr in sub.items():
                 fixture[f"{name}/{v}/{key}"] = arr
+            # histograms of the fixture events alone, the way the CPU test refills them
+            rk.put_tracks(snap.tracks_vtx)
+            rk.put_dimuons(snap.dims)
+            rk.put_flags(snap.toomany_xz)
+            hf = rk.histograms([e for e in fix if not snap.toomany_xz[e]], O.hist_table(), snap.trig)
+            fixture[f"{name}/{v}/hist_values"] = hf.values_array()
         report["configs"][name] = crep
         print(name, json.dumps({k: crep[k] for k in ("generated", "in_domain")}), flush=True)
     for rk in images.values():
@@ -222,10 +271,14 @@ def _subset(ref, idx):
     h = _take_hits(ref["hits_er"], idx)
     out["er_counts"], out["er_hits"] = G.compact_hits(h)
     out["er_flags"] = ref["flags_er"][idx]
-    for stage in ("yz", "clean", "global", "sel"):
+    for stage in ("yz", "clean", "global", "sel", "vtx"):
         t = _take_tracks(ref["tracks_" + stage], idx)
         nt, w, r = G.compact_tracks(t)
         out[f"{stage}_ntracks"], out[f"{stage}_where"], out[f"{stage}_records"] = nt, w, r
+    d = L.HostDimuons(len(idx))
+    d.ndimuons[:] = ref["dims"].ndimuons[idx]
+    d.dimuons[:] = ref["dims"].dimuons.reshape(ref["dims"].n, L.EVT_DIM_FLOATS)[idx].reshape(-1)
+    out["dim_n"], out["dim_records"] = G.compact_dimuons(d)
     return out
 
 
@@ -253,7 +306,9 @@ def _summary(report):
                                 "flags_recomputed": r["er_flags"]["recomputed_vs_oracle_mismatch"],
                                 **{st: [r[st]["n_count_mismatch"], r[st]["n_discrete_mismatch"],
                                         r[st]["n_value_mismatch"], r[st]["max_rel_fit"]]
-                                   for st in ("yz", "clean", "global", "sel")}}
+                                   for st in ("yz", "clean", "global", "sel", "vtx")},
+                                "dim": [r["dim"]["n_count_mismatch"], r["dim"]["n_value_mismatch"]],
+                                "hist": r["hist"]["differing_tables"]}
     return s
 
 

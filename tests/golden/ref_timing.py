@@ -107,10 +107,10 @@ def tracks_mismatch(torch, rk, b, n, toomany):
     a, c = rt[..., fit].double(), ot[..., fit].double()
     rel = ((a - c).abs() / c.abs().clamp_min(1e-30))
     rel = torch.where(valid[..., None] & (a != c), rel, torch.zeros_like(rel))
-    return int(disc_bad.sum()), int(any_bad.sum()), float(rel.max()) if rel.numel() else 0.0
+    return int(disc_bad.sum()), int(any_bad.sum()), float(rel.max()) if rel.numel() else 0.0, any_bad
 
 
-def run_config(torch, plane, geo, rc, images, name, cfg):
+def run_config(torch, plane, geo, rc, images, name, cfg, dump=None, dump_image="fmad0", dump_max=0):
     from orgpu import pipeline
     t0 = time.time()
     rec, off, _ = S.generate(geo, cfg)
@@ -184,7 +184,14 @@ def run_config(torch, plane, geo, rc, images, name, cfg):
                 rk.view("flags", m).copy_(src["toomany"])
                 fns[s](m)
                 want = b_tracks(b, snaps[s])
-                d, a, r = tracks_mismatch(torch, rk, want, m, snaps["xz"]["toomany"])
+                d, a, r, bad = tracks_mismatch(torch, rk, want, m, snaps["xz"]["toomany"])
+                if dump is not None and v == dump_image and a:
+                    for ie in torch.nonzero(bad).flatten().tolist()[:max(0, dump_max - len(dump[s]))]:
+                        dump[s].append({"event": c0 + ie, "records": r_c[o_c[ie]:o_c[ie + 1]].copy(),
+                                        "ours_ntracks": want.ntracks.view(m, L.NSLOTS)[ie].cpu().numpy(),
+                                        "ours_tracks": want.tracks.view(m, -1)[ie].cpu().numpy(),
+                                        "ref_ntracks": rk.view("ntracks", m).view(m, L.NSLOTS)[ie].cpu().numpy(),
+                                        "ref_tracks": rk.view("tracks", m).view(m, -1)[ie].cpu().numpy()})
                 par[v][s][0] += d
                 par[v][s][1] += a
                 par[v][s][2] = max(par[v][s][2], r)
@@ -237,6 +244,8 @@ def main():
     ap.add_argument("--out", default=os.path.join(REPO, "gpurun_out", "ref_timing"))
     ap.add_argument("--uneven-events", type=int, default=100000)
     ap.add_argument("--images", default="fmad1,fmad0")
+    ap.add_argument("--configs", default="small,uneven,high_occupancy")
+    ap.add_argument("--dump", type=int, default=0, help="save up to this many differing events per stage (fmad0)")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     import torch
@@ -248,7 +257,17 @@ def main():
     images = {v: refrun.RefKernels(v) for v in args.images.split(",")}
     report = {"device": torch.cuda.get_device_name(0), "chunk_events": CHUNK, "configs": {}}
     for name, cfg in configs(args.uneven_events):
-        report["configs"][name] = run_config(torch, plane, geo, rc, images, name, cfg)
+        if name not in args.configs.split(","):
+            continue
+        dump = {s: [] for s in ("yz", "back_clean", "global", "select")} if args.dump else None
+        report["configs"][name] = run_config(torch, plane, geo, rc, images, name, cfg, dump, "fmad0", args.dump)
+        if dump is not None and any(dump.values()):
+            flat = {}
+            for s, lst in dump.items():
+                for i, d in enumerate(lst):
+                    for k, x in d.items():
+                        flat[f"{s}/{i}/{k}"] = np.asarray(x)
+            np.savez_compressed(os.path.join(args.out, f"mismatch_{name}.npz"), **flat)
         print(name, json.dumps(report["configs"][name]), flush=True)
     for rk in images.values():
         rk.close()

@@ -50,7 +50,8 @@ def golden(geometry):
         rec = z[f"{name}/records"].reshape(-1).view(L.HIT_RECORD_DTYPE)
         off = z[f"{name}/offsets"]
         hits = S.pack(rec, off, geo.wire_pos_f32())
-        out[name] = (z, M.Snap(plane, hits))
+        trig = z[f"{name}/trigger_bits"] if f"{name}/trigger_bits" in z else None
+        out[name] = (z, M.Snap(plane, hits, trig))
     return G, M, out
 
 
@@ -119,3 +120,53 @@ def test_tracking_stages_fmad1_band(golden, name):
         else:
             assert len(r["discrete_mismatch"]) <= max(2, r["tracks"] // 10), (stage, r)
             assert len(r["value_mismatch"]) <= max(2, r["tracks"] // 10), (stage, r)
+
+
+@pytest.mark.parametrize("name", CONFIGS)
+def test_vertexing_bit_exact_fmad0(golden, name):
+    """gKernel_Vertexing: the double-precision FMag swim and the closest
+    approach to the beam line, bit for bit."""
+    G, M, data = golden
+    z, snap = data[name]
+    ref = tuple(z[f"{name}/fmad0/vtx_{k}"] for k in ("ntracks", "where", "records"))
+    r = G.compare_tracks(_masked(ref, snap.toomany_xz), G.compact_tracks(snap.tracks_vtx, snap.toomany_xz), 0.0)
+    assert r["count_mismatch"] == [] and r["value_mismatch"] == [], r
+
+
+@pytest.mark.parametrize("name", CONFIGS)
+def test_dimuons_fmad0(golden, name):
+    """gKernel_DimuonBuilding: counts and every field bit for bit; phi (from
+    atan2f, whose C-library and CUDA versions may differ) within 4 ulps."""
+    G, M, data = golden
+    z, snap = data[name]
+    ref = (z[f"{name}/fmad0/dim_n"], z[f"{name}/fmad0/dim_records"])
+    r = G.compare_dimuons(ref, G.compact_dimuons(snap.dims), 0.0, phi_ulps=4)
+    assert r["count_mismatch"] == [] and r["value_mismatch"] == [], r
+
+
+@pytest.mark.parametrize("variant", ["fmad0", "fmad1"])
+@pytest.mark.parametrize("name", CONFIGS)
+def test_histograms(golden, name, variant):
+    """gKernel_fill_display_histograms run one event at a time: the same
+    counts in every (trigger, variable) table."""
+    G, M, data = golden
+    from orgpu import layout as L
+    z, snap = data[name]
+    ref = L.OrHists.from_bytes(snap.hists.to_bytes())
+    vals = np.ctypeslib.as_array(ref.values)
+    vals[:] = z[f"{name}/{variant}/hist_values"].reshape(-1)
+    assert G.compare_hists(ref, snap.hists, phi_slack=2) == []
+
+
+@pytest.mark.parametrize("name", CONFIGS)
+def test_vertexing_dimuons_fmad1_band(golden, name):
+    """Against the default (contracting) build: the same vertexed tracks and
+    dimuons, values within 1e-5 relative."""
+    G, M, data = golden
+    z, snap = data[name]
+    ref = tuple(z[f"{name}/fmad1/vtx_{k}"] for k in ("ntracks", "where", "records"))
+    r = G.compare_tracks(_masked(ref, snap.toomany_xz), G.compact_tracks(snap.tracks_vtx, snap.toomany_xz), 1e-5)
+    assert r["count_mismatch"] == [] and r["discrete_mismatch"] == [], r
+    ref = (z[f"{name}/fmad1/dim_n"], z[f"{name}/fmad1/dim_records"])
+    r = G.compare_dimuons(ref, G.compact_dimuons(snap.dims), 1e-5, phi_ulps=64)
+    assert r["count_mismatch"] == [], r
