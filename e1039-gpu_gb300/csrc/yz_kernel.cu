@@ -307,6 +307,14 @@ __device__ __forceinline__ void walk_newhits(int n, UvHit *h, const Stale &st, f
         if (!h[k].sign) h[k].sign = single_sign_newhits(x0, tx, y0, ty, h[k].det, h[k].pos, P);
 }
 
+// The per-survivor work below runs once per 32 queued survivors, between long
+// stretches of the first-cut loop; it is kept out of line (one copy each) so
+// that the loop's instructions stay resident in the instruction cache.
+__device__ __noinline__ void walk_uv(int n, UvHit *h, const Stale &st, float x0, float tx, float y0, float ty,
+                                     float ex0, float etx, float ey0, float ety, const or_plane_t &P) {
+    walk_newhits(n, h, st, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
+}
+
 // Index of the last station-3 hit when the walk pairs it with the first
 // station-2 hit, else -1.  The walk's pairs depend only on plane ids.
 __device__ __forceinline__ int cross_pair_index(int n3, const UvHit *h, int nuv) {
@@ -476,6 +484,45 @@ __device__ __forceinline__ int yz_gather(const YzWarp &S, const YzHit *base, int
     return nuv;
 }
 
+// gates of a candidate after the refit: the hard cut (K:1638), the prop-tube
+// y segments (K:1640-1702) and the hodoscopes with y (H:1002-1087)
+__device__ __noinline__ bool yz_gates(const YzEvent &E, const or_plane_t &P, float x0, float y0, float tx, float ty,
+                                      float ex0, float ey0, float etx, float ety) {
+    if (fabsf(y0) > Y0_MAX || fabsf(ty) > TY_MAX) return false;
+    const int nprop = prop_hits(E.p1y1, P.z[DET_P1Y1], E.p1y2, P.z[DET_P1Y2], 5.08f, y0, ty) +
+                      prop_hits(E.p2y1, P.z[DET_P2Y1], E.p2y2, P.z[DET_P2Y2], 10.16f, y0, ty);
+    if (nprop < NPROP_MIN) return false;
+#pragma unroll 1
+    for (int qq = 0; qq < 3; ++qq) {
+        bool ok = false;
+#pragma unroll 1
+        for (int c = 0; c < 2 && !ok; ++c)
+            ok = match_tracklet_to_hodo(qq + 1, c_hodoplanesx[qq + 1][c], E.hod[qq][c], x0, y0, tx, ty, ex0, ey0, etx,
+                                        ety, P);
+        if (!ok) return false;
+    }
+    return true;
+}
+
+// chi2_track over the x hits and the uv hits (H:1182-1204), residuals into resid
+__device__ __noinline__ float yz_chi2(const YzWarp &S, const UvHit *h, int nuv, int nhx, const or_plane_t &P, float x0,
+                                      float y0, float tx, float ty, float *resid) {
+    float chi2 = 0.f;
+    for (int m = 0; m < nhx; ++m) {
+        resid[m] = residual_line(S.xp1x[m], S.xp1y[m], S.xp1z[m], S.xdpx[m], S.xdpy[m], S.xdpz[m], S.xdd[m], S.xhs[m],
+                                 x0, y0, tx, ty);
+        chi2 += resid[m] * resid[m] / S.xres[m] / S.xres[m];
+    }
+    for (int k = 0; k < nuv; ++k) {
+        const short d = h[k].det;
+        const float r = residual_line(x_bep(d, h[k].el, P), y_bep(d, h[k].el, P), z_bep(d, h[k].el, P), P.deltapx[d],
+                                      P.deltapy[d], P.deltapz[d], h[k].drift, h[k].sign, x0, y0, tx, ty);
+        resid[nhx + k] = r;
+        chi2 += r * r / P.resolution[d] / P.resolution[d];
+    }
+    return chi2;
+}
+
 // Evaluate combinations [c0, c1) (whole outer iterations) of the current
 // tracklet.  `st` is advanced to the scratch state after the range.  Returns
 // the best key (chi2 bits << 32 | combination index) or ~0, with that
@@ -586,7 +633,7 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
         const bool carried_f = (g == cg) && cg_hasf;
         const int fl = __ffs(vm & seg) - 1;
         const bool is_first = valid && !carried_f && fl == lane;
-        if (is_first) walk_newhits(nuv, h, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
+        if (is_first) walk_uv(nuv, h, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
         short sig[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -619,37 +666,11 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
                 if (xs >= 0) h[n3 - 1].sign = xprev;
                 else if (g == cg && cg_hascross) h[n3 - 1].sign = cg_cross;
             }
-            walk_newhits(nuv, h, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
+            walk_uv(nuv, h, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
         }
         if (valid) {
-            // the refit repeats the first fit exactly (same inputs); hard cut K:1638
-            pass = !(fabsf(y0) > Y0_MAX || fabsf(ty) > TY_MAX);
-            if (pass) {
-                const int nprop = prop_hits(E.p1y1, P.z[DET_P1Y1], E.p1y2, P.z[DET_P1Y2], 5.08f, y0, ty) +
-                                  prop_hits(E.p2y1, P.z[DET_P2Y1], E.p2y2, P.z[DET_P2Y2], 10.16f, y0, ty);
-                pass = nprop >= NPROP_MIN;
-            }
-            for (int qq = 0; qq < 3 && pass; ++qq) {
-                pass = match_tracklet_to_hodo(qq + 1, c_hodoplanesx[qq + 1][0], E.hod[qq][0], x0, y0, tx, ty, ex0, ey0,
-                                              etx, ety, P) ||
-                       match_tracklet_to_hodo(qq + 1, c_hodoplanesx[qq + 1][1], E.hod[qq][1], x0, y0, tx, ty, ex0, ey0,
-                                              etx, ety, P);
-            }
-            if (pass) {  // chi2_track, H:1182-1204
-                for (int m = 0; m < nhx; ++m) {
-                    resid[m] = residual_line(S.xp1x[m], S.xp1y[m], S.xp1z[m], S.xdpx[m], S.xdpy[m], S.xdpz[m],
-                                             S.xdd[m], S.xhs[m], x0, y0, tx, ty);
-                    chi2 += resid[m] * resid[m] / S.xres[m] / S.xres[m];
-                }
-                for (int k = 0; k < nuv; ++k) {
-                    const short d = h[k].det;
-                    const float r = residual_line(x_bep(d, h[k].el, P), y_bep(d, h[k].el, P), z_bep(d, h[k].el, P),
-                                                  P.deltapx[d], P.deltapy[d], P.deltapz[d], h[k].drift, h[k].sign, x0,
-                                                  y0, tx, ty);
-                    resid[nhx + k] = r;
-                    chi2 += r * r / P.resolution[d] / P.resolution[d];
-                }
-            }
+            pass = yz_gates(E, P, x0, y0, tx, ty, ex0, ey0, etx, ety);
+            if (pass) chi2 = yz_chi2(S, h, nuv, nhx, P, x0, y0, tx, ty, resid);
         }
         // carry of the sign state to the next survivor chunk
         {
@@ -1028,7 +1049,7 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
 
 // persistent warps drain the unit queue
 template <int W>
-__global__ void __launch_bounds__(W * 32)
+__global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
     yz_work_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv, YzScratch sc) {
     extern __shared__ __align__(16) unsigned char yz_smem[];
     or_plane_t &P = *reinterpret_cast<or_plane_t *>(yz_smem);

@@ -192,6 +192,19 @@ def run_config(torch, plane, geo, rc, images, name, cfg, dump=None, dump_image="
                                         "ours_tracks": want.tracks.view(m, -1)[ie].cpu().numpy(),
                                         "ref_ntracks": rk.view("ntracks", m).view(m, L.NSLOTS)[ie].cpu().numpy(),
                                         "ref_tracks": rk.view("tracks", m).view(m, -1)[ie].cpu().numpy()})
+                if s in ("yz", "global"):
+                    # the reference again on the same inputs: events where its
+                    # two runs disagree (its uninitialised per-thread scratch)
+                    first = _View()
+                    first.ntracks = rk.view("ntracks", m).clone()
+                    first.tracks = rk.view("tracks", m).clone()
+                    saved, rk.timing = rk.timing, None
+                    rk.view("ntracks", m).copy_(src["ntracks"])
+                    rk.view("tracks", m).copy_(src["tracks"])
+                    fns[s](m)
+                    rk.timing = saved
+                    self_bad = tracks_mismatch(torch, rk, first, m, snaps["xz"]["toomany"])[1]
+                    par[v]["self_" + s] = par[v].get("self_" + s, 0) + self_bad
                 par[v][s][0] += d
                 par[v][s][1] += a
                 par[v][s][2] = max(par[v][s][2], r)
@@ -214,6 +227,7 @@ def run_config(torch, plane, geo, rc, images, name, cfg, dump=None, dump_image="
                   "library_events_per_s": n / (sum(ours.values()) / 1000.0),
                   "speedup_per_stage": {s: (r[s] / ours[s] if ours[s] else None) for s in REF_KEYS},
                   "speedup_chain_without_xz": chain / lib_no_xz if lib_no_xz else None,
+                  "reference_run_twice_differing_events": {st: par[v].get("self_" + st, 0) for st in ("yz", "global")},
                   "parity": {"er_hit_mismatch_events": par[v]["er_events"],
                              "er_flag_mismatch_events_raw": par[v]["er_flag_events"],
                              **{s: {"discrete_mismatch_events": par[v][s][0], "any_bit_mismatch_events": par[v][s][1],
