@@ -81,6 +81,63 @@ static __device__ void sagitta_st1(float x0, float tx, float y0, float ty, int d
 // finish early keep taking units instead of idling behind a heavy event.
 constexpr int GL_CHUNK = 8;
 
+// The survivor work of the (u1,v1) loop -- left/right walk and chi2 --
+// kept out of line (one copy each) so that the loop's instructions stay
+// resident in the instruction cache.
+
+// resolve_leftright_newhits over the x + uv hits (H:714-780), with the
+// scratch entry past the end, then the singles (H:785-804)
+__device__ __noinline__ void gl_walk(GHit *h, int nall, const Stale &st, float xs0, float xst, float yc, float tyc,
+                                     float ex0s, float etxs, float eyc, float etyc, const or_plane_t &P) {
+    for (int i = 0; i < nall;) {
+        const int j = i + 1;
+        const short di = h[i].det;
+        const short dj = j < nall ? h[j].det : st.det;
+        if (abs(di - dj) != 1) {
+            i += 1;
+            continue;
+        }
+        const short sj = j < nall ? h[j].sign : (short)0;
+        if (h[i].sign * sj == 0) {
+            const float pj = j < nall ? h[j].pos : st.pos;
+            const float drj = j < nall ? h[j].drift : st.drift;
+            const int k = lr_pair_newhits(xs0, xst, yc, tyc, ex0s, etxs, eyc, etyc, di, dj, h[i].pos, h[i].drift, pj,
+                                          drj, P, 150.f);
+            if (k >= 0) {
+                h[i].sign = c_lrpossibility[k][0];
+                if (j < nall) h[j].sign = c_lrpossibility[k][1];
+            }
+        }
+        i += 2;
+    }
+    for (int k = 0; k < nall; ++k)
+        if (!h[k].sign) h[k].sign = single_sign_newhits(xs0, xst, yc, tyc, h[k].det, h[k].pos, P);
+}
+
+// chi2 over the station-2/3 hits (H:1149-1180) plus chi2_track over the
+// station-1 hits (K:2449-2461); residuals into rst / rs1
+__device__ __noinline__ float gl_chi2(const GlWarp &S, int nst, const GHit *h, int nall, const or_plane_t &P, float x0,
+                                      float tx, float xs0, float xst, float yc, float tyc, float *rst, float *rs1) {
+    float chi2 = 0.f;
+    for (int m = 0; m < nst && m < 12; ++m) {
+        const short d = S.s_det[m];
+        const float r = residual_line(x_bep(d, S.s_chan[m], P), y_bep(d, S.s_chan[m], P), z_bep(d, S.s_chan[m], P),
+                                      P.deltapx[d], P.deltapy[d], P.deltapz[d], S.s_drift[m], S.s_sign[m], x0, yc, tx,
+                                      tyc);
+        rst[m] = r;
+        chi2 += r * r / (S.s_res[m] * S.s_res[m]);
+    }
+    float c1 = 0.f;
+    for (int k = 0; k < nall; ++k) {
+        const short d = h[k].det;
+        const float r = residual_line(x_bep(d, h[k].el, P), y_bep(d, h[k].el, P), z_bep(d, h[k].el, P), P.deltapx[d],
+                                      P.deltapy[d], P.deltapz[d], h[k].drift, h[k].sign, xs0, yc, xst, tyc);
+        rs1[k] = r;
+        c1 += r * r / P.resolution[d] / P.resolution[d];
+    }
+    return chi2 + c1;
+}
+
 template <int W>
 __global__ void __launch_bounds__(W * 32)
     global_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
@@ -337,8 +394,9 @@ __global__ void __launch_bounds__(W * 32)
                         short xval = 0;
                         const bool cross = pass1 && nhx == 1 && h[0].det == 3 && h[1].det == 2;
                         if (cross) {
-                            const int k = lr_pair_newhits(xs0, xst, yc, tyc, ex0s, etxs, eyc, etyc, h[0].det, h[1].det,
-                                                          h[0].pos, h[0].drift, h[1].pos, h[1].drift, P, 150.f);
+                            const int k = lr_pair_newhits_ool(xs0, xst, yc, tyc, ex0s, etxs, eyc, etyc, h[0].det,
+                                                              h[1].det, h[0].pos, h[0].drift, h[1].pos, h[1].drift, P,
+                                                              150.f);
                             if (k >= 0) {
                                 xok = true;
                                 xval = c_lrpossibility[k][0];
@@ -355,51 +413,10 @@ __global__ void __launch_bounds__(W * 32)
                                 if (xs >= 0) h[0].sign = xprev;
                                 else if (xcarry) h[0].sign = xcarry_v;
                             }
-                            // walk over x + uv hits (H:714-780) and singles
-                            for (int i = 0; i < nall;) {
-                                const int j = i + 1;
-                                const short di = h[i].det;
-                                const short dj = j < nall ? h[j].det : st.det;
-                                if (abs(di - dj) != 1) {
-                                    i += 1;
-                                    continue;
-                                }
-                                const short sj = j < nall ? h[j].sign : (short)0;
-                                if (h[i].sign * sj == 0) {
-                                    const float pj = j < nall ? h[j].pos : st.pos;
-                                    const float drj = j < nall ? h[j].drift : st.drift;
-                                    const int k = lr_pair_newhits(xs0, xst, yc, tyc, ex0s, etxs, eyc, etyc, di, dj,
-                                                                  h[i].pos, h[i].drift, pj, drj, P, 150.f);
-                                    if (k >= 0) {
-                                        h[i].sign = c_lrpossibility[k][0];
-                                        if (j < nall) h[j].sign = c_lrpossibility[k][1];
-                                    }
-                                }
-                                i += 2;
-                            }
-                            for (int k = 0; k < nall; ++k)
-                                if (!h[k].sign) h[k].sign = single_sign_newhits(xs0, xst, yc, tyc, h[k].det, h[k].pos, P);
+                            gl_walk(h, nall, st, xs0, xst, yc, tyc, ex0s, etxs, eyc, etyc, P);
                             pass = !(fabsf(yc) > Y0_MAX || fabsf(tyc) > TY_MAX);  // K:2410
                             if (pass) {  // K:2449-2461
-                                for (int m = 0; m < nst && m < 12; ++m) {
-                                    const short d = S.s_det[m];
-                                    const float r = residual_line(x_bep(d, S.s_chan[m], P), y_bep(d, S.s_chan[m], P),
-                                                                  z_bep(d, S.s_chan[m], P), P.deltapx[d], P.deltapy[d],
-                                                                  P.deltapz[d], S.s_drift[m], S.s_sign[m], x0, yc, tx,
-                                                                  tyc);
-                                    rst[m] = r;
-                                    chi2 += r * r / (S.s_res[m] * S.s_res[m]);
-                                }
-                                float c1 = 0.f;
-                                for (int k = 0; k < nall; ++k) {
-                                    const short d = h[k].det;
-                                    const float r = residual_line(x_bep(d, h[k].el, P), y_bep(d, h[k].el, P),
-                                                                  z_bep(d, h[k].el, P), P.deltapx[d], P.deltapy[d],
-                                                                  P.deltapz[d], h[k].drift, h[k].sign, xs0, yc, xst, tyc);
-                                    rs1[k] = r;
-                                    c1 += r * r / P.resolution[d] / P.resolution[d];
-                                }
-                                chi2 += c1;
+                                chi2 = gl_chi2(S, nst, h, nall, P, x0, tx, xs0, xst, yc, tyc, rst, rs1);
                                 pass = !(chi2 > 10000.f);
                             }
                         }

@@ -222,6 +222,14 @@ __device__ __forceinline__ int lr_pair_newhits(float x0, float tx, float y0, flo
     return (indexmin > 0 && pull_min < thr) ? indexmin : -1;
 }
 
+// The same, out of line: for call sites outside a kernel's hot loop, so that
+// the loop's instructions stay resident in the instruction cache.
+static __device__ __noinline__ int lr_pair_newhits_ool(float x0, float tx, float y0, float ty, float err_x0, float err_tx,
+                                                float err_y0, float err_ty, short di, short dj, float pos_i,
+                                                float dr_i, float pos_j, float dr_j, const or_plane_t &P, float thr) {
+    return lr_pair_newhits(x0, tx, y0, ty, err_x0, err_tx, err_y0, err_ty, di, dj, pos_i, dr_i, pos_j, dr_j, P, thr);
+}
+
 // Resolve one adjacent pair of resolve_leftright_xhits, H:829-868.
 __device__ __forceinline__ int lr_pair_xhits(float x0, float tx, float err_x0, float err_tx, short di, short dj,
                                              float pos_i, float dr_i, float pos_j, float dr_j, const float *zarr,

@@ -242,7 +242,7 @@ __device__ __forceinline__ SwimPt dim_start(const float *T, const float *z, floa
 }
 
 // one FMag step (H:1290-1333); d1 = the linear energy-loss coefficient of the
-// first update, DEDX_UNIT_2 for the reference's second track (H:1348)
+// first update, DEDX_UNIT_2 for the reference's second track (H:1354)
 __device__ __forceinline__ void dim_fmag_step(SwimPt &s, float charge, float ty, double d1) {
     using namespace phys;
     const float tx_i = s.mx / s.mz;
@@ -284,7 +284,7 @@ __device__ float closest_approach(float *v, float *p_pos, float *p_neg, float c1
     float dca2_min = 1.e18f;
     int best = -1;
     SwimPt b1 = s1, b2 = s2;
-    float z66_1 = 0.f, z66_2 = 0.f;  // element 200 of the reference's flat arrays (H:1451-1456)
+    float z66_1 = 0.f, z66_2 = 0.f;  // element 200 of the reference's flat arrays (H:1447-1449)
     for (int j = 0; j <= NSTEPS_FMAG + NSTEPS_TARGET; ++j) {
         if (j >= 1 && j <= NSTEPS_FMAG) {
             dim_fmag_step(s1, c1, ty1, DEDX_UNIT_1);

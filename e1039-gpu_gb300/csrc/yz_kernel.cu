@@ -646,7 +646,7 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
         if (valid && !is_first) {
             const int xi = cross_pair_index(n3, h, nuv);
             if (xi >= 0) {
-                const int k = lr_pair_newhits(x0, tx, y0, ty, ex0, etx, ey0, ety, h[xi].det, h[xi + 1].det, h[xi].pos,
+                const int k = lr_pair_newhits_ool(x0, tx, y0, ty, ex0, etx, ey0, ety, h[xi].det, h[xi + 1].det, h[xi].pos,
                                               h[xi].drift, h[xi + 1].pos, h[xi + 1].drift, P, 150.f);
                 if (k >= 0) {
                     xok = true;
