@@ -767,9 +767,9 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
     for (;;) {
         if (basec < c1) {
             // the chunk's first combination in a dead outer iteration: jump
-            // to the next live one (every combination in between is dead)
-            const int g = basec / C2;
-            const int iv = g / nu3, iu = g - iv * nu3;
+            // to the next live one (every combination in between is dead);
+            // lane 0 holds that combination's digits
+            const int iu = __shfl_sync(0xffffffffu, d2, 0), iv = __shfl_sync(0xffffffffu, d3, 0);
             if (!(bit128(alive.u, iu) && bit128(alive.v, iv))) {
                 const int gn = next_alive_outer(alive, nu3, iu, iv);
                 basec = gn < 0 ? c1 : min(gn * C2, c1);
@@ -783,7 +783,9 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
             const int c = basec + lane;
             const bool valid = c < c1;
             int nuv = 0;
-            Stale own0{DET_SENTINEL, 0.f, 0.f}, own1 = own0, own2 = own0, own3 = own0;
+            // scratch entries this combination writes (offsets 4..7 past the
+            // hit count): arena offsets of the hits, 16 bits each
+            unsigned long long own = 0ull;
             unsigned wmask = 0u;
             float y0 = 0.f, ty = 0.f, ey0 = 0.f, ety = 0.f;
             bool pass1 = false;
@@ -806,27 +808,31 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
                 if (alive3) {
                     // station-2 attempts in the reference order (K:1467-1597):
                     // every attempted hit writes the scratch entry at the
-                    // running count, accepted ones enter the fit
+                    // running count (4..7 at most: n3 <= 4, four attempts),
+                    // accepted ones enter the fit
                     Fit2 f = f3;
                     nuv = n3;
                     const short2 pu = S.pair[0][d0];
-                    auto attempt = [&](const YzHit &r) {
-                        if (nuv == 4) { own0 = Stale{r.det, r.pos, r.drift}; wmask |= 1u; }
-                        else if (nuv == 5) { own1 = Stale{r.det, r.pos, r.drift}; wmask |= 2u; }
-                        else if (nuv == 6) { own2 = Stale{r.det, r.pos, r.drift}; wmask |= 4u; }
-                        else if (nuv == 7) { own3 = Stale{r.det, r.pos, r.drift}; wmask |= 8u; }
+                    auto attempt = [&](int off) {
+                        const YzHit &r = base[off];
+                        const int k = nuv - 4;
+                        if (k >= 0) {
+                            const int sh = k << 4;
+                            own = (own & ~(0xFFFFull << sh)) | ((unsigned long long)off << sh);
+                            wmask |= 1u << k;
+                        }
                         if (r.acc) {
                             f.add(r.Y, r.z, r.eY);
                             ++nuv;
                         }
                     };
-                    if (pu.x >= 0) attempt(Lh[0][pu.x]);
-                    if (pu.y >= 0) attempt(Lh[1][pu.y]);
+                    if (pu.x >= 0) attempt(S.woff[0] + pu.x);
+                    if (pu.y >= 0) attempt(S.woff[1] + pu.y);
                     const int nu2hits = nuv;
                     if (nu2hits > n3) {
                         const short2 pv = S.pair[1][d1];
-                        if (pv.x >= 0) attempt(Lh[2][pv.x]);
-                        if (pv.y >= 0) attempt(Lh[3][pv.y]);
+                        if (pv.x >= 0) attempt(S.woff[2] + pv.x);
+                        if (pv.y >= 0) attempt(S.woff[3] + pv.y);
                         if (nuv > nu2hits) {  // the v2 group gave a hit: the fit is reached
                             f.solve(y0, ty, ey0, ety);
                             pass1 = !(fabsf(y0) > Y0_MAX + 2 * ey0 || fabsf(ty) > TY_MAX + 2 * ety);
@@ -835,29 +841,36 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
                 }
             }
             // --- scratch entry past the hit count ------------------------------
+            // entry k+4 as combination c reads it: its own write, else the
+            // last earlier lane's write in this chunk, else the state before
+            // the chunk; the chunk's last write becomes the new state
             Stale stj{DET_SENTINEL, 0.f, 0.f};
+            int stj_off = -1;
             {
                 const int j = nuv;
                 const unsigned lt = lanemask_lt();
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    const Stale own = k == 0 ? own0 : (k == 1 ? own1 : (k == 2 ? own2 : own3));
-                    const unsigned m = __ballot_sync(0xffffffffu, (wmask >> k) & 1u);
+                    const bool mine = (wmask >> k) & 1u;
+                    const int ok = (int)((own >> (16 * k)) & 0xFFFFull);
+                    const unsigned m = __ballot_sync(0xffffffffu, mine);
                     const int src = last_lane(m & lt);
-                    const short sd = (short)__shfl_sync(0xffffffffu, (int)own.det, src < 0 ? 0 : src);
-                    const float sp = __shfl_sync(0xffffffffu, own.pos, src < 0 ? 0 : src);
-                    const float sdr = __shfl_sync(0xffffffffu, own.drift, src < 0 ? 0 : src);
+                    const int so = __shfl_sync(0xffffffffu, ok, src < 0 ? 0 : src);
                     if (j == k + 4) {
-                        if ((wmask >> k) & 1u) stj = own;
-                        else if (src >= 0) stj = Stale{sd, sp, sdr};
+                        if (mine) stj_off = ok;
+                        else if (src >= 0) stj_off = so;
                         else stj = st[k];
                     }
                     const int lw = last_lane(m);
-                    const short cd = (short)__shfl_sync(0xffffffffu, (int)own.det, lw < 0 ? 0 : lw);
-                    const float cp = __shfl_sync(0xffffffffu, own.pos, lw < 0 ? 0 : lw);
-                    const float cdr = __shfl_sync(0xffffffffu, own.drift, lw < 0 ? 0 : lw);
-                    if (lw >= 0) st[k] = Stale{cd, cp, cdr};
+                    if (lw >= 0) {
+                        const YzHit &r = base[__shfl_sync(0xffffffffu, ok, lw)];
+                        st[k] = Stale{r.det, r.pos, r.drift};
+                    }
                 }
+            }
+            if (pass1 && stj_off >= 0) {
+                const YzHit &r = base[stj_off];
+                stj = Stale{r.det, r.pos, r.drift};
             }
             // --- queue the survivors in order ----------------------------------
             const unsigned pm = __ballot_sync(0xffffffffu, pass1);
