@@ -14,7 +14,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "liborgpu.so")
 BUILD = os.path.join(HERE, "_build")
 CU = ["er_kernel.cu", "xz_kernel.cu", "yz_kernel.cu", "clean_kernel.cu", "global_kernel.cu", "pack_kernel.cu",
-      "collect_kernel.cu", "learned_kernel.cu", "mlp_kernel.cu", "select_kernel.cu", "physics_kernel.cu", "yz_noalloc.cu",
+      "collect_kernel.cu", "learned_kernel.cu", "mlp_kernel.cu", "select_kernel.cu", "physics_kernel.cu", "output_kernel.cu",
+      "yz_noalloc.cu",
       "capi.cu"]
 CPP = ["geometry.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

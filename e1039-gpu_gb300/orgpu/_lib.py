@@ -22,7 +22,7 @@ EXPORTS = ("or_version", "or_last_error", "or_status_string", "or_geometry_load"
            "or_tracklet_labels", "or_track_agreement", "or_mlp_grad_blocks", "or_mlp_forward", "or_mlp_gradient",
            "or_mlp_adam", "or_prop_matching", "or_global_clean", "or_run_selection", "or_set_launch",
            "or_get_launch", "or_vertexing", "or_dimuons", "or_fill_histograms", "or_hist_table_init",
-           "or_run_physics")
+           "or_run_physics", "or_output_rows")
 
 # tunable kernels (or_kernel_id_t)
 KERNELS = {"event_reduce": 0, "xz": 1, "yz": 2, "back_clean": 3, "global": 4, "select": 5, "features": 6}
@@ -101,6 +101,8 @@ def lib():
     lb.or_hist_table_init.argtypes = [C.POINTER(L.OrHists)]
     lb.or_hist_table_init.restype = None
     lb.or_run_physics.argtypes = [vp, L.OrTracksView, L.OrDimuonsView, vp, vp, vp, i32, vp]
+    lb.or_output_rows.argtypes = [vp, L.OrHitsView, L.OrTracksView, L.OrDimuonsView, vp, vp, vp, f32, L.OrOutputView,
+                                  i32, vp]
     for name in EXPORTS:
         getattr(lb, name)
     _lib = lb

@@ -16,6 +16,7 @@ EVT_CHAM_FLOATS = NCHAM * NHITSPARAM * MAXHITS_CHAM
 EVT_HODO_FLOATS = NHODO * NHITSPARAM * MAXHITS_HODO
 EVT_PROP_FLOATS = NPROP * NHITSPARAM * MAXHITS_PROP
 NTRKPARAM, TRKMAX, NSLOTS = 148, 512, 32
+MAXHITS_PER_TRACK = 18
 SLOTCAP = TRKMAX // NSLOTS
 EVT_TRK_FLOATS = TRKMAX * NTRKPARAM
 WIREPOS_STRIDE = 400
@@ -215,6 +216,29 @@ class HostDimuons:
     def records(self, e):
         n = min(int(self.ndimuons[e]), DIMUON_MAX)
         return self.dimuons[e * EVT_DIM_FLOATS:e * EVT_DIM_FLOATS + n * NDIMUONPARAM].reshape(n, NDIMUONPARAM)
+
+
+# event output rows (include/or_layout.h, or_output_view_t; the fields of the
+# reference's ORoutput_tree, OnlineReconstruction/OROutput.h:25-102)
+OUT_EV_FIELDS, OUT_HIT_FIELDS, OUT_TRACK_FIELDS, OUT_TRACKHIT_FIELDS, OUT_DIMUON_FIELDS = 9, 5, 20, 7, 39
+OUT_TRACK_SRC = (TRK_STID, TRK_NHITS, TRK_CHI2, TRK_X0, TRK_Y0, TRK_TX, TRK_TY, TRK_INVP, TRK_ERR_X0, TRK_ERR_Y0,
+                 TRK_ERR_TX, TRK_ERR_TY, TRK_ERR_INVP, TRK_CHARGE, TRK_VX, TRK_VX + 1, TRK_VX + 2, TRK_PX,
+                 TRK_PX + 1, TRK_PX + 2)
+# dimuon row fields from the 36-float record; ("sum", k) = pos + neg momentum component k
+OUT_DIMUON_SRC = (DIM_MASS, DIM_PT, DIM_XF, DIM_X1, DIM_X2, DIM_COSTHETA, DIM_PHI, DIM_MASS_SINGLE, DIM_CHI2_SINGLE,
+                  DIM_VTX, DIM_VTX + 1, DIM_VTX + 2, ("sum", 0), ("sum", 1), ("sum", 2), DIM_POS_VTX, DIM_POS_VTX + 1,
+                  DIM_POS_VTX + 2, DIM_NEG_VTX, DIM_NEG_VTX + 1, DIM_NEG_VTX + 2, DIM_POS_P + 3, DIM_POS_P,
+                  DIM_POS_P + 1, DIM_POS_P + 2, DIM_NEG_P + 3, DIM_NEG_P, DIM_NEG_P + 1, DIM_NEG_P + 2,
+                  DIM_POS_P_SINGLE + 3, DIM_POS_P_SINGLE, DIM_POS_P_SINGLE + 1, DIM_POS_P_SINGLE + 2,
+                  DIM_NEG_P_SINGLE + 3, DIM_NEG_P_SINGLE, DIM_NEG_P_SINGLE + 1, DIM_NEG_P_SINGLE + 2, DIM_CHI2_VTX,
+                  DIM_CHI2_KF)
+
+
+class OrOutputView(C.Structure):
+    _fields_ = [("events", C.c_void_p), ("hits", C.c_void_p), ("tracks", C.c_void_p), ("track_hits", C.c_void_p),
+                ("dimuons", C.c_void_p), ("cap_events", C.c_int64), ("cap_hits", C.c_int64),
+                ("cap_tracks", C.c_int64), ("cap_track_hits", C.c_int64), ("cap_dimuons", C.c_int64),
+                ("counts", C.c_void_p)]
 
 
 class HostTracks:

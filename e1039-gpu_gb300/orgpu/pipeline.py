@@ -230,6 +230,47 @@ class Reconstruction:
                                            None if hists is None else hists.ptr(), b.n, self._stream(stream)),
                    "or_run_physics")
 
+    def output_rows(self, b, d, raw_hits=None, event_ids=None, min_stid=7.0, caps=None, stream=None):
+        """The reference's per-event output (ORoutput_tree fields) as row
+        tables, read back to the host: a dict of numpy arrays "events" [n, 9]
+        int64, "hits" [n, 5], "tracks" [n, 20], "track_hits" [n, 7],
+        "dimuons" [n, 39] float32.  raw_hits / event_ids: device int32
+        tensors of b.n entries or None.  caps: rows per table; when given and
+        too small, OrError (capacity); when None, the tables are sized from
+        the counts of a first call if the defaults do not hold them."""
+        fixed = caps is not None
+        if caps is None:
+            caps = (b.n, b.n * 512, b.n * 8, b.n * 8 * L.MAXHITS_PER_TRACK, b.n * 4)
+        t, n = self._output_rows_once(b, d, raw_hits, event_ids, min_stid, caps, stream)
+        if any(a > c for a, c in zip(n, caps)):
+            if fixed:
+                raise _lib.OrError(_lib.OR_ERR_CAPACITY, f"output rows {n} exceed capacities {tuple(caps)}")
+            t, n = self._output_rows_once(b, d, raw_hits, event_ids, min_stid, tuple(n), stream)
+        widths = (L.OUT_EV_FIELDS, L.OUT_HIT_FIELDS, L.OUT_TRACK_FIELDS, L.OUT_TRACKHIT_FIELDS, L.OUT_DIMUON_FIELDS)
+        return {k: t[k][:m * w].view(m, w).cpu().numpy()
+                for k, m, w in zip(("events", "hits", "tracks", "track_hits", "dimuons"), n, widths)}
+
+    def _output_rows_once(self, b, d, raw_hits, event_ids, min_stid, caps, stream):
+        torch = _torch()
+        dev = b.toomany.device
+        t = {"events": torch.empty(max(1, caps[0]) * L.OUT_EV_FIELDS, dtype=torch.int64, device=dev),
+             "hits": torch.empty(max(1, caps[1]) * L.OUT_HIT_FIELDS, dtype=torch.float32, device=dev),
+             "tracks": torch.empty(max(1, caps[2]) * L.OUT_TRACK_FIELDS, dtype=torch.float32, device=dev),
+             "track_hits": torch.empty(max(1, caps[3]) * L.OUT_TRACKHIT_FIELDS, dtype=torch.float32, device=dev),
+             "dimuons": torch.empty(max(1, caps[4]) * L.OUT_DIMUON_FIELDS, dtype=torch.float32, device=dev)}
+        counts = torch.zeros(5, dtype=torch.int64, device=dev)
+        v = L.OrOutputView()
+        v.events, v.hits, v.tracks, v.track_hits, v.dimuons = (t[k].data_ptr() for k in
+                                                                ("events", "hits", "tracks", "track_hits", "dimuons"))
+        v.cap_events, v.cap_hits, v.cap_tracks, v.cap_track_hits, v.cap_dimuons = (int(c) for c in caps)
+        v.counts = counts.data_ptr()
+        _lib.check(self.lib.or_output_rows(self.ctx, b.hits_view(), b.tracks_view(), d.view(), b.toomany.data_ptr(),
+                                           None if raw_hits is None else raw_hits.data_ptr(),
+                                           None if event_ids is None else event_ids.data_ptr(), float(min_stid), v,
+                                           b.n, self._stream(stream)), "or_output_rows")
+        self.sync(stream)
+        return t, [int(x) for x in counts.cpu().tolist()]
+
     def run_batch(self, b, stream=None):
         _lib.check(self.lib.or_run_batch(self.ctx, b.hits_view(), b.tracks_view(), b.ntracklets.data_ptr(),
                                          b.toomany.data_ptr(), b.n, self._stream(stream)), "or_run_batch")

@@ -146,6 +146,19 @@ void or_hist_table_init(or_hists_t *host_table);
 int or_run_physics(or_ctx_t *ctx, or_tracks_view_t tracks, or_dimuons_view_t dimuons, const int32_t *trigger_bits,
                    const uint8_t *toomany, or_hists_t *d_hists, int n_events, void *stream);
 
+/* The reference's per-event output (the host loop online_reconstruction.cu:
+ * 1063-1222 that fills ORoutput_tree, OROutput.h:25-102) as row tables in
+ * device memory (or_output_view_t), events in batch order: events with raw
+ * hits (raw_hits[e] > 0; NULL: every event) and no reject flag; every reduced
+ * hit; the tracks with stationID >= min_stid (7 in the reference build) and
+ * their hits; the dimuons.  event_ids may be NULL (the batch index is used).
+ * out.counts[0..4] receives the rows each table needs (events, hits, tracks,
+ * track hits, dimuons); rows beyond a table's capacity are not written, so a
+ * caller compares counts with capacities after the stream completes. */
+int or_output_rows(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, or_dimuons_view_t dimuons,
+                   const uint8_t *toomany, const int32_t *raw_hits, const int32_t *event_ids, float min_stid,
+                   or_output_view_t out, int n_events, void *stream);
+
 /* Map the reference's fixed-capacity structs (EstnEvtMax = 10000 events)
  * onto views.  `coll` points at a gEventHitCollections / gEventTrackCollection
  * laid out exactly as reconstruction_classes.cuh:76-87 / :542-544. */

@@ -211,6 +211,42 @@ typedef struct or_hists {
     float values[OR_HIST_NTRIGGERS * OR_HIST_NVARS * OR_HIST_NBINS_MAX];
 } or_hists_t;
 
+/* Event output rows: the fields of the reference's output tree
+ * (ORoutput_tree, OnlineReconstruction/OROutput.h:25-102) in its order, filled
+ * as online_reconstruction.cu:1063-1222 fills it: events with raw hits and no
+ * reject flag, every reduced hit, the tracks with stationID >= a threshold (7
+ * in the reference build) with their hits, every dimuon. */
+enum { /* int64 per event */
+    OR_OUT_EV_INDEX = 0,     /* index in the batch */
+    OR_OUT_EV_ID = 1,        /* fEventID */
+    OR_OUT_EV_NHITS = 2,     /* fNHits */
+    OR_OUT_EV_NTRACKS = 3,   /* fNTracks */
+    OR_OUT_EV_NDIMUONS = 4,  /* fNDimuons */
+    OR_OUT_EV_HIT0 = 5,      /* first row of each table */
+    OR_OUT_EV_TRACK0 = 6,
+    OR_OUT_EV_TRACKHIT0 = 7,
+    OR_OUT_EV_DIMUON0 = 8,
+    OR_OUT_EV_FIELDS = 9
+};
+#define OR_OUT_HIT_FIELDS 5       /* DetID, Chan, Pos, TDC, Drift */
+#define OR_OUT_TRACK_FIELDS 20    /* StID, NHits, Chi2, X0, Y0, TX, TY, InvP, ErrX0, ErrY0, ErrTX, ErrTY,
+                                     ErrInvP, Charge, Vx, Vy, Vz, Px, Py, Pz */
+#define OR_OUT_TRACKHIT_FIELDS 7  /* DetID, Chan, Pos, Drift, Sign, TDC, Residual */
+#define OR_OUT_DIMUON_FIELDS 39   /* Mass, PT, XF, X1, X2, Costheta, Phi, MassSingle, Chi2Single, Vx, Vy,
+                                     Vz, Px, Py, Pz, PosVx, PosVy, PosVz, NegVx, NegVy, NegVz, PosE,
+                                     PosPx, PosPy, PosPz, NegE, NegPx, NegPy, NegPz, PosSingleE,
+                                     PosSinglePx, PosSinglePy, PosSinglePz, NegSingleE, NegSinglePx,
+                                     NegSinglePy, NegSinglePz, Chi2Vtx, Chi2KF */
+typedef struct or_output_view {
+    int64_t *events;     /* [cap_events * OR_OUT_EV_FIELDS] */
+    float *hits;         /* [cap_hits * 5] */
+    float *tracks;       /* [cap_tracks * 20] */
+    float *track_hits;   /* [cap_track_hits * 7] */
+    float *dimuons;      /* [cap_dimuons * 39] */
+    int64_t cap_events, cap_hits, cap_tracks, cap_track_hits, cap_dimuons;
+    int64_t *counts;     /* [5] (device): rows of each table the batch needs */
+} or_output_view_t;
+
 /* Compact hit record, the raw-event format of the reference's input
  * (OnlineReconstruction/LoadInput.h:10-20: detectorID, elementID, tdcTime,
  * driftDistance, plus the in-time flag bit the host packer turns into

@@ -1119,6 +1119,38 @@ static pair_t *alloc_pairs(void) {
     return (pair_t *)malloc(sizeof(pair_t) * (size_t)(OR_MAXHITS_CHAM * OR_MAXHITS_CHAM + 2 * OR_MAXHITS_CHAM));
 }
 
+/* Analysis hook (orc_yz_outer_dump): one record per (u3, v3) outer iteration
+ * that loads a u3 and a v3 hit, with its station-3 hits and whether it held
+ * the tracklet's best combination.  Single-threaded use only. */
+#define ORC_OUTER_FIELDS 24
+static struct {
+    float *buf;
+    int64_t cap, n;
+} g_outer;
+
+static void outer_record(long e, int slot, int i, int i_uv3, int nu3h, int nv3h, const float *Y, const float *eY,
+                         const float *Z, int ncomb_uv2, float x0, float tx, int nhits_x) {
+    if (!g_outer.buf || g_outer.n >= g_outer.cap) return;
+    float *r = g_outer.buf + g_outer.n * ORC_OUTER_FIELDS;
+    memset(r, 0, ORC_OUTER_FIELDS * sizeof(float));
+    r[0] = (float)e;
+    r[1] = (float)slot;
+    r[2] = (float)i;
+    r[3] = (float)i_uv3;
+    r[4] = (float)nu3h;
+    r[5] = (float)nv3h;
+    for (int k = 0; k < nu3h + nv3h && k < 4; k++) {
+        r[6 + k] = Y[k];
+        r[10 + k] = eY[k];
+        r[14 + k] = Z[k];
+    }
+    r[18] = (float)ncomb_uv2;
+    r[19] = x0;
+    r[20] = tx;
+    r[22] = (float)nhits_x;
+    g_outer.n++;
+}
+
 static void yz_event(const or_plane_t *P, or_hits_view_t hv, or_tracks_view_t tv, long e, const uint8_t *toomany,
                      pair_scratch_t *ps, int64_t *cnt) {
     if (toomany[e]) return; /* K:873-878 */
@@ -1207,6 +1239,8 @@ static void yz_event(const or_plane_t *P, or_hits_view_t hv, or_tracks_view_t tv
                 dpz[m] = P->deltapz[detid];
             }
             const int ncomb_uv3 = nu3 * nv3, ncomb_uv2 = nu2 * nv2;
+            int best_uv3 = -1;
+            const int64_t outer0 = g_outer.n;
             /* one uv hit load, K:1326-1355 */
 #define YZ_LOAD(LISTK, HIDX)                                                                                     \
     do {                                                                                                         \
@@ -1247,6 +1281,7 @@ static void yz_event(const or_plane_t *P, or_hits_view_t hv, or_tracks_view_t tv
                 if (pv3.second >= 0) YZ_LOAD(7, pv3.second);
                 short nhits_v3 = (short)(nuv - nhits_u3);
                 if (nhits_v3 == 0) continue;
+                outer_record(e, slot, i, i_uv3, nhits_u3, nhits_v3, Y, errY, Z, ncomb_uv2, x0, tx, nhits_x);
                 for (int i_uv2 = 0; i_uv2 < ncomb_uv2; i_uv2++) {
                     short i_u2 = (short)(i_uv2 % nu2), i_v2 = (short)((i_uv2 - i_u2) / nu2);
                     if (cnt) cnt[1]++;
@@ -1332,6 +1367,7 @@ static void yz_event(const or_plane_t *P, or_hits_view_t hv, or_tracks_view_t tv
                     if (chi2 < chi2min) {              /* K:1778-1799 */
                         chi2min = chi2;
                         update_track = 1;
+                        best_uv3 = i_uv3;
                         best[2] = nuv;
                         best[3] = chi2;
                         best[6] = ty;
@@ -1352,6 +1388,9 @@ static void yz_event(const or_plane_t *P, or_hits_view_t hv, or_tracks_view_t tv
                 }
             }
 #undef YZ_LOAD
+            if (g_outer.buf && update_track)
+                for (int64_t q = outer0; q < g_outer.n; q++)
+                    if ((int)g_outer.buf[q * ORC_OUTER_FIELDS + 3] == best_uv3) g_outer.buf[q * ORC_OUTER_FIELDS + 21] = 1.f;
             if (update_track) { /* K:1804-1825 */
                 T[OR_TRK_STID] = 5.f;
                 nhits_x = (int)T[OR_TRK_NHITS];
@@ -2081,4 +2120,15 @@ void orc_run_all_counted(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t
                          uint8_t *toomany, uint32_t *status, int64_t *counts, int n_events, int n_threads) {
     for (long e = 0; e < (long)ORC_NCOUNTS * n_events; e++) counts[e] = 0;
     run_stage(ST_ALL, p, h, t, ntracklets, toomany, status, counts, n_events, n_threads);
+}
+
+int64_t orc_yz_outer_dump(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, const uint8_t *toomany,
+                          int n_events, float *buf, int64_t cap) {
+    g_outer.buf = buf;
+    g_outer.cap = cap;
+    g_outer.n = 0;
+    run_stage(ST_YZ, p, h, t, NULL, (uint8_t *)toomany, NULL, NULL, n_events, 1);
+    const int64_t n = g_outer.n;
+    g_outer.buf = NULL;
+    return n;
 }

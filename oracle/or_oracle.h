@@ -93,6 +93,14 @@ void orc_hist_table(or_hists_t *h);
 void orc_fill_histograms(or_tracks_view_t t, or_dimuons_view_t d, or_hists_t *h, const int32_t *trigger_bits,
                          const uint8_t *toomany, int n_events);
 
+/* analysis hook: the YZ stage run single-threaded, recording every (u3, v3)
+ * outer iteration that loads a u3 and a v3 hit (24 floats: event, slot,
+ * tracklet, outer index, u3/v3 hit counts, their y, y errors and z, u2 x v2
+ * combinations, x0, tx, 1 if it held the tracklet's best combination, x-hit
+ * count); returns the records written (at most cap) */
+int64_t orc_yz_outer_dump(const or_plane_t *p, or_hits_view_t h, or_tracks_view_t t, const uint8_t *toomany,
+                          int n_events, float *buf, int64_t cap);
+
 int orc_hardware_threads(void);
 
 #ifdef __cplusplus

@@ -90,6 +90,9 @@ def _load(path):
         _lib.orc_tracklet_features.argtypes = [P(L.OrPlane), L.OrHitsView, L.OrTracksView, C.c_void_p, C.c_int,
                                                C.c_void_p, C.c_void_p, C.c_int64]
         _lib.orc_tracklet_features.restype = C.c_int64
+        _lib.orc_yz_outer_dump.argtypes = [P(L.OrPlane), L.OrHitsView, L.OrTracksView, C.c_void_p, C.c_int,
+                                            C.c_void_p, C.c_int64]
+        _lib.orc_yz_outer_dump.restype = C.c_int64
         _lib.orc_vertexing.argtypes = [P(L.OrPlane), L.OrTracksView, C.c_void_p, C.c_int, C.c_int]
         _lib.orc_dimuons.argtypes = [P(L.OrPlane), L.OrTracksView, L.OrDimuonsView, C.c_void_p, C.c_int, C.c_int]
         _lib.orc_hist_table.argtypes = [P(L.OrHists)]
@@ -188,6 +191,15 @@ def fill_histograms(tracks, dims, hists, trigger_bits, state):
     tb = None if trigger_bits is None else np.ascontiguousarray(trigger_bits, np.int32)
     lib().orc_fill_histograms(tracks.view(), dims.view(), C.byref(hists), None if tb is None else tb.ctypes.data,
                               state.toomany.ctypes.data, tracks.n)
+
+
+def yz_outer_dump(plane, hits, tracks, state, cap=20_000_000):
+    """YZ on `tracks` (single thread) with one record per live (u3, v3) outer
+    iteration: float32 [n, 24] (see orc_yz_outer_dump)."""
+    buf = np.zeros(cap * 24, np.float32)
+    n = lib().orc_yz_outer_dump(C.byref(plane), hits.view(), tracks.view(), state.toomany.ctypes.data, hits.n,
+                                buf.ctypes.data, cap)
+    return buf[:n * 24].reshape(n, 24)
 
 
 def hardware_threads():

@@ -110,3 +110,39 @@ def count_tracks(t, stid):
         for s, k, r in t.records(e):
             n += int(r[L.TRK_STID] == stid)
     return n
+
+
+def output_rows_oracle(hits, tracks, dims, toomany, raw_hits=None, event_ids=None, min_stid=7.0):
+    """The reference host's output loop (online_reconstruction.cu:1063-1222)
+    restated on host buffers: the row tables or_output_rows writes."""
+    ev, hr, tr, th, dr = [], [], [], [], []
+    for e in range(hits.n):
+        if toomany[e] or (raw_hits is not None and raw_hits[e] == 0):
+            continue
+        h0, t0, th0, d0 = len(hr), len(tr), len(th), len(dr)
+        for det in range(1, L.NDET):
+            n, data = hits.plane(e, det)
+            for l in range(n):
+                hr.append((det, data[0, l], data[1, l], data[2, l], data[4, l]))
+        for s in range(L.NSLOTS):
+            for k in range(min(int(tracks.ntracks[e * L.NSLOTS + s]), L.SLOTCAP)):
+                base = e * L.EVT_TRK_FLOATS + (s * L.SLOTCAP + k) * L.NTRKPARAM
+                T = tracks.tracks[base:base + L.NTRKPARAM]
+                if T[L.TRK_STID] < min_stid:
+                    continue
+                tr.append([T[i] for i in L.OUT_TRACK_SRC])
+                for l in range(max(0, min(int(T[L.TRK_NHITS]), 18))):
+                    th.append([T[L.TRK_HIT_DETID + l], T[L.TRK_HIT_CHAN + l], T[L.TRK_HIT_POS + l],
+                               T[L.TRK_HIT_DRIFT + l], T[L.TRK_HIT_SIGN + l], T[L.TRK_HIT_TDC + l],
+                               T[L.TRK_HIT_RESID + l]])
+        for D in dims.records(e):
+            dr.append([np.float32(D[L.DIM_POS_P + f[1]] + D[L.DIM_NEG_P + f[1]]) if isinstance(f, tuple) else D[f]
+                       for f in L.OUT_DIMUON_SRC])
+        ev.append((e, e if event_ids is None else int(event_ids[e]), len(hr) - h0, len(tr) - t0, len(dr) - d0, h0, t0,
+                   th0, d0))
+    f32 = np.float32
+    return {"events": np.array(ev, np.int64).reshape(-1, L.OUT_EV_FIELDS),
+            "hits": np.array(hr, f32).reshape(-1, L.OUT_HIT_FIELDS),
+            "tracks": np.array(tr, f32).reshape(-1, L.OUT_TRACK_FIELDS),
+            "track_hits": np.array(th, f32).reshape(-1, L.OUT_TRACKHIT_FIELDS),
+            "dimuons": np.array(dr, f32).reshape(-1, L.OUT_DIMUON_FIELDS)}

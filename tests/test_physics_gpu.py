@@ -145,3 +145,37 @@ def test_flagged_events_untouched(setup):
     s["rc"].sync()
     assert torch.equal(before, b.tracks)
     assert bool((d.ndimuons == -1).all())
+
+
+@pytest.mark.parametrize("min_stid", [7.0, 5.0])
+def test_output_rows(setup, min_stid):
+    """The reference's output tree fields as row tables, event order, bit for
+    bit against the restated host loop; events without raw hits skipped."""
+    import torch
+    from helpers import output_rows_oracle
+    s = setup
+    n = s["n"]
+    b = _batch(s, s["tv"])
+    d = _dims(s)
+    raw = np.full(n, 5, np.int32)
+    raw[::7] = 0
+    ids = np.arange(n, dtype=np.int32) * 3 + 1000
+    got = s["rc"].output_rows(b, d, torch.from_numpy(raw).cuda(), torch.from_numpy(ids).cuda(), min_stid)
+    want = output_rows_oracle(s["snap"].hits_er, s["tv"], s["dims"], s["snap"].toomany_xz, raw, ids, min_stid)
+    for k in ("events", "hits", "tracks", "track_hits", "dimuons"):
+        assert got[k].shape == want[k].shape, k
+        if k == "events":
+            np.testing.assert_array_equal(got[k], want[k])
+        else:
+            assert np.array_equal(got[k].view(np.uint32), want[k].view(np.uint32)), k
+    assert len(got["tracks"]) > 50 and len(got["dimuons"]) > 10
+
+
+def test_output_rows_capacity(setup):
+    import torch
+    from orgpu import _lib
+    s = setup
+    b = _batch(s, s["tv"])
+    d = _dims(s)
+    with pytest.raises(_lib.OrError):
+        s["rc"].output_rows(b, d, caps=(10, 10, 10, 10, 10))
