@@ -16,6 +16,9 @@ cudaError_t launch_yz_tuned(const or_plane_t *, or_hits_view_t, or_tracks_view_t
 cudaError_t launch_yz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *, void *,
                       int, int, int, cudaStream_t, int);
 size_t yz_scratch_bytes(int, int, int);
+size_t output_scratch_bytes(int);
+cudaError_t launch_output_rows(or_hits_view_t, or_tracks_view_t, or_dimuons_view_t, const uint8_t *, const int32_t *,
+                               const int32_t *, float, or_output_view_t, int, void *, cudaStream_t, int);
 cudaError_t launch_vertexing(const or_plane_t *, or_tracks_view_t, const uint8_t *, int, cudaStream_t, int);
 cudaError_t launch_dimuons(const or_plane_t *, or_tracks_view_t, or_dimuons_view_t, const uint8_t *, int,
                            cudaStream_t, int);
@@ -61,6 +64,9 @@ struct or_ctx {
     void *yz_scratch;
     int yz_cap_units, yz_cap_heavy, yz_garena_warps;
     int warps[OR_K_COUNT];  // events (work units) per CTA of each tunable kernel
+    // per-event row counts and offsets of or_output_rows, grown on demand
+    void *out_scratch = nullptr;
+    size_t out_scratch_bytes = 0;
 };
 
 namespace {
@@ -187,6 +193,7 @@ int or_destroy(or_ctx_t *ctx) {
     cudaFree(ctx->d_errw);
     cudaFree(ctx->d_sched);
     cudaFree(ctx->yz_scratch);
+    cudaFree(ctx->out_scratch);
     delete ctx;
     return OR_OK;
 }
@@ -408,6 +415,33 @@ int or_run_physics(or_ctx_t *ctx, or_tracks_view_t tracks, or_dimuons_view_t dim
     if ((rc = or_dimuons(ctx, tracks, dimuons, toomany, n_events, stream))) return rc;
     if (!d_hists) return OR_OK;
     return or_fill_histograms(ctx, tracks, dimuons, trigger_bits, toomany, d_hists, n_events, stream);
+}
+
+/* ---- event output rows (the reference's output tree) --------------------- */
+
+int or_output_rows(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, or_dimuons_view_t dimuons,
+                   const uint8_t *toomany, const int32_t *raw_hits, const int32_t *event_ids, float min_stid,
+                   or_output_view_t out, int n_events, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany) return fail(OR_ERR_ARG, "bad event count or flag array");
+    if ((rc = check_hits(hits)) || (rc = check_tracks(tracks)) || (rc = check_dimuons(dimuons))) return rc;
+    if (!out.counts || (out.cap_events > 0 && !out.events) || (out.cap_hits > 0 && !out.hits) ||
+        (out.cap_tracks > 0 && !out.tracks) || (out.cap_track_hits > 0 && !out.track_hits) ||
+        (out.cap_dimuons > 0 && !out.dimuons) || out.cap_events < 0 || out.cap_hits < 0 || out.cap_tracks < 0 ||
+        out.cap_track_hits < 0 || out.cap_dimuons < 0)
+        return fail(OR_ERR_ARG, "output view: null table with a capacity, or no counts array");
+    const size_t need = orgpu::output_scratch_bytes(n_events);
+    if (need > ctx->out_scratch_bytes) {
+        cudaFree(ctx->out_scratch);
+        ctx->out_scratch = nullptr;
+        ctx->out_scratch_bytes = 0;
+        if (cudaMalloc(&ctx->out_scratch, need) != cudaSuccess) return fail(OR_ERR_NOMEM, "output scratch");
+        ctx->out_scratch_bytes = need;
+    }
+    cudaError_t e = orgpu::launch_output_rows(hits, tracks, dimuons, toomany, raw_hits, event_ids, min_stid, out,
+                                              n_events, ctx->out_scratch, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "output rows");
 }
 
 /* ---- learned tracklet scorer ------------------------------------------- */

@@ -230,7 +230,7 @@ static void dim_start(const float *T, const float *z, float *ty_out, float *char
 
 /* one FMag step of FindDimuonClosestApproach for one track (H:1290-1333);
  * `d1` is the linear energy-loss coefficient of the first update: the
- * reference uses DEDX_UNIT_2 there for its second track (H:1348) */
+ * reference uses DEDX_UNIT_2 there for its second track (H:1354) */
 static void dim_fmag_step(swim_pt_t *s, float charge, float ty, double d1) {
     const float tx_i = s->mom[0] / s->mom[2];
     const float tx_f = (float)(tx_i + 2.f * charge * PTKICK_UNIT * STEP_FMAG /
@@ -284,7 +284,7 @@ static float closest_approach(float *v, float *p_pos, float *p_neg, float charge
     int best = -1;
     swim_pt_t b1, b2;
     /* the fallback reads element 200 of the reference's flat position arrays:
-     * the z of point 66 (H:1451-1456) */
+     * the z of point 66 (H:1447-1449) */
     float z66_1 = 0.f, z66_2 = 0.f;
     for (int j = 0; j <= NSTEPS_FMAG + NSTEPS_TARGET; j++) {
         if (j >= 1 && j <= NSTEPS_FMAG) {
