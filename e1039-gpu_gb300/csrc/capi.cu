@@ -15,7 +15,7 @@ cudaError_t launch_yz_tuned(const or_plane_t *, or_hits_view_t, or_tracks_view_t
                             void *, int, int, int, cudaStream_t, int, int);
 cudaError_t launch_yz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *, void *,
                       int, int, int, cudaStream_t, int);
-size_t yz_scratch_bytes(int, int, int);
+size_t yz_scratch_bytes_ctx(int, int, int);
 size_t output_scratch_bytes(int);
 cudaError_t launch_output_rows(or_hits_view_t, or_tracks_view_t, or_dimuons_view_t, const uint8_t *, const int32_t *,
                                const int32_t *, float, or_output_view_t, int, void *, cudaStream_t, int);
@@ -155,11 +155,15 @@ int or_create(int device, or_ctx_t **out) {
         delete c;
         return fail(OR_ERR_NOMEM, "cudaMalloc work counters");
     }
-    c->yz_cap_units = 1 << 20;
-    c->yz_cap_heavy = 1 << 18;
+    // room for every heavy tracklet of a 100,000-event batch of the uneven
+    // workload (about 1.5 M tracklets); a batch beyond it evaluates the
+    // excess in the planning pass, correct but without the queue's balance
+    c->yz_cap_units = 1 << 22;
+    c->yz_cap_heavy = 1 << 21;
     c->yz_garena_warps = c->sm_count * 16;
     if ((e = cudaMalloc(&c->yz_scratch,
-                        orgpu::yz_scratch_bytes(c->yz_cap_units, c->yz_cap_heavy, c->yz_garena_warps))) != cudaSuccess) {
+                        orgpu::yz_scratch_bytes_ctx(c->yz_cap_units, c->yz_cap_heavy, c->yz_garena_warps))) !=
+        cudaSuccess) {
         cudaFree(c->d_plane);
         cudaFree(c->d_errw);
         cudaFree(c->d_sched);

@@ -40,11 +40,20 @@ namespace orgpu {
 constexpr int YZ_MAXWIN = 100;          // windowed hits per plane (the reference's hitidx arrays)
 constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's hitpairs arrays)
 constexpr int YZ_ARENA_HITS = 192;      // windowed hits kept in shared memory per warp
-constexpr long YZ_LIGHT = 4096;         // combinations a planning warp evaluates itself per tracklet
-constexpr long YZ_CHUNK_INLINE = 4096;  // ... and per planning unit
+#ifndef OR_YZ_LIGHT
+#define OR_YZ_LIGHT 256
+#endif
+constexpr long YZ_LIGHT = OR_YZ_LIGHT;         // combinations a planning warp evaluates itself per tracklet
+constexpr long YZ_CHUNK_INLINE = OR_YZ_LIGHT;  // ... and per planning unit
 constexpr int YZ_PLAN_CHUNK = 8;        // slots per planning unit
 constexpr long YZ_UNIT = 4096;          // combinations per queued unit (whole (u3,v3) iterations)
 constexpr int YZ_GARENA_HITS = 8 * YZ_MAXWIN;  // per-warp global overflow arena
+// survivors of the first cut wait in a per-warp queue in global memory and
+// are evaluated in a batch when it fills or the range ends, so that the two
+// phases do not alternate every 32 survivors (each switch refetches the
+// other phase's instructions)
+constexpr int YZ_QCAP_MIN = 64;     // queue entries per warp: the static (no-allocation) scratch
+constexpr int YZ_QCAP_CTX = 2048;   // ... and a context's scratch
 
 struct __align__(16) YzHit {
     float Y, eY, pos, drift;
@@ -87,7 +96,8 @@ struct YzScratch {
     YzBest *best;
     unsigned int *counters;  // [0] units reserved, [1] heavy reserved, [2] queue head, [4..5] planning units
     YzHit *garena;           // per-warp overflow arenas
-    int cap_units, cap_heavy, garena_warps;
+    struct PassEntryStore *qbuf;  // per-warp survivor queues (qcap entries each)
+    int cap_units, cap_heavy, garena_warps, qcap;
 };
 
 // optional pruning: tracklet rows (row_off, as the scorer's) and keep flags
@@ -114,7 +124,6 @@ struct YzWarp {
     float xdd[4], xres[4], xp1x[4], xp1y[4], xp1z[4], xdpx[4], xdpy[4], xdpz[4];
     short xhs[4];
     YzBest b;
-    PassEntryStore q[64];  // survivors of the first cut, in order
 };
 
 struct YzEvent {
@@ -523,6 +532,141 @@ __device__ __noinline__ float yz_chi2(const YzWarp &S, const UvHit *h, int nuv, 
     return chi2;
 }
 
+// Sign state carried from one survivor chunk to the next (the first
+// combination of an outer iteration fixes the station-3 signs), and the best
+// key so far.
+struct Phase2Carry {
+    int g = -1;
+    bool hasf = false, hascross = false;
+    short sig[4] = {0, 0, 0, 0};
+    short cross = 0;
+    unsigned long long best = ~0ull;
+};
+
+// The full evaluation of n (<= 32) queued survivors Qc[0..n), in order: sign
+// state, left/right walk, prop and hodoscope gates, chi2, best key
+// (K:1613-1799).  Out of line: it runs once per 32 survivors, and inlined it
+// would sit in the middle of the first-cut loop's instructions.
+__device__ __noinline__ void yz_phase2(YzWarp &S, const YzEvent &E, const YzHit *base, int C2, const or_plane_t &P,
+                                       const PassEntryStore *Qc, int n, Phase2Carry &cs) {
+    const int lane = lane_id();
+    const float x0 = S.x0, tx = S.tx, ex0 = S.ex0, etx = S.etx;
+    const int nhx = S.nhx;
+    // --- one chunk of survivors ------------------------------------------
+    const bool valid = lane < n;
+    PassEntry q;
+    if (valid) q = Qc[lane];
+    const int c = valid ? q.c : 0;
+    const int g = valid ? c / C2 : -1 - lane;
+    UvHit h[8];
+    int n3 = 0, nuv = 0;
+    if (valid) nuv = yz_gather(S, base, c, C2, h, n3, P);
+    const Stale stj{(short)(valid ? q.stdet : DET_SENTINEL), valid ? q.stpos : 0.f, valid ? q.stdrift : 0.f};
+    const float y0 = valid ? q.y0 : 0.f, ty = valid ? q.ty : 0.f;
+    const float ey0 = valid ? q.ey0 : 0.f, ety = valid ? q.ety : 0.f;
+    const unsigned seg = __match_any_sync(0xffffffffu, g);
+    const unsigned vm = __ballot_sync(0xffffffffu, valid);
+    const bool carried_f = (g == cs.g) && cs.hasf;
+    const int fl = __ffs(vm & seg) - 1;
+    const bool is_first = valid && !carried_f && fl == lane;
+    if (is_first) walk_uv(nuv, h, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
+    short sig[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const short mine = (k < n3) ? h[k].sign : (short)0;
+        const short v = (short)__shfl_sync(0xffffffffu, (int)mine, fl < 0 ? 0 : fl);
+        sig[k] = carried_f ? cs.sig[k] : v;
+    }
+    bool xok = false;
+    short xval = 0;
+    if (valid && !is_first) {
+        const int xi = cross_pair_index(n3, h, nuv);
+        if (xi >= 0) {
+            const int k = lr_pair_newhits_ool(x0, tx, y0, ty, ex0, etx, ey0, ety, h[xi].det, h[xi + 1].det, h[xi].pos,
+                                          h[xi].drift, h[xi + 1].pos, h[xi + 1].drift, P, 150.f);
+            if (k >= 0) {
+                xok = true;
+                xval = c_lrpossibility[k][0];
+            }
+        }
+    }
+    const unsigned xm = __ballot_sync(0xffffffffu, xok);
+    const int xs = last_lane(xm & seg & lanemask_lt());
+    const short xprev = (short)__shfl_sync(0xffffffffu, (int)xval, xs < 0 ? 0 : xs);
+    bool pass = false;
+    float chi2 = 0.f;
+    float resid[12];
+    if (valid && !is_first) {
+        for (int k = 0; k < n3 && k < 4; ++k) h[k].sign = sig[k];
+        if (n3 > 0) {
+            if (xs >= 0) h[n3 - 1].sign = xprev;
+            else if (g == cs.g && cs.hascross) h[n3 - 1].sign = cs.cross;
+        }
+        walk_uv(nuv, h, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
+    }
+    if (valid) {
+        pass = yz_gates(E, P, x0, y0, tx, ty, ex0, ey0, etx, ety);
+        if (pass) chi2 = yz_chi2(S, h, nuv, nhx, P, x0, y0, tx, ty, resid);
+    }
+    // carry of the sign state to the next survivor chunk
+    {
+        const int last = last_lane(vm);
+        const int gl = __shfl_sync(0xffffffffu, g, last < 0 ? 0 : last);
+        const unsigned segl = __ballot_sync(0xffffffffu, valid && g == gl);
+        const int fnew = __ffs(__ballot_sync(0xffffffffu, is_first) & segl) - 1;
+        short ns[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) ns[k] = (short)__shfl_sync(0xffffffffu, (int)sig[k], fnew < 0 ? 0 : fnew);
+        const int xl = last_lane(xm & segl);
+        const short nx = (short)__shfl_sync(0xffffffffu, (int)xval, xl < 0 ? 0 : xl);
+        const bool cont = (gl == cs.g);
+        if (fnew >= 0) {
+            cs.hasf = true;
+            for (int k = 0; k < 4; ++k) cs.sig[k] = ns[k];
+        } else if (!cont) {
+            cs.hasf = false;
+        }
+        if (xl >= 0) {
+            cs.hascross = true;
+            cs.cross = nx;
+        } else if (!cont) {
+            cs.hascross = false;
+        }
+        cs.g = gl;
+    }
+    // best: min (chi2, index) over chi2 < 10000.1 (K:1778)
+    const bool elig = pass && chi2 < 10000.1f;
+    const unsigned key = elig ? __float_as_uint(chi2) : 0xffffffffu;
+    const unsigned kmin = __reduce_min_sync(0xffffffffu, key);
+    if (kmin != 0xffffffffu) {
+        const int win = __ffs(__ballot_sync(0xffffffffu, key == kmin)) - 1;
+        const int cw = __shfl_sync(0xffffffffu, c, win);
+        const unsigned long long full = ((unsigned long long)kmin << 32) | (unsigned long long)(unsigned)cw;
+        if (full < cs.best) {
+            cs.best = full;
+            if (lane == win) {
+                S.b.key = full;
+                S.b.nuv = nuv;
+                S.b.chi2 = chi2;
+                S.b.ty = ty;
+                S.b.y0 = y0;
+                S.b.ety = ety;
+                S.b.ey0 = ey0;
+                for (int n = 0; n < nuv; ++n) {
+                    S.b.det[n] = h[n].det;
+                    S.b.el[n] = h[n].el;
+                    S.b.pos[n] = h[n].pos;
+                    S.b.drift[n] = h[n].drift;
+                    S.b.sign[n] = h[n].sign;
+                    S.b.tdc[n] = h[n].tdc;
+                }
+                for (int n = 0; n < nhx + nuv; ++n) S.b.res[n] = resid[n];
+            }
+        }
+    }
+    __syncwarp();
+}
+
 // Evaluate combinations [c0, c1) (whole outer iterations) of the current
 // tracklet.  `st` is advanced to the scratch state after the range.  Returns
 // the best key (chi2 bits << 32 | combination index) or ~0, with that
@@ -530,9 +674,10 @@ __device__ __noinline__ float yz_chi2(const YzWarp &S, const UvHit *h, int nuv, 
 //
 // Phase 1 (every combination, registers only): station-3/2 load attempts in
 // the reference order, the first y fit, its 2-sigma cut (K:1602-1611) and the
-// scratch-entry scan.  Survivors (about 6% on the uneven batch) go to a
-// shared-memory queue in order.  Phase 2 (survivors, 32 at a time): sign
-// state, left/right walk, prop and hodoscope gates, chi2 (K:1613-1799).
+// scratch-entry scan.  Survivors (about 6% on the uneven batch) go to the
+// warp's queue in global memory, in order.  Phase 2 (yz_phase2, 32 at a time,
+// when the queue fills or the range ends): sign state, left/right walk, prop
+// and hodoscope gates, chi2 (K:1613-1799).
 //
 // Outer iterations (iu3, iv3) whose u3 pair or v3 pair gives no accepted hit
 // are skipped whole: the reference leaves such an iteration before any
@@ -601,135 +746,16 @@ __device__ __forceinline__ int next_alive_outer(const YzAlive &m, int nu3, int i
 }
 
 __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l, long c1l, Stale st[4],
-                                       const or_plane_t &P) {
+                                       const or_plane_t &P, PassEntryStore *Q, int qcap) {
     const int lane = lane_id();
     const int nu2 = S.np[0], nu3 = S.np[2];
     const int C2 = S.np[0] * S.np[1];
     const int c0 = (int)c0l, c1 = (int)c1l;  // at most 100^4 combinations
     const float x0 = S.x0, tx = S.tx, ex0 = S.ex0, etx = S.etx;
     const int nhx = S.nhx;
-    unsigned long long best = ~0ull;
-    int cg = -1;
-    bool cg_hasf = false, cg_hascross = false;
-    short cg_sig[4] = {0, 0, 0, 0};
-    short cg_cross = 0;
-    int qn = 0;  // queued survivors
+    Phase2Carry cs;
+    int qh = 0, qn = 0;  // survivors Q[qh..qn) wait for the full evaluation
 
-    auto phase2 = [&](int n) {
-        // --- one chunk of survivors ------------------------------------------
-        const bool valid = lane < n;
-        PassEntry q;
-        if (valid) q = S.q[lane];
-        const int c = valid ? q.c : 0;
-        const int g = valid ? c / C2 : -1 - lane;
-        UvHit h[8];
-        int n3 = 0, nuv = 0;
-        if (valid) nuv = yz_gather(S, base, c, C2, h, n3, P);
-        const Stale stj{(short)(valid ? q.stdet : DET_SENTINEL), valid ? q.stpos : 0.f, valid ? q.stdrift : 0.f};
-        const float y0 = valid ? q.y0 : 0.f, ty = valid ? q.ty : 0.f;
-        const float ey0 = valid ? q.ey0 : 0.f, ety = valid ? q.ety : 0.f;
-        const unsigned seg = __match_any_sync(0xffffffffu, g);
-        const unsigned vm = __ballot_sync(0xffffffffu, valid);
-        const bool carried_f = (g == cg) && cg_hasf;
-        const int fl = __ffs(vm & seg) - 1;
-        const bool is_first = valid && !carried_f && fl == lane;
-        if (is_first) walk_uv(nuv, h, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
-        short sig[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const short mine = (k < n3) ? h[k].sign : (short)0;
-            const short v = (short)__shfl_sync(0xffffffffu, (int)mine, fl < 0 ? 0 : fl);
-            sig[k] = carried_f ? cg_sig[k] : v;
-        }
-        bool xok = false;
-        short xval = 0;
-        if (valid && !is_first) {
-            const int xi = cross_pair_index(n3, h, nuv);
-            if (xi >= 0) {
-                const int k = lr_pair_newhits_ool(x0, tx, y0, ty, ex0, etx, ey0, ety, h[xi].det, h[xi + 1].det, h[xi].pos,
-                                              h[xi].drift, h[xi + 1].pos, h[xi + 1].drift, P, 150.f);
-                if (k >= 0) {
-                    xok = true;
-                    xval = c_lrpossibility[k][0];
-                }
-            }
-        }
-        const unsigned xm = __ballot_sync(0xffffffffu, xok);
-        const int xs = last_lane(xm & seg & lanemask_lt());
-        const short xprev = (short)__shfl_sync(0xffffffffu, (int)xval, xs < 0 ? 0 : xs);
-        bool pass = false;
-        float chi2 = 0.f;
-        float resid[12];
-        if (valid && !is_first) {
-            for (int k = 0; k < n3 && k < 4; ++k) h[k].sign = sig[k];
-            if (n3 > 0) {
-                if (xs >= 0) h[n3 - 1].sign = xprev;
-                else if (g == cg && cg_hascross) h[n3 - 1].sign = cg_cross;
-            }
-            walk_uv(nuv, h, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
-        }
-        if (valid) {
-            pass = yz_gates(E, P, x0, y0, tx, ty, ex0, ey0, etx, ety);
-            if (pass) chi2 = yz_chi2(S, h, nuv, nhx, P, x0, y0, tx, ty, resid);
-        }
-        // carry of the sign state to the next survivor chunk
-        {
-            const int last = last_lane(vm);
-            const int gl = __shfl_sync(0xffffffffu, g, last < 0 ? 0 : last);
-            const unsigned segl = __ballot_sync(0xffffffffu, valid && g == gl);
-            const int fnew = __ffs(__ballot_sync(0xffffffffu, is_first) & segl) - 1;
-            short ns[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) ns[k] = (short)__shfl_sync(0xffffffffu, (int)sig[k], fnew < 0 ? 0 : fnew);
-            const int xl = last_lane(xm & segl);
-            const short nx = (short)__shfl_sync(0xffffffffu, (int)xval, xl < 0 ? 0 : xl);
-            const bool cont = (gl == cg);
-            if (fnew >= 0) {
-                cg_hasf = true;
-                for (int k = 0; k < 4; ++k) cg_sig[k] = ns[k];
-            } else if (!cont) {
-                cg_hasf = false;
-            }
-            if (xl >= 0) {
-                cg_hascross = true;
-                cg_cross = nx;
-            } else if (!cont) {
-                cg_hascross = false;
-            }
-            cg = gl;
-        }
-        // best: min (chi2, index) over chi2 < 10000.1 (K:1778)
-        const bool elig = pass && chi2 < 10000.1f;
-        const unsigned key = elig ? __float_as_uint(chi2) : 0xffffffffu;
-        const unsigned kmin = __reduce_min_sync(0xffffffffu, key);
-        if (kmin != 0xffffffffu) {
-            const int win = __ffs(__ballot_sync(0xffffffffu, key == kmin)) - 1;
-            const int cw = __shfl_sync(0xffffffffu, c, win);
-            const unsigned long long full = ((unsigned long long)kmin << 32) | (unsigned long long)(unsigned)cw;
-            if (full < best) {
-                best = full;
-                if (lane == win) {
-                    S.b.key = full;
-                    S.b.nuv = nuv;
-                    S.b.chi2 = chi2;
-                    S.b.ty = ty;
-                    S.b.y0 = y0;
-                    S.b.ety = ety;
-                    S.b.ey0 = ey0;
-                    for (int n = 0; n < nuv; ++n) {
-                        S.b.det[n] = h[n].det;
-                        S.b.el[n] = h[n].el;
-                        S.b.pos[n] = h[n].pos;
-                        S.b.drift[n] = h[n].drift;
-                        S.b.sign[n] = h[n].sign;
-                        S.b.tdc[n] = h[n].tdc;
-                    }
-                    for (int n = 0; n < nhx + nuv; ++n) S.b.res[n] = resid[n];
-                }
-            }
-        }
-        __syncwarp();
-    };
 
     const YzHit *Lh[8];
 #pragma unroll
@@ -778,7 +804,7 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
             }
         }
         const bool more = basec < c1;
-        if (!more && qn == 0) break;
+        if (!more && qn == qh) break;
         if (more) {
             const int c = basec + lane;
             const bool valid = c < c1;
@@ -884,7 +910,7 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
                 e.stdet = stj.det;
                 e.stpos = stj.pos;
                 e.stdrift = stj.drift;
-                S.q[qn + __popc(pm & lanemask_lt())] = e;
+                Q[qn + __popc(pm & lanemask_lt())] = e;
             }
             qn += __popc(pm);
             __syncwarp();
@@ -902,15 +928,19 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
             d2 -= cy ? nu3 : 0;
             d3 += s3 + cy;
         }
-        if (qn >= 32 || (!more && qn > 0)) {
-            const int n = min(qn, 32);
-            phase2(n);
-            if (lane < qn - n) S.q[lane] = S.q[n + lane];
-            qn -= n;
-            __syncwarp();
+        if (qn > qcap - 32 || (!more && qn > qh)) {
+            // a full queue (the next chunk could add 32) or the end of the
+            // range: evaluate every waiting survivor, 32 at a time, in order
+            while (qh < qn) {
+                const int n = min(qn - qh, 32);
+                yz_phase2(S, E, base, C2, P, Q + qh, n, cs);
+                qh += n;
+                __syncwarp();
+            }
+            qh = qn = 0;
         }
     }
-    return best;
+    return cs.best;
 }
 
 // write the best combination into the track record (K:1804-1825)
@@ -957,6 +987,7 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
     const int lane = threadIdx.x & 31;
     YzWarp &S = warps[w];
     YzHit *garena = yz_garena(sc, blockIdx.x * W + w);
+    PassEntryStore *Q = sc.qbuf + (long)((blockIdx.x * W + w) % sc.garena_warps) * sc.qcap;
 
     // planning units (event, YZ_PLAN_CHUNK slots) from a device counter: slots
     // are independent (one reference thread each), events very uneven
@@ -1050,7 +1081,7 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
                 }
                 if (inline_it) {
                     budget -= Cl;
-                    const unsigned long long bk = yz_range(S, E, base, 0, C, st, P);
+                    const unsigned long long bk = yz_range(S, E, base, 0, C, st, P, Q, sc.qcap);
                     __syncwarp();
                     if (bk != ~0ull) yz_store(T, S.b, S.nhx);
                 }
@@ -1073,6 +1104,7 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
     const int lane = threadIdx.x & 31;
     YzWarp &S = warps[w];
     YzHit *garena = yz_garena(sc, blockIdx.x * W + w);
+    PassEntryStore *Q = sc.qbuf + (long)((blockIdx.x * W + w) % sc.garena_warps) * sc.qcap;
     const int nunits = min((int)sc.counters[0], sc.cap_units);
     for (;;) {
         int u = 0;
@@ -1092,7 +1124,7 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
         Stale st[4];
         for (int k = 0; k < 4; ++k) st[k] = un.entry[k];
         const long C2 = (long)S.np[0] * S.np[1];
-        const unsigned long long bk = yz_range(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P);
+        const unsigned long long bk = yz_range(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, Q, sc.qcap);
         __syncwarp();
         YzBest *dst = sc.best + u;
         if (bk == ~0ull) {
@@ -1143,16 +1175,28 @@ size_t yz_smem_bytes(int warps) {
 
 // Scratch the YZ stage needs: queue of units, per-unit best records, heavy
 // tracklets, per-warp overflow arenas.
-size_t yz_scratch_bytes(int cap_units, int cap_heavy, int garena_warps) {
+size_t yz_scratch_bytes_q(int cap_units, int cap_heavy, int garena_warps, int qcap) {
     size_t b = 256 + (sizeof(YzUnit) + sizeof(YzBest)) * (size_t)cap_units + sizeof(YzHeavy) * (size_t)cap_heavy;
     b = (b + 255) & ~size_t(255);
-    return b + sizeof(YzHit) * YZ_GARENA_HITS * (size_t)garena_warps;
+    b += sizeof(YzHit) * YZ_GARENA_HITS * (size_t)garena_warps;
+    return b + sizeof(PassEntryStore) * (size_t)qcap * (size_t)garena_warps;
+}
+
+// the static (no-allocation) scratch: survivor queues of YZ_QCAP_MIN entries
+size_t yz_scratch_bytes(int cap_units, int cap_heavy, int garena_warps) {
+    return yz_scratch_bytes_q(cap_units, cap_heavy, garena_warps, YZ_QCAP_MIN);
+}
+
+// a context's scratch
+size_t yz_scratch_bytes_ctx(int cap_units, int cap_heavy, int garena_warps) {
+    return yz_scratch_bytes_q(cap_units, cap_heavy, garena_warps, YZ_QCAP_CTX);
 }
 
 template <int W>
 static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
                                   const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
-                                  int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, YzPrune prune) {
+                                  int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, YzPrune prune,
+                                  int qcap) {
     if (n_events <= 0) return cudaSuccess;
     const size_t smem = yz_smem_bytes(W);
     cudaError_t err;
@@ -1172,9 +1216,12 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
     p += sizeof(YzHeavy) * (size_t)cap_heavy;
     p = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
     sc.garena = reinterpret_cast<YzHit *>(p);
+    p += sizeof(YzHit) * YZ_GARENA_HITS * (size_t)garena_warps;
+    sc.qbuf = reinterpret_cast<PassEntryStore *>(p);
     sc.cap_units = cap_units;
     sc.cap_heavy = cap_heavy;
     sc.garena_warps = garena_warps;
+    sc.qcap = qcap;
     if ((err = cudaMemsetAsync(sc.counters, 0, 256, stream))) return err;
     const long blocks = garena_warps / W;
     const long blocks_plan = min(((long)n_events * (OR_NSLOTS / YZ_PLAN_CHUNK) + W - 1) / W, blocks);
@@ -1190,18 +1237,18 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
 static cudaError_t launch_yz_w(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
                                const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
                                int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, YzPrune prune,
-                               int warps) {
+                               int warps, int qcap) {
     switch (warps) {
     case 1: return launch_yz_impl<1>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                     garena_warps, stream, sm_count, prune);
+                                     garena_warps, stream, sm_count, prune, qcap);
     case 2: return launch_yz_impl<2>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                     garena_warps, stream, sm_count, prune);
+                                     garena_warps, stream, sm_count, prune, qcap);
     case 8: return launch_yz_impl<8>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                     garena_warps, stream, sm_count, prune);
+                                     garena_warps, stream, sm_count, prune, qcap);
     case 16: return launch_yz_impl<16>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                       garena_warps, stream, sm_count, prune);
+                                       garena_warps, stream, sm_count, prune, qcap);
     default: return launch_yz_impl<4>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                      garena_warps, stream, sm_count, prune);
+                                      garena_warps, stream, sm_count, prune, qcap);
     }
 }
 
@@ -1209,7 +1256,7 @@ cudaError_t launch_yz(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_vi
                       int n_events, uint32_t *errw, void *scratch, int cap_units, int cap_heavy, int garena_warps,
                       cudaStream_t stream, int sm_count) {
     return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
-                       sm_count, YzPrune{nullptr, nullptr, 0}, 4);
+                       sm_count, YzPrune{nullptr, nullptr, 0}, 4, YZ_QCAP_MIN);
 }
 
 // with `warps` events (work units) per CTA: 1, 2, 4, 8 or 16
@@ -1217,7 +1264,7 @@ cudaError_t launch_yz_tuned(const or_plane_t *d_plane, or_hits_view_t hv, or_tra
                             const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
                             int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, int warps) {
     return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
-                       sm_count, YzPrune{nullptr, nullptr, 0}, warps);
+                       sm_count, YzPrune{nullptr, nullptr, 0}, warps, YZ_QCAP_CTX);
 }
 
 // YZ with the scorer's keep flags: pruned tracklets are left as tracklets no
@@ -1227,7 +1274,7 @@ cudaError_t launch_yz_pruned(const or_plane_t *d_plane, or_hits_view_t hv, or_tr
                              int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count,
                              const int32_t *row_off, const uint8_t *keep, long max_rows, int warps) {
     return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
-                       sm_count, YzPrune{row_off, keep, max_rows}, warps);
+                       sm_count, YzPrune{row_off, keep, max_rows}, warps, YZ_QCAP_CTX);
 }
 
 }  // namespace orgpu
