@@ -755,11 +755,6 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
     const int nhx = S.nhx;
     Phase2Carry cs;
     int qh = 0, qn = 0;  // survivors Q[qh..qn) wait for the full evaluation
-
-
-    const YzHit *Lh[8];
-#pragma unroll
-    for (int l = 0; l < 8; ++l) Lh[l] = yz_list(S, base, l);
     const int nv2 = S.np[1];
     // Lane's combination as digits (iu2, iv2, iu3, iv3) in radices (nu2, nv2,
     // nu3, nv3) -- the reference's index order (u2 fastest) -- advanced by 32
@@ -818,13 +813,22 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
             if (valid) {
                 if (need3) {
                     const short2 pu = S.pair[2][d2], pv = S.pair[3][d3];
+                    const unsigned long long offs =
+                        (unsigned long long)(pu.x >= 0 ? S.woff[4] + pu.x : 0xFFFF) |
+                        ((unsigned long long)(pu.y >= 0 ? S.woff[5] + pu.y : 0xFFFF) << 16) |
+                        ((unsigned long long)(pv.x >= 0 ? S.woff[6] + pv.x : 0xFFFF) << 32) |
+                        ((unsigned long long)(pv.y >= 0 ? S.woff[7] + pv.y : 0xFFFF) << 48);
                     Fit2 f;
                     int nu = 0, nv = 0;
-                    if (pu.x >= 0) { const YzHit &r = Lh[4][pu.x]; if (r.acc) { f.add(r.Y, r.z, r.eY); ++nu; } }
-                    if (pu.y >= 0) { const YzHit &r = Lh[5][pu.y]; if (r.acc) { f.add(r.Y, r.z, r.eY); ++nu; } }
-                    if (nu > 0) {
-                        if (pv.x >= 0) { const YzHit &r = Lh[6][pv.x]; if (r.acc) { f.add(r.Y, r.z, r.eY); ++nv; } }
-                        if (pv.y >= 0) { const YzHit &r = Lh[7][pv.y]; if (r.acc) { f.add(r.Y, r.z, r.eY); ++nv; } }
+#pragma unroll 1
+                    for (int a = 0; a < 4; ++a) {
+                        if (a == 2 && nu == 0) break;  // no u3 hit: v3 is not loaded
+                        const int off = (int)((offs >> (16 * a)) & 0xFFFFull);
+                        if (off == 0xFFFF) continue;
+                        const YzHit &r = base[off];
+                        if (!r.acc) continue;
+                        f.add(r.Y, r.z, r.eY);
+                        if (a < 2) ++nu; else ++nv;
                     }
                     f3 = f;
                     n3 = nu + nv;
@@ -852,18 +856,29 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
                             ++nuv;
                         }
                     };
-                    if (pu.x >= 0) attempt(S.woff[0] + pu.x);
-                    if (pu.y >= 0) attempt(S.woff[1] + pu.y);
-                    const int nu2hits = nuv;
-                    if (nu2hits > n3) {
-                        const short2 pv = S.pair[1][d1];
-                        if (pv.x >= 0) attempt(S.woff[2] + pv.x);
-                        if (pv.y >= 0) attempt(S.woff[3] + pv.y);
-                        if (nuv > nu2hits) {  // the v2 group gave a hit: the fit is reached
-                            f.solve(y0, ty, ey0, ety);
-                            pass1 = !(fabsf(y0) > Y0_MAX + 2 * ey0 || fabsf(ty) > TY_MAX + 2 * ety);
+                    // the four attempts as one loop body: arena offsets
+                    // (0xFFFF = no hit) of u2, u2', v2, v2' packed in 64 bits
+                    const short2 pv = S.pair[1][d1];
+                    const unsigned long long offs =
+                        (unsigned long long)(pu.x >= 0 ? S.woff[0] + pu.x : 0xFFFF) |
+                        ((unsigned long long)(pu.y >= 0 ? S.woff[1] + pu.y : 0xFFFF) << 16) |
+                        ((unsigned long long)(pv.x >= 0 ? S.woff[2] + pv.x : 0xFFFF) << 32) |
+                        ((unsigned long long)(pv.y >= 0 ? S.woff[3] + pv.y : 0xFFFF) << 48);
+                    int nu2hits = n3;
+#pragma unroll 1
+                    for (int a = 0; a < 4; ++a) {
+                        if (a == 2) {
+                            nu2hits = nuv;
+                            if (nu2hits == n3) break;  // the u2 group gave no hit
                         }
+                        const int off = (int)((offs >> (16 * a)) & 0xFFFFull);
+                        if (off != 0xFFFF) attempt(off);
                     }
+                    if (nu2hits > n3 && nuv > nu2hits) {  // the v2 group gave a hit: the fit is reached
+                        f.solve(y0, ty, ey0, ety);
+                        pass1 = !(fabsf(y0) > Y0_MAX + 2 * ey0 || fabsf(ty) > TY_MAX + 2 * ety);
+                    }
+
                 }
             }
             // --- scratch entry past the hit count ------------------------------
@@ -875,7 +890,7 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
             {
                 const int j = nuv;
                 const unsigned lt = lanemask_lt();
-#pragma unroll
+#pragma unroll 1
                 for (int k = 0; k < 4; ++k) {
                     const bool mine = (wmask >> k) & 1u;
                     const int ok = (int)((own >> (16 * k)) & 0xFFFFull);
