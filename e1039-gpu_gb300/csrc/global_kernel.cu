@@ -23,6 +23,7 @@ namespace orgpu {
 constexpr int GL_PAIRCAP = 128;
 constexpr int GL_NST = 7;  // scratch entries tracked for stale reads: 0..6
 
+
 struct GlWarp {
     short2 pairs[3][GL_PAIRCAP];  // x1, u1, v1
     WindowScratch W;
@@ -308,9 +309,10 @@ __global__ void __launch_bounds__(W * 32)
                         for (int k = 0; k < nhx; ++k) h[k] = xh[k];
                         float Yu[4], eYu[4], Zu[4];
                         int nuv = 0, nhu = 0;
-                        Stale own[GL_NST];
+                        // scratch entries this combination writes: (list << 12 | hit index)
+                        // codes, 16 bits each, entries 0-3 and 4-6
+                        unsigned long long own_lo = 0ull, own_hi = 0ull;
                         unsigned wmask = 0u;
-                        for (int k = 0; k < GL_NST; ++k) own[k] = Stale{DET_SENTINEL, 0.f, 0.f};
                         bool reached = false, pass1 = false;
                         float yc = 0.f, tyc = 0.f, eyc = 0.f, etyc = 0.f;
                         if (valid) {
@@ -326,7 +328,9 @@ __global__ void __launch_bounds__(W * 32)
                                 u.drift = hc[lk].drift(hidx);
                                 u.pos = hc[lk].pos(hidx);
                                 if (a < GL_NST) {
-                                    own[a] = Stale{u.det, u.pos, u.drift};
+                                    const unsigned long long code = (unsigned long long)((lk << 12) | hidx);
+                                    if (a < 4) own_lo = (own_lo & ~(0xFFFFull << (16 * a))) | (code << (16 * a));
+                                    else own_hi = (own_hi & ~(0xFFFFull << (16 * (a - 4)))) | (code << (16 * (a - 4)));
                                     wmask |= 1u << a;
                                 }
                                 float yy, ey;
@@ -337,14 +341,22 @@ __global__ void __launch_bounds__(W * 32)
                                     ++nuv;
                                 }
                             };
-                            if (pu.x >= 0) attempt(2, pu.x);
-                            if (pu.y >= 0) attempt(3, pu.y);
-                            nhu = nuv;
-                            if (nhu > 0) {
-                                if (pv.x >= 0) attempt(4, pv.x);
-                                if (pv.y >= 0) attempt(5, pv.y);
-                                reached = nuv > nhu;
+                            // u1, u1', then v1, v1' if the u1 group gave a hit, as one loop body
+                            const unsigned long long codes =
+                                (unsigned long long)(pu.x >= 0 ? (2 << 12) | pu.x : 0xFFFF) |
+                                ((unsigned long long)(pu.y >= 0 ? (3 << 12) | pu.y : 0xFFFF) << 16) |
+                                ((unsigned long long)(pv.x >= 0 ? (4 << 12) | pv.x : 0xFFFF) << 32) |
+                                ((unsigned long long)(pv.y >= 0 ? (5 << 12) | pv.y : 0xFFFF) << 48);
+#pragma unroll 1
+                            for (int q = 0; q < 4; ++q) {
+                                if (q == 2) {
+                                    nhu = nuv;
+                                    if (nhu == 0) break;
+                                }
+                                const int code = (int)((codes >> (16 * q)) & 0xFFFFull);
+                                if (code != 0xFFFF) attempt(code >> 12, code & 0xFFF);
                             }
+                            reached = nhu > 0 && nuv > nhu;
                             if (reached) {  // K:2368-2379
                                 Fit2 f;
                                 for (int k = 0; k < nyh; ++k) f.add(S.Y[k], S.Zy[k], S.eY[k]);
@@ -356,26 +368,29 @@ __global__ void __launch_bounds__(W * 32)
                         const int nall = nhx + nuv;
                         // scratch entry past the hit count
                         Stale st{DET_SENTINEL, 0.f, 0.f};
+                        int st_code = -1;
                         {
                             const unsigned lt = lanemask_lt();
-#pragma unroll
+                            auto decode = [&](int code) {
+                                const int lk = code >> 12, hidx = code & 0xFFF;
+                                return Stale{dl[lk], hc[lk].pos(hidx), hc[lk].drift(hidx)};
+                            };
+#pragma unroll 1
                             for (int k = 0; k < GL_NST; ++k) {
-                                const unsigned m = __ballot_sync(0xffffffffu, (wmask >> k) & 1u);
+                                const bool mine = (wmask >> k) & 1u;
+                                const int code = (int)(((k < 4 ? own_lo : own_hi) >> (16 * (k & 3))) & 0xFFFFull);
+                                const unsigned m = __ballot_sync(0xffffffffu, mine);
                                 const int src = last_lane(m & lt);
-                                const short sd = (short)__shfl_sync(0xffffffffu, (int)own[k].det, src < 0 ? 0 : src);
-                                const float sp = __shfl_sync(0xffffffffu, own[k].pos, src < 0 ? 0 : src);
-                                const float sdr = __shfl_sync(0xffffffffu, own[k].drift, src < 0 ? 0 : src);
+                                const int sc = __shfl_sync(0xffffffffu, code, src < 0 ? 0 : src);
                                 if (nall == k) {
-                                    if ((wmask >> k) & 1u) st = own[k];
-                                    else if (src >= 0) st = Stale{sd, sp, sdr};
+                                    if (mine) st_code = code;
+                                    else if (src >= 0) st_code = sc;
                                     else st = stc[k];
                                 }
                                 const int lw = last_lane(m);
-                                const short cd = (short)__shfl_sync(0xffffffffu, (int)own[k].det, lw < 0 ? 0 : lw);
-                                const float cp = __shfl_sync(0xffffffffu, own[k].pos, lw < 0 ? 0 : lw);
-                                const float cdr = __shfl_sync(0xffffffffu, own[k].drift, lw < 0 ? 0 : lw);
-                                if (lw >= 0) stc[k] = Stale{cd, cp, cdr};
+                                if (lw >= 0) stc[k] = decode(__shfl_sync(0xffffffffu, code, lw));
                             }
+                            if (pass1 && st_code >= 0) st = decode(st_code);
                         }
                         // y0/ty of the last combination that reached the fit
                         {

@@ -46,7 +46,10 @@ constexpr int YZ_ARENA_HITS = 192;      // windowed hits kept in shared memory p
 constexpr long YZ_LIGHT = OR_YZ_LIGHT;         // combinations a planning warp evaluates itself per tracklet
 constexpr long YZ_CHUNK_INLINE = OR_YZ_LIGHT;  // ... and per planning unit
 constexpr int YZ_PLAN_CHUNK = 8;        // slots per planning unit
-constexpr long YZ_UNIT = 4096;          // combinations per queued unit (whole (u3,v3) iterations)
+#ifndef OR_YZ_UNIT
+#define OR_YZ_UNIT 8192
+#endif
+constexpr long YZ_UNIT = OR_YZ_UNIT;    // live combinations per queued unit (whole (u3,v3) iterations)
 constexpr int YZ_GARENA_HITS = 8 * YZ_MAXWIN;  // per-warp global overflow arena
 // survivors of the first cut wait in a per-warp queue in global memory and
 // are evaluated in a batch when it fills or the range ends, so that the two
