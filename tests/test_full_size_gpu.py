@@ -1,0 +1,97 @@
+"""The plain path at the benchmark's full size (100,000 uneven-noise events),
+through properties that do not need the oracle at that size:
+
+  - determinism: the same batch run twice gives the same buffers, bit for bit;
+  - event independence: the batch run as four chunks gives, event by event,
+    the same tracks and flags as the batch run whole (the work queue, the
+    planning units and the overflow arenas differ between the two);
+  - well-formed output: every global track has 5-18 hits with detector ids
+    in the chamber range, charge +-1, a finite chi2 and 1/p in the window
+    the global stage enforces.
+
+Bit-exactness against the oracle is tested on smaller batches
+(test_gpu_parity.py); this adds the full-size behaviour of the queue and
+the scratch limits.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N_EVENTS = 100000
+
+
+@pytest.fixture(scope="module")
+def full(geometry):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from orgpu import synth as S
+    plane, wp = geometry
+    geo = S.Geometry(plane, wp)
+    rec, off, _ = S.generate(geo, S.config_uneven(N_EVENTS, 906002))
+    rec, off = S.cap_records(rec, off)
+    return plane, geo, rec, off
+
+
+def _run(plane, geo, rec, off):
+    import torch
+    from orgpu import pipeline
+    n = len(off) - 1
+    rc = pipeline.Reconstruction(plane, 0)
+    b = pipeline.DeviceBatch(n)
+    rc.pack(b, torch.from_numpy(rec.view(np.uint8)).cuda(), torch.from_numpy(off).cuda(),
+            torch.from_numpy(geo.wire_pos_f32().reshape(-1)).cuda())
+    rc.run_batch(b)
+    rc.sync()
+    t = b.download_tracks()
+    return t.ntracks.reshape(n, -1).copy(), t.tracks.reshape(n, -1).copy(), b.toomany.cpu().numpy().copy()
+
+
+def _valid_tracks(nt, tr):
+    """records of the valid slots only (the rest of a slot is never written)"""
+    n = nt.shape[0]
+    T = tr.reshape(n, 32, 16, 148)
+    m = np.arange(16)[None, None, :] < nt.reshape(n, 32)[:, :, None].astype(np.int64)
+    return T, m
+
+
+def test_full_batch_deterministic_and_chunk_independent(full):
+    plane, geo, rec, off = full
+    nt1, tr1, f1 = _run(plane, geo, rec, off)
+    nt2, tr2, f2 = _run(plane, geo, rec, off)
+    np.testing.assert_array_equal(nt1, nt2)
+    np.testing.assert_array_equal(f1, f2)
+    T1, m1 = _valid_tracks(nt1, tr1)
+    T2, _ = _valid_tracks(nt2, tr2)
+    assert np.array_equal(T1[m1].view(np.uint32), T2[m1].view(np.uint32))
+    # four chunks
+    n = len(off) - 1
+    cuts = np.linspace(0, n, 5).astype(int)
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        r = rec[off[a]:off[b]]
+        o = (off[a:b + 1] - off[a]).astype(off.dtype)
+        ntc, trc, fc = _run(plane, geo, r, o)
+        np.testing.assert_array_equal(ntc, nt1[a:b])
+        np.testing.assert_array_equal(fc, f1[a:b])
+        Tc, mc = _valid_tracks(ntc, trc)
+        assert np.array_equal(Tc[mc].view(np.uint32), T1[a:b][mc].view(np.uint32))
+
+
+def test_full_batch_tracks_well_formed(full):
+    from orgpu import layout as L
+    plane, geo, rec, off = full
+    nt, tr, flags = _run(plane, geo, rec, off)
+    T, m = _valid_tracks(nt, tr)
+    recs = T[m & (flags == 0)[:, None, None]]
+    g = recs[recs[:, L.TRK_STID] == 6]
+    assert len(g) > 100000
+    nh = g[:, L.TRK_NHITS].astype(int)
+    assert ((nh >= 5) & (nh <= 18)).all()
+    for row, k in zip(g, nh):
+        d = row[L.TRK_HIT_DETID:L.TRK_HIT_DETID + k]
+        assert ((d >= 1) & (d <= 30)).all()
+    assert np.isin(g[:, L.TRK_CHARGE], (-1.0, 1.0)).all()
+    assert np.isfinite(g[:, L.TRK_CHI2]).all()
+    invp = g[:, L.TRK_INVP]
+    assert ((invp > 0.0) & (invp < 0.25)).all()
