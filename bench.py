@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-rt", action="store_true", help="skip the R-T calibration packer leg")
     return ap.parse_args()
 
 
@@ -326,6 +327,7 @@ def main():
         cpu = {"value": ns / dt, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": "first %d events of the workload, one pass, all host threads" % ns}
 
+    rt_res = None if args.no_rt else rt_leg(args, rc, b, plane, rec, d_rec, d_off, d_wp, dev)
     learned_res = None if args.no_learned else learned_leg(args, rc, b, rec, off, d_rec, d_off, d_wp, value, dev)
     serving_res = None if args.no_serving else serving_leg(plane, wp, tuned)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -338,7 +340,7 @@ def main():
             "gpu_launches": LAUNCHES_PER_STEP * args.steps,
             "stage_ms": stage_ms,
             "events_rejected_frac": float(toomany.mean()), "global_tracks_last_step": ntrk,
-            "learned": learned_res, "serving": serving_res,
+            "learned": learned_res, "serving": serving_res, "rt_calibration": rt_res,
             "autotune": None if tuned is None else {"events_per_cta": tuned["best"], "sample_events": tuned["events"],
                                                     "stage_ms_by_shape": tuned["ms"]}}
     print(json.dumps(line))
@@ -347,6 +349,41 @@ def main():
 # kernels one step launches: pack, event reducer, XZ, YZ plan/work/apply,
 # cleaning, global tracking
 LAUNCHES_PER_STEP = 8
+
+
+def rt_leg(args, rc, b, plane, rec, d_rec, d_off, d_wp, dev):
+    """The device packer with the drift distance from the R-T calibration
+    (clamped cubic spline per plane, evaluated in double per hit), and the
+    same conversion in place on packed hits, against the plain packer, on
+    the workload's records; device time per launch (CUDA events)."""
+    import torch
+    from orgpu import CALIBRATION_E906, _lib, pipeline
+    rt, _ = _lib.rt_load(CALIBRATION_E906, plane)
+    d_rt = pipeline.rt_to_device(rt, dev.index)
+    stream = torch.cuda.current_stream(dev)
+    legs = {"pack_ms": lambda: rc.pack(b, d_rec, d_off, d_wp),
+            "pack_rt_ms": lambda: rc.pack_rt(b, d_rec, d_off, d_wp, d_rt),
+            "rt_apply_ms": lambda: rc.rt_apply(b, d_rt)}
+    out = {}
+    for name, fn in legs.items():
+        for _ in range(args.warmup):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = e0.elapsed_time(e1) / args.steps
+    # leave the batch as the plain chain had it
+    rc.pack(b, d_rec, d_off, d_wp)
+    rc.sync()
+    n_rt = int(np.isin(rec["det"], np.r_[1:31, 47:55]).sum())
+    out["records"] = int(len(rec))
+    out["converted_hits"] = n_rt
+    # algorithmic bytes of the packer: 16 B record read + 20 B hit written
+    out["pack_rt_gbs"] = 36.0 * len(rec) / (out["pack_rt_ms"] / 1000.0) / 1e9
+    return out
 
 
 def learned_leg(args, rc, b_plain, rec, off, d_rec, d_off, d_wp, plain_value, dev):

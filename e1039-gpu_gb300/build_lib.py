@@ -17,7 +17,7 @@ CU = ["er_kernel.cu", "xz_kernel.cu", "yz_kernel.cu", "clean_kernel.cu", "global
       "collect_kernel.cu", "learned_kernel.cu", "mlp_kernel.cu", "select_kernel.cu", "physics_kernel.cu", "output_kernel.cu",
       "yz_noalloc.cu",
       "capi.cu"]
-CPP = ["geometry.cpp"]
+CPP = ["geometry.cpp", "rt_calib.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
                      "-ftz=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]

@@ -27,8 +27,9 @@ cudaError_t launch_histograms(or_tracks_view_t, or_dimuons_view_t, const int32_t
 cudaError_t launch_back_clean(or_tracks_view_t, const uint8_t *, int, cudaStream_t, int, int);
 cudaError_t launch_global(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
                           unsigned long long *, cudaStream_t, int, int);
-cudaError_t launch_pack(const or_hit_record_t *, const int64_t *, int, const float *, or_hits_view_t, cudaStream_t,
-                        int);
+cudaError_t launch_pack(const or_hit_record_t *, const int64_t *, int, const float *, const or_rt_table_t *,
+                        or_hits_view_t, cudaStream_t, int);
+cudaError_t launch_rt_apply(const or_rt_table_t *, or_hits_view_t, int, cudaStream_t, int);
 cudaError_t launch_collect(or_tracks_view_t, const uint8_t *, int, float, float *, long long, unsigned long long *,
                            cudaStream_t);
 cudaError_t launch_yz_pruned(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
@@ -635,8 +636,28 @@ int or_pack_hits(or_ctx_t *ctx, const or_hit_record_t *records, const int64_t *r
     if (n_events < 0 || !rec_offsets || !wire_pos_f) return fail(OR_ERR_ARG, "bad packer arguments");
     if ((rc = check_hits(hits))) return rc;
     cudaError_t e =
-        orgpu::launch_pack(records, rec_offsets, n_events, wire_pos_f, hits, S(stream), ctx->sm_count);
+        orgpu::launch_pack(records, rec_offsets, n_events, wire_pos_f, nullptr, hits, S(stream), ctx->sm_count);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "packer launch");
+}
+
+int or_pack_hits_rt(or_ctx_t *ctx, const or_hit_record_t *records, const int64_t *rec_offsets, int n_events,
+                    const float *wire_pos_f, const or_rt_table_t *rt_dev, or_hits_view_t hits, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n_events < 0 || !rec_offsets || !wire_pos_f || !rt_dev) return fail(OR_ERR_ARG, "bad packer arguments");
+    if ((rc = check_hits(hits))) return rc;
+    cudaError_t e =
+        orgpu::launch_pack(records, rec_offsets, n_events, wire_pos_f, rt_dev, hits, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "packer launch");
+}
+
+int or_rt_apply(or_ctx_t *ctx, const or_rt_table_t *rt_dev, or_hits_view_t hits, int n_events, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (n_events < 0 || !rt_dev) return fail(OR_ERR_ARG, "bad R-T arguments");
+    if ((rc = check_hits(hits))) return rc;
+    cudaError_t e = orgpu::launch_rt_apply(rt_dev, hits, n_events, S(stream), ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "R-T launch");
 }
 
 int or_collect_tracks(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, int n_events, float stid,

@@ -53,6 +53,7 @@ static __device__ void sagitta_st1(float x0, float tx, float y0, float ty, int d
     const float z_st3 = P.z[detid_lasthit];
     const float x_st3 = x0 + tx * z_st3;
     const float y_st3 = y0 + ty * z_st3;
+#pragma unroll 1
     for (int i = 0; i < 3; i++) {
         const short detid = (short)(2 * i + 2);
         const short idx = c_planetype[detid / 2 - 1];
@@ -90,6 +91,7 @@ constexpr int GL_CHUNK = 8;
 // scratch entry past the end, then the singles (H:785-804)
 __device__ __noinline__ void gl_walk(GHit *h, int nall, const Stale &st, float xs0, float xst, float yc, float tyc,
                                      float ex0s, float etxs, float eyc, float etyc, const or_plane_t &P) {
+#pragma unroll 1
     for (int i = 0; i < nall;) {
         const int j = i + 1;
         const short di = h[i].det;
@@ -111,6 +113,7 @@ __device__ __noinline__ void gl_walk(GHit *h, int nall, const Stale &st, float x
         }
         i += 2;
     }
+#pragma unroll 1
     for (int k = 0; k < nall; ++k)
         if (!h[k].sign) h[k].sign = single_sign_newhits(xs0, xst, yc, tyc, h[k].det, h[k].pos, P);
 }
@@ -120,6 +123,7 @@ __device__ __noinline__ void gl_walk(GHit *h, int nall, const Stale &st, float x
 __device__ __noinline__ float gl_chi2(const GlWarp &S, int nst, const GHit *h, int nall, const or_plane_t &P, float x0,
                                       float tx, float xs0, float xst, float yc, float tyc, float *rst, float *rs1) {
     float chi2 = 0.f;
+#pragma unroll 1
     for (int m = 0; m < nst && m < 12; ++m) {
         const short d = S.s_det[m];
         const float r = residual_line(x_bep(d, S.s_chan[m], P), y_bep(d, S.s_chan[m], P), z_bep(d, S.s_chan[m], P),
@@ -129,6 +133,7 @@ __device__ __noinline__ float gl_chi2(const GlWarp &S, int nst, const GHit *h, i
         chi2 += r * r / (S.s_res[m] * S.s_res[m]);
     }
     float c1 = 0.f;
+#pragma unroll 1
     for (int k = 0; k < nall; ++k) {
         const short d = h[k].det;
         const float r = residual_line(x_bep(d, h[k].el, P), y_bep(d, h[k].el, P), z_bep(d, h[k].el, P), P.deltapx[d],
@@ -165,12 +170,16 @@ __global__ void __launch_bounds__(W * 32)
         const int slot0 = (int)(u % (OR_NSLOTS / GL_CHUNK)) * GL_CHUNK;
         if (toomany[e]) continue;
         HitPlane hc[6];
+#pragma unroll 1
         for (int k = 0; k < 6; ++k) hc[k] = hits_of(hv, e, dl[k]);
+#pragma unroll 1
         for (int slot = slot0; slot < slot0 + GL_CHUNK; ++slot) {
             const int ntr = min((int)tv.ntracks[e * OR_NSLOTS + slot], OR_SLOTCAP);
             if (ntr == 0) continue;
             Stale stc[GL_NST];
+#pragma unroll 1
             for (int k = 0; k < GL_NST; ++k) stc[k] = Stale{DET_SENTINEL, 0.f, 0.f};
+#pragma unroll 1
             for (int it = 0; it < ntr; ++it) {
                 float *T = trk_rec(tv, e, slot, it);
                 const short nst = (short)min((int)T[OR_TRK_NHITS], 12);  // YZ tracks carry <= 12 hits
@@ -180,6 +189,7 @@ __global__ void __launch_bounds__(W * 32)
                 // get_lasthitdetid (reconstruction_classes.cuh:500-515)
                 short dmax = 1;
                 float zmax = -10000.f;
+#pragma unroll 1
                 for (short k = 0; k < nst; ++k) {
                     const short d = (short)T[OR_TRK_HIT_DETID + k];
                     if (d > 0 && P.z[d] > zmax) {
@@ -191,6 +201,7 @@ __global__ void __launch_bounds__(W * 32)
                 sagitta_st1(x0, tx, y0, ty, dmax, pexp, win, P);
                 int np[3];
                 bool overcap = false;
+#pragma unroll 1
                 for (int q = 0; q < 3; ++q) {
                     const float spacing = c_spacingplane[c_detsuperid[0][q]];
                     np[q] = window_pairs(hc[2 * q], dl[2 * q], hc[2 * q + 1], dl[2 * q + 1], spacing,
@@ -206,6 +217,7 @@ __global__ void __launch_bounds__(W * 32)
                 if (nx1 == 0 || nu1 == 0 || nv1 == 0) continue;
                 // station-2/3 hits and their y (K:2086-2102)
                 int nyh = 0;
+#pragma unroll 1
                 for (int k = 0; k < nst && k < 12; ++k) {
                     const short d = (short)T[OR_TRK_HIT_DETID + k];
                     const float dr = T[OR_TRK_HIT_DRIFT + k];
@@ -233,12 +245,14 @@ __global__ void __launch_bounds__(W * 32)
                 float chi2min = 10000.1f;
                 bool update = false;
                 const int C = nu1 * nv1;
+#pragma unroll 1
                 for (int ix = 0; ix < nx1; ++ix) {
                     // x hits (K:2108-2159), uniform over the warp
                     const short2 px = S.pairs[0][ix];
                     GHit xh[2];
                     float X[3], eX[3], Zx[3];
                     int nhx = 0;
+#pragma unroll 1
                     for (int wsel = 0; wsel < 2; ++wsel) {
                         const int hidx = wsel == 0 ? px.x : px.y;
                         if (hidx < 0) continue;
@@ -253,6 +267,7 @@ __global__ void __launch_bounds__(W * 32)
                         calculate_xz_fy(g.det, g.el, g.drift, 0, y0, ty, P, X[nhx], Zx[nhx]);
                         ++nhx;
                     }
+#pragma unroll 1
                     for (int k = 0; k < nhx; ++k) stc[k] = Stale{xh[k].det, xh[k].pos, xh[k].drift};
                     X[nhx] = x0 + tx * Z_KMAG_BEND;  // K:2163-2165
                     eX[nhx] = ex0 + etx * Z_KMAG_BEND;
@@ -260,12 +275,14 @@ __global__ void __launch_bounds__(W * 32)
                     float xs0, xst, e0, e1;
                     {
                         Fit2 f;
+#pragma unroll 1
                         for (int k = 0; k <= nhx; ++k) f.add(X[k], Zx[k], eX[k]);
                         f.solve(xs0, xst, e0, e1);
                     }
                     float ex0s = xs0, etxs = xst;  // K:2175-2176 as written
                     // resolve_leftright_xhits (H:820-871); the entry past the
                     // x hits holds the KMag point in X and stale det/drift
+#pragma unroll 1
                     for (int n = 0; n < nhx;) {
                         const int j = n + 1;
                         const short di = xh[n].det;
@@ -283,11 +300,14 @@ __global__ void __launch_bounds__(W * 32)
                         }
                         n += 2;
                     }
+#pragma unroll 1
                     for (int k = 0; k < nhx; ++k)
                         if (!xh[k].sign) xh[k].sign = single_sign_xhits(xs0, xst, xh[k].det, X[k], P.z);
+#pragma unroll 1
                     for (int k = 0; k < nhx; ++k) X[k] += (float)xh[k].sign * xh[k].drift;
                     {
                         Fit2 f;
+#pragma unroll 1
                         for (int k = 0; k <= nhx; ++k) f.add(X[k], Zx[k], eX[k]);
                         f.solve(xs0, xst, e0, e1);
                     }
@@ -302,10 +322,12 @@ __global__ void __launch_bounds__(W * 32)
                     float ny0 = 0.f, nty = 0.f;
                     bool xcarry = false;
                     short xcarry_v = 0;
+#pragma unroll 1
                     for (int base = 0; base < C; base += 32) {
                         const int c = base + lane;
                         const bool valid = c < C;
                         GHit h[6];
+#pragma unroll 1
                         for (int k = 0; k < nhx; ++k) h[k] = xh[k];
                         float Yu[4], eYu[4], Zu[4];
                         int nuv = 0, nhu = 0;
@@ -359,7 +381,9 @@ __global__ void __launch_bounds__(W * 32)
                             reached = nhu > 0 && nuv > nhu;
                             if (reached) {  // K:2368-2379
                                 Fit2 f;
+#pragma unroll 1
                                 for (int k = 0; k < nyh; ++k) f.add(S.Y[k], S.Zy[k], S.eY[k]);
+#pragma unroll 1
                                 for (int k = 0; k < nuv; ++k) f.add(Yu[k], Zu[k], eYu[k]);
                                 f.solve(yc, tyc, eyc, etyc);
                                 pass1 = !(fabsf(yc) > Y0_MAX + 2 * eyc || fabsf(tyc) > TY_MAX + 2 * etyc);
@@ -460,7 +484,9 @@ __global__ void __launch_bounds__(W * 32)
                                 S.b_ey0 = eyc;
                                 S.b_einvp = einvP;
                                 S.b_charge = (float)charge;
+#pragma unroll 1
                                 for (int m = 0; m < nst && m < 12; ++m) S.b_res[m] = rst[m];
+#pragma unroll 1
                                 for (int k = 0; k < nall; ++k) {
                                     S.b_det[k] = h[k].det;
                                     S.b_el[k] = h[k].el;

@@ -17,6 +17,14 @@
 
 #include "../../include/or_layout.h"
 
+// Small and per-hit loops on the combinatorial paths are kept rolled
+// (`#pragma unroll 1`): those kernels are limited by instruction-cache
+// misses, and one copy of a loop body costs less there than unrolled copies
+// save in issue slots (measured per loop group on the 100,000-event uneven
+// batch: YZ 191 -> 122 ms, global 33 -> 16 ms, outputs bit-identical).
+// The XZ kernel is the exception: there the unrolled loops are faster.
+
+
 namespace orgpu {
 
 // ---------------------------------------------------------------------------
@@ -206,7 +214,7 @@ __device__ __forceinline__ int lr_pair_newhits(float x0, float tx, float y0, flo
     const float err_inter = fabsf(P.costheta[di] * err_x0) + fabsf(P.sintheta[di] * err_y0);
     int indexmin = -1;
     float pull_min = 1.e6f;
-#pragma unroll
+#pragma unroll 1
     for (int k = 0; k < 4; k++) {
         const float pi = position(pos_i, dr_i, c_lrpossibility[k][0]);
         const float pj = position(pos_j, dr_j, c_lrpossibility[k][1]);
@@ -236,7 +244,7 @@ __device__ __forceinline__ int lr_pair_xhits(float x0, float tx, float err_x0, f
                                              float thr) {
     int indexmin = -1;
     float pull_min = 1.e6f;
-#pragma unroll
+#pragma unroll 1
     for (int k = 0; k < 4; k++) {
         const float pi = position(pos_i, dr_i, c_lrpossibility[k][0]);
         const float pj = position(pos_j, dr_j, c_lrpossibility[k][1]);
@@ -320,6 +328,7 @@ __device__ __forceinline__ bool match_track_XZ_to_hodo(int stid, int detid, cons
     const float fudgefac = c_hodofudgefac[stid];
     const float cellwidth = c_hodoXcellwidth[stid];
     float err_x = 3.f * (fabsf(zarr[detid] * err_tx) + err_x0);
+#pragma unroll 1
     for (int i = 0; i < h.n; i++) {
         const float p = h.pos(i);
         float xmin = p - cellwidth * 0.5f;
@@ -346,6 +355,7 @@ __device__ __forceinline__ bool match_tracklet_to_hodo(int stid, int detid, cons
     const float yhodo = P.z[detid] * ty + y0;
     float err_x = 3.f * (fabsf(P.z[detid] * err_tx) + err_x0);
     const float err_y = 3.f * (fabsf(P.z[detid] * err_ty) + err_y0);
+#pragma unroll 1
     for (int i = 0; i < h.n; i++) {
         const float p = h.pos(i);
         float xmin = p - cellwidth * 0.5f;
@@ -371,10 +381,12 @@ __device__ __forceinline__ bool match_tracklet_to_hodo(int stid, int detid, cons
 // `proj0`/`slope` are the track's intercept and slope in that projection.
 __device__ __forceinline__ int prop_hits(const HitPlane &a, float za, const HitPlane &b, float zb, float tol,
                                          float proj0, float slope) {
+#pragma unroll 1
     for (int n = 0; n < a.n; n++) {
         const float e = slope * za + proj0;
         if (fabsf(a.pos(n) - e) < tol) return 1;
     }
+#pragma unroll 1
     for (int n = 0; n < b.n; n++) {
         const float e = slope * zb + proj0;
         if (fabsf(b.pos(n) - e) < tol) return 1;

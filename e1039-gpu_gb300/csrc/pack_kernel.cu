@@ -9,15 +9,57 @@
 // plane's slot capacity are dropped (the reference host would write past the
 // slot).  One warp per event: a shared-memory histogram per plane, an
 // exclusive scan, then coalesced field writes.
+//
+// With an R-T table the drift field is computed from the tdc as the
+// reference host does while packing (online_reconstruction.cu:387-396); the
+// same conversion also runs in place on hits packed elsewhere (rt_apply).
 #include "or_device.cuh"
 
 namespace orgpu {
 
 constexpr int PK_WARPS = 8;
 
+// Drift distance of a hit on plane det from the R-T calibration, or `drift`
+// unchanged when the plane has no profile (hodoscopes never have one).
+// Evaluation follows the spline's piece convention: piece k covers
+// (t[k], t[k+1]]; x <= t[0] uses piece 0 and x >= t[n-1] piece n-2.  The
+// cubic is evaluated in double in nested form and rounded to float once, as
+// the reference's float drift_distance receives the double result (:332, :395).
+static __device__ __forceinline__ float rt_drift(const or_rt_table_t *__restrict__ rt, int det, float tdc,
+                                                 float drift) {
+    const int n = rt->nknots[det];
+    if (n <= 0) return drift;
+    if (tdc < rt->tmin[det]) return (float)((double)rt->cellwidth[det] * 0.5);
+    if (tdc > rt->tmax[det]) return 0.f;
+    const double *t = rt->t[det];
+    const double x = (double)tdc;
+    int k = 0;
+    if (n > 1) {
+        if (x >= t[n - 1]) {
+            k = n - 2;
+        } else if (x > t[0]) {
+            int lo = 0, hi = n - 1;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (x > t[mid]) lo = mid;
+                else hi = mid;
+            }
+            k = lo;
+        }
+    }
+    const double dx = x - t[k];
+    const double v = rt->r[det][k] + dx * (rt->b[det][k] + dx * (rt->c[det][k] + dx * rt->d[det][k]));
+    return (float)v;
+}
+
+static __device__ __forceinline__ bool rt_plane(int det) {
+    return (det >= 1 && det <= OR_NCHAM) || (det > OR_NCHAM + OR_NHODO && det < OR_NDET);
+}
+
+template <bool RT>
 __global__ void __launch_bounds__(PK_WARPS * 32)
     pack_kernel(const or_hit_record_t *__restrict__ rec, const int64_t *__restrict__ off, int n_events,
-                const float *__restrict__ wire_pos_f, or_hits_view_t hv) {
+                const float *__restrict__ wire_pos_f, const or_rt_table_t *__restrict__ rt, or_hits_view_t hv) {
     __shared__ int cnt[PK_WARPS][64];
     __shared__ int start[PK_WARPS][64];
     const int w = threadIdx.x >> 5;
@@ -82,19 +124,58 @@ __global__ void __launch_bounds__(PK_WARPS * 32)
             slot[n + k] = pos;
             slot[2 * n + k] = h.tdc;
             slot[3 * n + k] = (float)h.flag;
-            slot[4 * n + k] = h.drift;
+            slot[4 * n + k] = (RT && rt_plane(d)) ? rt_drift(rt, d, h.tdc, h.drift) : h.drift;
         }
         __syncwarp();
     }
 }
 
-cudaError_t launch_pack(const or_hit_record_t *rec, const int64_t *off, int n_events, const float *wire_pos_f,
-                        or_hits_view_t hv, cudaStream_t stream, int sm_count) {
-    if (n_events <= 0) return cudaSuccess;
+// In-place R-T conversion on the reference layout: one warp per event, the
+// chamber and prop-tube planes in turn, lanes over a plane's hits.
+__global__ void __launch_bounds__(PK_WARPS * 32)
+    rt_apply_kernel(const or_rt_table_t *__restrict__ rt, or_hits_view_t hv, int n_events) {
+    const int w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    for (long e = (long)blockIdx.x * PK_WARPS + w; e < n_events; e += (long)gridDim.x * PK_WARPS) {
+        for (int p = 0; p < OR_NCHAM + OR_NPROP; ++p) {
+            const bool cham = p < OR_NCHAM;
+            const int d = cham ? 1 + p : OR_NCHAM + OR_NHODO + 1 + (p - OR_NCHAM);
+            if (rt->nknots[d] <= 0) continue;
+            float *slot;
+            int n;
+            if (cham) {
+                n = min((int)hv.nhits_cham[e * OR_NCHAM + p], OR_MAXHITS_CHAM);
+                slot = hv.hits_cham + e * OR_EVT_CHAM_FLOATS + (long)OR_NHITSPARAM * OR_MAXHITS_CHAM * p;
+            } else {
+                n = min((int)hv.nhits_prop[e * OR_NPROP + p - OR_NCHAM], OR_MAXHITS_PROP);
+                slot = hv.hits_prop + e * OR_EVT_PROP_FLOATS + (long)OR_NHITSPARAM * OR_MAXHITS_PROP * (p - OR_NCHAM);
+            }
+            for (int k = lane; k < n; k += 32) slot[4 * n + k] = rt_drift(rt, d, slot[2 * n + k], slot[4 * n + k]);
+        }
+    }
+}
+
+static long pack_blocks(int n_events, int sm_count) {
     long blocks = (n_events + PK_WARPS - 1) / PK_WARPS;
     const long cap = (long)sm_count * 8;
-    if (blocks > cap) blocks = cap;
-    pack_kernel<<<(unsigned)blocks, PK_WARPS * 32, 0, stream>>>(rec, off, n_events, wire_pos_f, hv);
+    return blocks > cap ? cap : blocks;
+}
+
+cudaError_t launch_pack(const or_hit_record_t *rec, const int64_t *off, int n_events, const float *wire_pos_f,
+                        const or_rt_table_t *rt, or_hits_view_t hv, cudaStream_t stream, int sm_count) {
+    if (n_events <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)pack_blocks(n_events, sm_count);
+    if (rt)
+        pack_kernel<true><<<blocks, PK_WARPS * 32, 0, stream>>>(rec, off, n_events, wire_pos_f, rt, hv);
+    else
+        pack_kernel<false><<<blocks, PK_WARPS * 32, 0, stream>>>(rec, off, n_events, wire_pos_f, nullptr, hv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rt_apply(const or_rt_table_t *rt, or_hits_view_t hv, int n_events, cudaStream_t stream,
+                            int sm_count) {
+    if (n_events <= 0) return cudaSuccess;
+    rt_apply_kernel<<<(unsigned)pack_blocks(n_events, sm_count), PK_WARPS * 32, 0, stream>>>(rt, hv, n_events);
     return cudaGetLastError();
 }
 

@@ -47,6 +47,7 @@ __device__ inline int window_pairs(const HitPlane &h1, int det1, const HitPlane 
     const int lane = lane_id();
     const int n1 = min(h1.n, WP_MAXHITS), n2 = min(h2.n, WP_MAXHITS);
     int c1 = 0, c2 = 0;
+#pragma unroll 1
     for (int b = 0; b < n1; b += 32) {
         const int i = b + lane;
         const bool in = i < n1 && wp_in_window(det1, h1.chan(i), xmin, xmax, P);
@@ -58,6 +59,7 @@ __device__ inline int window_pairs(const HitPlane &h1, int det1, const HitPlane 
         }
         c1 += __popc(m);
     }
+#pragma unroll 1
     for (int b = 0; b < n2; b += 32) {
         const int i = b + lane;
         const bool in = i < n2 && wp_in_window(det2, h2.chan(i), xmin, xmax, P);
@@ -72,6 +74,7 @@ __device__ inline int window_pairs(const HitPlane &h1, int det1, const HitPlane 
     __syncwarp();
     int np = 0;
     const int nn = c1 * c2;
+#pragma unroll 1
     for (int b = 0; b < nn; b += 32) {
         const int c = b + lane;
         bool take = false;
@@ -89,11 +92,13 @@ __device__ inline int window_pairs(const HitPlane &h1, int det1, const HitPlane 
         wp_append(take, v, out, cap, np);
     }
     __syncwarp();
+#pragma unroll 1
     for (int b = 0; b < c1; b += 32) {
         const int a = b + lane;
         const bool take = a < c1 && !W.fl1[a];
         wp_append(take, make_short2(take ? W.idx1[a] : 0, -1), out, cap, np);
     }
+#pragma unroll 1
     for (int b = 0; b < c2; b += 32) {
         const int a = b + lane;
         const bool take = a < c2 && !W.fl2[a];

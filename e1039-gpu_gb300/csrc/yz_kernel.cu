@@ -140,6 +140,7 @@ __device__ __forceinline__ void yz_event_planes(YzEvent &E, const or_hits_view_t
     // u2 u2' v2 v2' u3 u3' v3 v3' (K:910-984)
     const short dl[8] = {DET_U2, DET_UP2, DET_V2, DET_VP2, (short)det_u3(st3), (short)(det_u3(st3) - 1),
                          (short)det_v3(st3), (short)(det_v3(st3) - 1)};
+#pragma unroll 1
     for (int k = 0; k < 8; ++k) {
         E.dl[k] = dl[k];
         E.hc[k] = hits_of(hv, e, dl[k]);
@@ -148,7 +149,9 @@ __device__ __forceinline__ void yz_event_planes(YzEvent &E, const or_hits_view_t
     E.p1y2 = hits_of(hv, e, DET_P1Y2);
     E.p2y1 = hits_of(hv, e, DET_P2Y1);
     E.p2y2 = hits_of(hv, e, DET_P2Y2);
+#pragma unroll 1
     for (int q = 0; q < 3; ++q)
+#pragma unroll 1
         for (int c = 0; c < 2; ++c) E.hod[q][c] = hits_of(hv, e, c_hodoplanesx[q + 1][c]);
 }
 
@@ -163,16 +166,19 @@ __device__ bool yz_build(YzWarp &S, const YzEvent &E, const float *T, const or_p
     bool ok = true;
     int total = 0;
     // windowed hit lists, in plane order (H:480-511)
+#pragma unroll 1
     for (int q = 0; q < 4; ++q) {
         const int a = 2 * q;
         const float za = P.z[E.dl[a]], zb = P.z[E.dl[a + 1]];
         const float sp = P.spacing[E.dl[a]];
         const float xmin = fminf((tx - etx) * za, (tx - etx) * zb) + x0 - ex0 - sp;
         const float xmax = fmaxf((tx + etx) * za, (tx + etx) * zb) + x0 + ex0 + sp;
+#pragma unroll 1
         for (int side = 0; side < 2; ++side) {
             const HitPlane &h = E.hc[a + side];
             const int det = E.dl[a + side];
             int c = 0;
+#pragma unroll 1
             for (int b0 = 0; b0 < h.n; b0 += 32) {
                 const int i = b0 + lane;
                 const bool in = i < h.n && wp_in_window(det, h.chan(i), xmin, xmax, P);
@@ -193,50 +199,13 @@ __device__ bool yz_build(YzWarp &S, const YzEvent &E, const float *T, const or_p
         }
     }
     __syncwarp();
-    // pairs over each projection's two windowed lists (H:513-546)
-    for (int q = 0; q < 4; ++q) {
-        const int a = 2 * q;
-        const int c1 = S.nw[a], c2 = S.nw[a + 1];
-        for (int i = lane; i < c1; i += 32) S.wfl[0][i] = 0;
-        for (int i = lane; i < c2; i += 32) S.wfl[1][i] = 0;
-        __syncwarp();
-        const float spacing = c_spacingplane[c_detsuperid[stid_of[q]][proj_of[q]]];
-        int np = 0;
-        for (int b0 = 0; b0 < c1 * c2; b0 += 32) {
-            const int c = b0 + lane;
-            bool take = false;
-            short2 v = make_short2(0, 0);
-            if (c < c1 * c2) {
-                const int ia = c / c2, ib = c - ia * c2;
-                if (!(fabsf(E.hc[a].pos(S.widx[a][ia]) - E.hc[a + 1].pos(S.widx[a + 1][ib])) > spacing)) {
-                    take = true;
-                    v = make_short2((short)ia, (short)ib);
-                    S.wfl[0][ia] = 1;
-                    S.wfl[1][ib] = 1;
-                }
-            }
-            wp_append(take, v, S.pair[q], YZ_MAXPAIR, np);
-        }
-        __syncwarp();
-        for (int b0 = 0; b0 < c1; b0 += 32) {
-            const int ia = b0 + lane;
-            const bool take = ia < c1 && !S.wfl[0][ia];
-            wp_append(take, make_short2((short)ia, -1), S.pair[q], YZ_MAXPAIR, np);
-        }
-        for (int b0 = 0; b0 < c2; b0 += 32) {
-            const int ib = b0 + lane;
-            const bool take = ib < c2 && !S.wfl[1][ib];
-            wp_append(take, make_short2(-1, (short)ib), S.pair[q], YZ_MAXPAIR, np);
-        }
-        if (np > YZ_MAXPAIR) ok = false;
-        if (lane == 0) S.np[q] = min(np, YZ_MAXPAIR);
-        __syncwarp();
-    }
     // windowed hit records (K:1326-1355 computes these per combination)
     YzHit *dst = (total <= YZ_ARENA_HITS) ? S.arena : garena;
+#pragma unroll 1
     for (int l = 0; l < 8; ++l) {
         const HitPlane &h = E.hc[l];
         const int det = E.dl[l];
+#pragma unroll 1
         for (int i = lane; i < S.nw[l]; i += 32) {
             const int hi = S.widx[l][i];
             YzHit r;
@@ -252,6 +221,52 @@ __device__ bool yz_build(YzWarp &S, const YzEvent &E, const float *T, const or_p
             r.z = P.z[det];
             dst[S.woff[l] + i] = r;
         }
+    }
+    __syncwarp();
+    // pairs over each projection's two windowed lists (H:513-546)
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        const int a = 2 * q;
+        const int c1 = S.nw[a], c2 = S.nw[a + 1];
+#pragma unroll 1
+        for (int i = lane; i < c1; i += 32) S.wfl[0][i] = 0;
+#pragma unroll 1
+        for (int i = lane; i < c2; i += 32) S.wfl[1][i] = 0;
+        __syncwarp();
+        const float spacing = c_spacingplane[c_detsuperid[stid_of[q]][proj_of[q]]];
+        int np = 0;
+#pragma unroll 1
+        for (int b0 = 0; b0 < c1 * c2; b0 += 32) {
+            const int c = b0 + lane;
+            bool take = false;
+            short2 v = make_short2(0, 0);
+            if (c < c1 * c2) {
+                const int ia = c / c2, ib = c - ia * c2;
+                if (!(fabsf(dst[S.woff[a] + ia].pos - dst[S.woff[a + 1] + ib].pos) > spacing)) {
+                    take = true;
+                    v = make_short2((short)ia, (short)ib);
+                    S.wfl[0][ia] = 1;
+                    S.wfl[1][ib] = 1;
+                }
+            }
+            wp_append(take, v, S.pair[q], YZ_MAXPAIR, np);
+        }
+        __syncwarp();
+#pragma unroll 1
+        for (int b0 = 0; b0 < c1; b0 += 32) {
+            const int ia = b0 + lane;
+            const bool take = ia < c1 && !S.wfl[0][ia];
+            wp_append(take, make_short2((short)ia, -1), S.pair[q], YZ_MAXPAIR, np);
+        }
+#pragma unroll 1
+        for (int b0 = 0; b0 < c2; b0 += 32) {
+            const int ib = b0 + lane;
+            const bool take = ib < c2 && !S.wfl[1][ib];
+            wp_append(take, make_short2(-1, (short)ib), S.pair[q], YZ_MAXPAIR, np);
+        }
+        if (np > YZ_MAXPAIR) ok = false;
+        if (lane == 0) S.np[q] = min(np, YZ_MAXPAIR);
+        __syncwarp();
     }
     base = dst;
     if (lane == 0) {
@@ -294,6 +309,7 @@ struct UvHit {
 // end given by `st` (H:714-780), then the singles (H:785-804).
 __device__ __forceinline__ void walk_newhits(int n, UvHit *h, const Stale &st, float x0, float tx, float y0, float ty,
                                              float ex0, float etx, float ey0, float ety, const or_plane_t &P) {
+#pragma unroll 1
     for (int i = 0; i < n;) {
         const int j = i + 1;
         const short di = h[i].det;
@@ -315,6 +331,7 @@ __device__ __forceinline__ void walk_newhits(int n, UvHit *h, const Stale &st, f
         }
         i += 2;
     }
+#pragma unroll 1
     for (int k = 0; k < n; ++k)
         if (!h[k].sign) h[k].sign = single_sign_newhits(x0, tx, y0, ty, h[k].det, h[k].pos, P);
 }
@@ -330,6 +347,7 @@ __device__ __noinline__ void walk_uv(int n, UvHit *h, const Stale &st, float x0,
 // Index of the last station-3 hit when the walk pairs it with the first
 // station-2 hit, else -1.  The walk's pairs depend only on plane ids.
 __device__ __forceinline__ int cross_pair_index(int n3, const UvHit *h, int nuv) {
+#pragma unroll 1
     for (int i = 0; i < n3;) {
         const int j = i + 1;
         if (j >= nuv) return -1;
@@ -396,18 +414,20 @@ __device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gp
     // last inner combination writing each offset m, and its hit
     int lastc[4] = {-1, -1, -1, -1};
     unsigned long long lasth[4] = {0, 0, 0, 0};
+#pragma unroll 1
     for (int b0 = 0; b0 < C2; b0 += 32) {
         const int c = b0 + lane;
         int mine[4] = {-1, -1, -1, -1};
         unsigned long long mh[4] = {0, 0, 0, 0};
         if (c < C2) {
             const S2Writes w = s2_writes(S, base, c % nu2, c / nu2);
+#pragma unroll 1
             for (int k = 0; k < w.n; ++k) {
                 mine[w.off[k]] = c;
                 mh[w.off[k]] = (unsigned long long)w.hit[k];
             }
         }
-#pragma unroll
+#pragma unroll 1
         for (int m = 0; m < 4; ++m) {
             const int l = last_lane(__ballot_sync(0xffffffffu, mine[m] >= 0));
             if (l >= 0) {
@@ -423,13 +443,14 @@ __device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gp
         const YzHit *r = (const YzHit *)lasth[m];
         return Stale{r->det, r->pos, r->drift};
     };
+#pragma unroll 1
     for (int b0 = 0; b0 < G; b0 += 32) {
         const int g = b0 + lane;
         int mk[4] = {-1, -1, -1, -1};
         if (g < G) {
             bool valid;
             const int n3 = s3_count(S, base, g % nu3, g / nu3, valid);
-#pragma unroll
+#pragma unroll 1
             for (int k = 0; k < 4; ++k) {
                 const int mm = k + 4 - n3;
                 if (valid && mm >= 0 && mm < 4 && lastc[mm] >= 0) mk[k] = mm;
@@ -437,7 +458,7 @@ __device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gp
         }
         const bool ustart = units && g < G && (g % gper) == 0;
         Stale ent[4];
-#pragma unroll
+#pragma unroll 1
         for (int k = 0; k < 4; ++k) {
             const unsigned wm = __ballot_sync(0xffffffffu, mk[k] >= 0);
             const int src = last_lane(wm & lanemask_lt());
@@ -473,7 +494,7 @@ __device__ __forceinline__ int yz_gather(const YzWarp &S, const YzHit *base, int
     const short2 pq[4] = {S.pair[2][iuv3 % nu3], S.pair[3][iuv3 / nu3], S.pair[0][iuv2 % nu2], S.pair[1][iuv2 / nu2]};
     const int lists[8] = {4, 5, 6, 7, 0, 1, 2, 3};
     int nuv = 0;
-#pragma unroll
+#pragma unroll 1
     for (int a = 0; a < 8; ++a) {
         if (a == 4) n3 = nuv;  // station-3 hits come first
         const short2 p = pq[a >> 1];
@@ -520,11 +541,13 @@ __device__ __noinline__ bool yz_gates(const YzEvent &E, const or_plane_t &P, flo
 __device__ __noinline__ float yz_chi2(const YzWarp &S, const UvHit *h, int nuv, int nhx, const or_plane_t &P, float x0,
                                       float y0, float tx, float ty, float *resid) {
     float chi2 = 0.f;
+#pragma unroll 1
     for (int m = 0; m < nhx; ++m) {
         resid[m] = residual_line(S.xp1x[m], S.xp1y[m], S.xp1z[m], S.xdpx[m], S.xdpy[m], S.xdpz[m], S.xdd[m], S.xhs[m],
                                  x0, y0, tx, ty);
         chi2 += resid[m] * resid[m] / S.xres[m] / S.xres[m];
     }
+#pragma unroll 1
     for (int k = 0; k < nuv; ++k) {
         const short d = h[k].det;
         const float r = residual_line(x_bep(d, h[k].el, P), y_bep(d, h[k].el, P), z_bep(d, h[k].el, P), P.deltapx[d],
@@ -600,6 +623,7 @@ __device__ __noinline__ void yz_phase2(YzWarp &S, const YzEvent &E, const YzHit 
     float chi2 = 0.f;
     float resid[12];
     if (valid && !is_first) {
+#pragma unroll 1
         for (int k = 0; k < n3 && k < 4; ++k) h[k].sign = sig[k];
         if (n3 > 0) {
             if (xs >= 0) h[n3 - 1].sign = xprev;
@@ -625,6 +649,7 @@ __device__ __noinline__ void yz_phase2(YzWarp &S, const YzEvent &E, const YzHit 
         const bool cont = (gl == cs.g);
         if (fnew >= 0) {
             cs.hasf = true;
+#pragma unroll 1
             for (int k = 0; k < 4; ++k) cs.sig[k] = ns[k];
         } else if (!cont) {
             cs.hasf = false;
@@ -655,6 +680,7 @@ __device__ __noinline__ void yz_phase2(YzWarp &S, const YzEvent &E, const YzHit 
                 S.b.y0 = y0;
                 S.b.ety = ety;
                 S.b.ey0 = ey0;
+#pragma unroll 1
                 for (int n = 0; n < nuv; ++n) {
                     S.b.det[n] = h[n].det;
                     S.b.el[n] = h[n].el;
@@ -663,6 +689,7 @@ __device__ __noinline__ void yz_phase2(YzWarp &S, const YzEvent &E, const YzHit 
                     S.b.sign[n] = h[n].sign;
                     S.b.tdc[n] = h[n].tdc;
                 }
+#pragma unroll 1
                 for (int n = 0; n < nhx + nuv; ++n) S.b.res[n] = resid[n];
             }
         }
@@ -754,8 +781,6 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
     const int nu2 = S.np[0], nu3 = S.np[2];
     const int C2 = S.np[0] * S.np[1];
     const int c0 = (int)c0l, c1 = (int)c1l;  // at most 100^4 combinations
-    const float x0 = S.x0, tx = S.tx, ex0 = S.ex0, etx = S.etx;
-    const int nhx = S.nhx;
     Phase2Carry cs;
     int qh = 0, qn = 0;  // survivors Q[qh..qn) wait for the full evaluation
     const int nv2 = S.np[1];
@@ -1023,8 +1048,10 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
         long row = 0;  // scorer row of the next tracklet (slots in order, tracklets in slot order)
         if (prune.keep) {
             row = prune.row_off[e];
+#pragma unroll 1
             for (int s = 0; s < slot0; ++s) row += min((int)tv.ntracks[e * OR_NSLOTS + s], OR_SLOTCAP);
         }
+#pragma unroll 1
         for (int slot = slot0; slot < slot0 + YZ_PLAN_CHUNK; ++slot) {
             const int ntr = min((int)tv.ntracks[e * OR_NSLOTS + slot], OR_SLOTCAP);
             const long slot_row = row;
@@ -1034,7 +1061,9 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
             YzEvent E;
             yz_event_planes(E, hv, e, st3);
             Stale st[4];
+#pragma unroll 1
             for (int k = 0; k < 4; ++k) st[k] = Stale{DET_SENTINEL, 0.f, 0.f};
+#pragma unroll 1
             for (int it = 0; it < ntr; ++it) {
                 float *T = trk_rec(tv, e, slot, it);
                 const YzHit *base;
@@ -1080,6 +1109,7 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
                     u0 = __shfl_sync(0xffffffffu, u0, 0);
                     if (hid >= sc.cap_heavy || (long)u0 + nunits > sc.cap_units) {
                         // no room on the queue: evaluate here; void the reserved units
+#pragma unroll 1
                         for (int u = lane; u < nunits; u += 32)
                             if (u0 + u < sc.cap_units) sc.units[u0 + u].heavy = -1;
                         if (lane == 0 && hid < sc.cap_heavy) sc.heavy[hid].nunits = 0;
@@ -1140,6 +1170,7 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
         yz_build(S, E, T, P, st3, base, garena);
         yz_xhits(S, T, P);
         Stale st[4];
+#pragma unroll 1
         for (int k = 0; k < 4; ++k) st[k] = un.entry[k];
         const long C2 = (long)S.np[0] * S.np[1];
         const unsigned long long bk = yz_range(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, Q, sc.qcap);
@@ -1150,6 +1181,7 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
         } else {
             const unsigned *src = reinterpret_cast<const unsigned *>(&S.b);
             unsigned *d = reinterpret_cast<unsigned *>(dst);
+#pragma unroll 1
             for (int i = lane; i < (int)(sizeof(YzBest) / 4); i += 32) d[i] = src[i];
         }
         __syncwarp();
@@ -1160,11 +1192,13 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
 __global__ void __launch_bounds__(128) yz_apply_kernel(or_tracks_view_t tv, YzScratch sc) {
     const int lane = threadIdx.x & 31;
     const int nheavy = min((int)sc.counters[1], sc.cap_heavy);
+#pragma unroll 1
     for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < nheavy; h += (gridDim.x * blockDim.x) >> 5) {
         const YzHeavy hv2 = sc.heavy[h];
         if (hv2.nunits <= 0 || (long)hv2.unit0 + hv2.nunits > sc.cap_units) continue;
         unsigned long long best = ~0ull;
         int bu = -1;
+#pragma unroll 1
         for (int u = lane; u < hv2.nunits; u += 32) {
             const unsigned long long k = sc.best[hv2.unit0 + u].key;
             if (k < best) {
@@ -1172,6 +1206,7 @@ __global__ void __launch_bounds__(128) yz_apply_kernel(or_tracks_view_t tv, YzSc
                 bu = hv2.unit0 + u;
             }
         }
+#pragma unroll 1
         for (int o = 16; o > 0; o >>= 1) {
             const unsigned long long ok = __shfl_xor_sync(0xffffffffu, best, o);
             const int ou = __shfl_xor_sync(0xffffffffu, bu, o);

@@ -7,3 +7,4 @@ import os
 
 DATA_DIR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "data")
 GEOMETRY_E906 = os.path.join(DATA_DIR, "basic_geometry_e906.txt")
+CALIBRATION_E906 = os.path.join(DATA_DIR, "calibration_e906.txt")

@@ -22,7 +22,8 @@ EXPORTS = ("or_version", "or_last_error", "or_status_string", "or_geometry_load"
            "or_tracklet_labels", "or_track_agreement", "or_mlp_grad_blocks", "or_mlp_forward", "or_mlp_gradient",
            "or_mlp_adam", "or_prop_matching", "or_global_clean", "or_run_selection", "or_set_launch",
            "or_get_launch", "or_vertexing", "or_dimuons", "or_fill_histograms", "or_hist_table_init",
-           "or_run_physics", "or_output_rows")
+           "or_run_physics", "or_output_rows", "or_rt_load", "or_rt_set_plane", "or_rt_table_bytes",
+           "or_pack_hits_rt", "or_rt_apply")
 
 # tunable kernels (or_kernel_id_t)
 KERNELS = {"event_reduce": 0, "xz": 1, "yz": 2, "back_clean": 3, "global": 4, "select": 5, "features": 6}
@@ -103,6 +104,12 @@ def lib():
     lb.or_run_physics.argtypes = [vp, L.OrTracksView, L.OrDimuonsView, vp, vp, vp, i32, vp]
     lb.or_output_rows.argtypes = [vp, L.OrHitsView, L.OrTracksView, L.OrDimuonsView, vp, vp, vp, f32, L.OrOutputView,
                                   i32, vp]
+    lb.or_rt_load.argtypes = [C.c_char_p, P(L.OrPlane), P(L.OrRtTable), P(C.c_int)]
+    lb.or_rt_set_plane.argtypes = [P(L.OrRtTable), i32, i32, vp, vp, f32, f32, f32]
+    lb.or_rt_table_bytes.argtypes = []
+    lb.or_rt_table_bytes.restype = C.c_size_t
+    lb.or_pack_hits_rt.argtypes = [vp, vp, vp, i32, vp, vp, L.OrHitsView, vp]
+    lb.or_rt_apply.argtypes = [vp, vp, L.OrHitsView, i32, vp]
     for name in EXPORTS:
         getattr(lb, name)
     _lib = lb
@@ -121,3 +128,12 @@ def geometry_load(path):
     wp = np.zeros(L.NDET * L.WIREPOS_STRIDE, np.float64)
     check(lib().or_geometry_load(str(path).encode(), C.byref(p), wp.ctypes.data), "or_geometry_load")
     return p, wp.reshape(L.NDET, L.WIREPOS_STRIDE)
+
+
+def rt_load(path, plane):
+    """Parse an R-T calibration file with the library's loader -> (OrRtTable,
+    number of planes with a profile).  `plane` supplies the cell widths."""
+    rt = L.OrRtTable()
+    n = C.c_int(0)
+    check(lib().or_rt_load(str(path).encode(), C.byref(plane), C.byref(rt), C.byref(n)), "or_rt_load")
+    return rt, n.value

@@ -82,6 +82,28 @@ class OrPlane(C.Structure):
         return p
 
 
+RT_MAXKNOTS = 500
+
+
+class OrRtTable(C.Structure):
+    """or_rt_table_t: per plane the clamped cubic R-T spline (knots t, values
+    r, piece coefficients b, c, d), the time window and the cell width."""
+    _fields_ = [
+        ("nknots", C.c_int32 * NDET), ("tmin", C.c_float * NDET), ("tmax", C.c_float * NDET),
+        ("cellwidth", C.c_float * NDET),
+        ("t", (C.c_double * RT_MAXKNOTS) * NDET), ("r", (C.c_double * RT_MAXKNOTS) * NDET),
+        ("b", (C.c_double * RT_MAXKNOTS) * NDET), ("c", (C.c_double * RT_MAXKNOTS) * NDET),
+        ("d", (C.c_double * RT_MAXKNOTS) * NDET),
+    ]
+
+    def arr(self, name):
+        """Field as a numpy array (a copy)."""
+        return np.ctypeslib.as_array(getattr(self, name)).copy()
+
+    def to_bytes(self):
+        return bytes(C.string_at(C.addressof(self), C.sizeof(self)))
+
+
 class OrHitsView(C.Structure):
     _fields_ = [
         ("nhits_cham", C.c_void_p), ("hits_cham", C.c_void_p),

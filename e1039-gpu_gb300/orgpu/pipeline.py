@@ -30,6 +30,14 @@ def _torch():
     return torch
 
 
+def rt_to_device(rt, device=0):
+    """Copy an OrRtTable (host, from _lib.rt_load) to a device uint8 tensor,
+    the `rt_dev` argument of Reconstruction.pack_rt / rt_apply."""
+    torch = _torch()
+    raw = np.frombuffer(rt.to_bytes(), np.uint8)
+    return torch.from_numpy(raw.copy()).to(torch.device("cuda", device))
+
+
 class DeviceBatch:
     """Device buffers of n events in the reference layout."""
 
@@ -281,6 +289,18 @@ class Reconstruction:
         _lib.check(self.lib.or_pack_hits(self.ctx, d_records.data_ptr(), d_offsets.data_ptr(), b.n,
                                           d_wire_pos_f.data_ptr(), b.hits_view(), self._stream(stream)),
                    "or_pack_hits")
+
+    def pack_rt(self, b, d_records, d_offsets, d_wire_pos_f, d_rt, stream=None):
+        """Device packer with the drift distance from the R-T calibration
+        (d_rt: device uint8 tensor holding an OrRtTable, see rt_to_device)."""
+        _lib.check(self.lib.or_pack_hits_rt(self.ctx, d_records.data_ptr(), d_offsets.data_ptr(), b.n,
+                                             d_wire_pos_f.data_ptr(), d_rt.data_ptr(), b.hits_view(),
+                                             self._stream(stream)), "or_pack_hits_rt")
+
+    def rt_apply(self, b, d_rt, stream=None):
+        """R-T conversion in place on b's packed hits (drift from tdc)."""
+        _lib.check(self.lib.or_rt_apply(self.ctx, d_rt.data_ptr(), b.hits_view(), b.n, self._stream(stream)),
+                   "or_rt_apply")
 
     def collect(self, b, d_out, d_count, stid=6.0, stream=None):
         """Gather tracks with stationID == stid into d_out (float32 rows of

@@ -176,6 +176,30 @@ size_t or_tracks_view_bytes(int n_events);
 int or_pack_hits(or_ctx_t *ctx, const or_hit_record_t *records, const int64_t *rec_offsets, int n_events,
                  const float *wire_pos_f, or_hits_view_t hits, void *stream);
 
+/* R-T calibration (online_reconstruction.cu:220-242): parse the calibration
+ * file and build every listed chamber / prop-tube plane's clamped cubic
+ * spline into *rt (host memory, or_rt_table_bytes() bytes); cellwidth comes
+ * from `plane`.  *nplanes_out (may be NULL) receives the number of planes
+ * that got a profile.  Host only. */
+int or_rt_load(const char *path, const or_plane_t *plane, or_rt_table_t *rt, int *nplanes_out);
+/* Build one plane's profile from n points (t strictly increasing, n <=
+ * OR_RT_MAXKNOTS); det must be a chamber (1..30) or prop-tube (47..54) plane. */
+int or_rt_set_plane(or_rt_table_t *rt, int det, int n, const double *t, const double *r, float tmin, float tmax,
+                    float cellwidth);
+size_t or_rt_table_bytes(void);
+
+/* or_pack_hits with the drift distance taken from the R-T calibration
+ * instead of the record (online_reconstruction.cu:387-396): on a chamber or
+ * prop-tube plane with a profile, tdc < tmin gives cellwidth/2, tdc > tmax
+ * gives 0, otherwise (float)R(tdc).  rt_dev: an or_rt_table_t in device
+ * memory.  Hodoscope hits and planes without a profile keep the record's. */
+int or_pack_hits_rt(or_ctx_t *ctx, const or_hit_record_t *records, const int64_t *rec_offsets, int n_events,
+                    const float *wire_pos_f, const or_rt_table_t *rt_dev, or_hits_view_t hits, void *stream);
+/* The same conversion in place on hits already in the reference layout
+ * (packed by a reference-style host, online_reconstruction.cu:406-417):
+ * every chamber and prop-tube hit's drift field from its tdc field. */
+int or_rt_apply(or_ctx_t *ctx, const or_rt_table_t *rt_dev, or_hits_view_t hits, int n_events, void *stream);
+
 /* Gather the tracks whose stationID equals `stid` (6 = global tracks) into
  * `out`, OR_COLLECT_STRIDE floats per row: [event, slot*16 + position,
  * 148-float record].  *d_count (device, uint64) receives the number of

@@ -259,6 +259,26 @@ typedef struct or_hit_record {
     int32_t flag; /* the packed float flag value: 2 = in time, 1 = out of time */
 } or_hit_record_t;
 
+/* R-T (drift time -> drift distance) calibration: per plane a cubic spline
+ * through the calibration points (T_k, R_k), clamped with zero slope at both
+ * ends (the reference builds ROOT TSpline3(name, T, R, n, "b1e1") per plane,
+ * online_reconstruction.cu:220-242), plus the plane's time window.  Spline
+ * piece k covers (t[k], t[k+1]]:  R(x) = r[k] + dx*(b[k] + dx*(c[k] + dx*d[k])),
+ * dx = x - t[k], all in double.  nknots[d] = 0: plane d has no profile and
+ * its hits keep the record's drift distance. */
+#define OR_RT_MAXKNOTS 500 /* the reference's T[500], R[500] (online_reconstruction.cu:226) */
+typedef struct or_rt_table {
+    int32_t nknots[OR_NDET];
+    float tmin[OR_NDET];      /* tdc < tmin: drift = cellwidth/2 (online_reconstruction.cu:390-391) */
+    float tmax[OR_NDET];      /* tdc > tmax: drift = 0 (:392-393) */
+    float cellwidth[OR_NDET]; /* gPlane::cellwidth */
+    double t[OR_NDET][OR_RT_MAXKNOTS];
+    double r[OR_NDET][OR_RT_MAXKNOTS];
+    double b[OR_NDET][OR_RT_MAXKNOTS];
+    double c[OR_NDET][OR_RT_MAXKNOTS];
+    double d[OR_NDET][OR_RT_MAXKNOTS];
+} or_rt_table_t;
+
 #ifdef __cplusplus
 }
 #endif
