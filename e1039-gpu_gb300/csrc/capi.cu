@@ -161,7 +161,10 @@ int or_create(int device, or_ctx_t **out) {
     // excess in the planning pass, correct but without the queue's balance
     c->yz_cap_units = 1 << 22;
     c->yz_cap_heavy = 1 << 21;
-    c->yz_garena_warps = c->sm_count * 16;
+#ifndef OR_YZ_WARPS_SM
+#define OR_YZ_WARPS_SM 16
+#endif
+    c->yz_garena_warps = c->sm_count * OR_YZ_WARPS_SM;
     if ((e = cudaMalloc(&c->yz_scratch,
                         orgpu::yz_scratch_bytes_ctx(c->yz_cap_units, c->yz_cap_heavy, c->yz_garena_warps))) !=
         cudaSuccess) {

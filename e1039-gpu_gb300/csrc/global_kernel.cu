@@ -25,6 +25,8 @@ constexpr int GL_NST = 7;  // scratch entries tracked for stale reads: 0..6
 
 
 struct GlWarp {
+    HitPlane hc[6];  // station-1 plane views of the current event, the same for every lane
+    short dl[6];
     short2 pairs[3][GL_PAIRCAP];  // x1, u1, v1
     WindowScratch W;
     // station-2/3 hits of the current track
@@ -158,7 +160,13 @@ __global__ void __launch_bounds__(W * 32)
     const int lane = threadIdx.x & 31;
     GlWarp &S = warps[w];
     // station-1 planes x x' u u' v v' (K:1880-1923, E1039 chamber ids)
-    const short dl[6] = {4, 3, 2, 1, 6, 5};
+    if (lane == 0) {
+        const short dl0[6] = {4, 3, 2, 1, 6, 5};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) S.dl[k] = dl0[k];
+    }
+    __syncwarp();
+    const short *dl = S.dl;
 
     const unsigned long long nunits = (unsigned long long)n_events * (OR_NSLOTS / GL_CHUNK);
     for (;;) {
@@ -169,9 +177,13 @@ __global__ void __launch_bounds__(W * 32)
         const long e = (long)(u / (OR_NSLOTS / GL_CHUNK));
         const int slot0 = (int)(u % (OR_NSLOTS / GL_CHUNK)) * GL_CHUNK;
         if (toomany[e]) continue;
-        HitPlane hc[6];
+        HitPlane *hc = S.hc;
+        __syncwarp();  // every lane is done with the previous event's views
+        if (lane == 0) {
 #pragma unroll 1
-        for (int k = 0; k < 6; ++k) hc[k] = hits_of(hv, e, dl[k]);
+            for (int k = 0; k < 6; ++k) hc[k] = hits_of(hv, e, dl[k]);
+        }
+        __syncwarp();
 #pragma unroll 1
         for (int slot = slot0; slot < slot0 + GL_CHUNK; ++slot) {
             const int ntr = min((int)tv.ntracks[e * OR_NSLOTS + slot], OR_SLOTCAP);

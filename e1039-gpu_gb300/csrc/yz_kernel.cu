@@ -39,7 +39,13 @@ namespace orgpu {
 
 constexpr int YZ_MAXWIN = 100;          // windowed hits per plane (the reference's hitidx arrays)
 constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's hitpairs arrays)
-constexpr int YZ_ARENA_HITS = 192;      // windowed hits kept in shared memory per warp
+#ifndef OR_YZ_ARENA
+#define OR_YZ_ARENA 64
+#endif
+#ifndef OR_YZ_WARPS_SM
+#define OR_YZ_WARPS_SM 16
+#endif
+constexpr int YZ_ARENA_HITS = OR_YZ_ARENA;      // windowed hits kept in shared memory per warp
 #ifndef OR_YZ_LIGHT
 #define OR_YZ_LIGHT 256
 #endif
@@ -116,7 +122,15 @@ struct PassEntryStore {
     int stdet;
 };
 
+struct YzEvent {
+    HitPlane hc[8];
+    HitPlane p1y1, p1y2, p2y1, p2y2;
+    HitPlane hod[3][2];
+    short dl[8];
+};
+
 struct YzWarp {
+    YzEvent ev;  // the event's plane views, the same for every lane
     YzHit arena[YZ_ARENA_HITS];
     short2 pair[4][YZ_MAXPAIR];  // windowed indices (or -1) in sides 0, 1 of list q
     short widx[8][YZ_MAXWIN];    // plane hit index of each windowed hit
@@ -127,13 +141,6 @@ struct YzWarp {
     float xdd[4], xres[4], xp1x[4], xp1y[4], xp1z[4], xdpx[4], xdpy[4], xdpz[4];
     short xhs[4];
     YzBest b;
-};
-
-struct YzEvent {
-    HitPlane hc[8];
-    HitPlane p1y1, p1y2, p2y1, p2y2;
-    HitPlane hod[3][2];
-    short dl[8];
 };
 
 __device__ __forceinline__ void yz_event_planes(YzEvent &E, const or_hits_view_t &hv, long e, int st3) {
@@ -1017,7 +1024,7 @@ __device__ __forceinline__ YzHit *yz_garena(const YzScratch &sc, int gwarp) {
 }
 
 template <int W>
-__global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
+__global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_SM / W : 1))
     yz_plan_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
                    const uint8_t *__restrict__ toomany, int n_events, YzScratch sc, uint32_t *__restrict__ errw,
                    YzPrune prune) {
@@ -1058,8 +1065,10 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
             row += ntr;
             if (ntr == 0) continue;
             const int st3 = 3 + (slot & 1);  // K:884
-            YzEvent E;
-            yz_event_planes(E, hv, e, st3);
+            YzEvent &E = S.ev;
+            __syncwarp();  // every lane is done with the previous slot's views
+            if (lane == 0) yz_event_planes(E, hv, e, st3);
+            __syncwarp();
             Stale st[4];
 #pragma unroll 1
             for (int k = 0; k < 4; ++k) st[k] = Stale{DET_SENTINEL, 0.f, 0.f};
@@ -1141,7 +1150,7 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
 
 // persistent warps drain the unit queue
 template <int W>
-__global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
+__global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_SM / W : 1))
     yz_work_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv, YzScratch sc) {
     extern __shared__ __align__(16) unsigned char yz_smem[];
     or_plane_t &P = *reinterpret_cast<or_plane_t *>(yz_smem);
@@ -1164,8 +1173,10 @@ __global__ void __launch_bounds__(W * 32, (16 / W > 0 ? 16 / W : 1))
         const YzHeavy hv2 = sc.heavy[un.heavy];
         const float *T = trk_rec(tv, hv2.e, hv2.slot, hv2.k);
         const int st3 = 3 + (hv2.slot & 1);
-        YzEvent E;
-        yz_event_planes(E, hv, hv2.e, st3);
+        YzEvent &E = S.ev;
+        __syncwarp();  // every lane is done with the previous unit's views
+        if (lane == 0) yz_event_planes(E, hv, hv2.e, st3);
+        __syncwarp();
         const YzHit *base;
         yz_build(S, E, T, P, st3, base, garena);
         yz_xhits(S, T, P);
