@@ -47,7 +47,7 @@ constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's
 #endif
 constexpr int YZ_ARENA_HITS = OR_YZ_ARENA;      // windowed hits kept in shared memory per warp
 #ifndef OR_YZ_LIGHT
-#define OR_YZ_LIGHT 256
+#define OR_YZ_LIGHT 128
 #endif
 constexpr long YZ_LIGHT = OR_YZ_LIGHT;         // combinations a planning warp evaluates itself per tracklet
 constexpr long YZ_CHUNK_INLINE = OR_YZ_LIGHT;  // ... and per planning unit
@@ -131,6 +131,7 @@ struct YzEvent {
 
 struct YzWarp {
     YzEvent ev;  // the event's plane views, the same for every lane
+    Stale st[4];  // scratch entries 4..7 as the next combination finds them, the same for every lane
     YzHit arena[YZ_ARENA_HITS];
     short2 pair[4][YZ_MAXPAIR];  // windowed indices (or -1) in sides 0, 1 of list q
     short widx[8][YZ_MAXWIN];    // plane hit index of each windowed hit
@@ -484,8 +485,10 @@ __device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gp
             for (int k = 0; k < 4; ++k) u.entry[k] = ent[k];
         }
     }
+    __syncwarp();  // every lane has read the entry states
 #pragma unroll
     for (int k = 0; k < 4; ++k) st[k] = resolve(k, carry[k]);
+    __syncwarp();
 }
 
 // A combination that passed the first y cut, queued for the full evaluation:
@@ -940,6 +943,7 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
                     const int lw = last_lane(m);
                     if (lw >= 0) {
                         const YzHit &r = base[__shfl_sync(0xffffffffu, ok, lw)];
+                        __syncwarp();  // every lane has read entry k
                         st[k] = Stale{r.det, r.pos, r.drift};
                     }
                 }
@@ -1069,9 +1073,11 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_
             __syncwarp();  // every lane is done with the previous slot's views
             if (lane == 0) yz_event_planes(E, hv, e, st3);
             __syncwarp();
-            Stale st[4];
+            Stale *st = S.st;
+            __syncwarp();  // every lane is done with the previous slot's states
 #pragma unroll 1
             for (int k = 0; k < 4; ++k) st[k] = Stale{DET_SENTINEL, 0.f, 0.f};
+            __syncwarp();
 #pragma unroll 1
             for (int it = 0; it < ntr; ++it) {
                 float *T = trk_rec(tv, e, slot, it);
@@ -1180,9 +1186,11 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_
         const YzHit *base;
         yz_build(S, E, T, P, st3, base, garena);
         yz_xhits(S, T, P);
-        Stale st[4];
+        Stale *st = S.st;
+        __syncwarp();  // every lane is done with the previous unit's states
 #pragma unroll 1
         for (int k = 0; k < 4; ++k) st[k] = un.entry[k];
+        __syncwarp();
         const long C2 = (long)S.np[0] * S.np[1];
         const unsigned long long bk = yz_range(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, Q, sc.qcap);
         __syncwarp();
