@@ -83,7 +83,10 @@ static __device__ void sagitta_st1(float x0, float tx, float y0, float ty, int d
 // counter: slots are independent in the reference (one thread each, state
 // kept per thread), and the cost per event is very uneven, so warps that
 // finish early keep taking units instead of idling behind a heavy event.
-constexpr int GL_CHUNK = 8;
+#ifndef OR_GL_CHUNK
+#define OR_GL_CHUNK 4
+#endif
+constexpr int GL_CHUNK = OR_GL_CHUNK;
 
 // The survivor work of the (u1,v1) loop -- left/right walk and chi2 --
 // kept out of line (one copy each) so that the loop's instructions stay

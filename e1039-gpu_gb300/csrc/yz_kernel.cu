@@ -51,7 +51,10 @@ constexpr int YZ_ARENA_HITS = OR_YZ_ARENA;      // windowed hits kept in shared 
 #endif
 constexpr long YZ_LIGHT = OR_YZ_LIGHT;         // combinations a planning warp evaluates itself per tracklet
 constexpr long YZ_CHUNK_INLINE = OR_YZ_LIGHT;  // ... and per planning unit
-constexpr int YZ_PLAN_CHUNK = 8;        // slots per planning unit
+#ifndef OR_YZ_PLAN_CHUNK
+#define OR_YZ_PLAN_CHUNK 8
+#endif
+constexpr int YZ_PLAN_CHUNK = OR_YZ_PLAN_CHUNK;  // slots per planning unit
 #ifndef OR_YZ_UNIT
 #define OR_YZ_UNIT 8192
 #endif
