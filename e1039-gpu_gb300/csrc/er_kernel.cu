@@ -4,13 +4,14 @@
 // Replaces gkernel_eR<<<N,8>>> (OnlineReconstruction/reconstruction_kernels
 // .cuh:8-172) and event_reduction() (reconstruction_helper.cuh:168-361).
 //
-// Layout on the GPU: one warp per event.  An elected lane stages the
+// Layout on the GPU: one warp per event.  The warp stages the
 // occupied part of each plane slot (5*n floats, rounded up to 16 bytes --
 // slot capacities are multiples of 16 bytes, so the round-up stays inside the
 // slot) into shared memory with 1-D TMA bulk copies completing on an
-// mbarrier; planes are taken in batches that fit the warp's buffer.  Each
-// lane then runs the reference's per-plane state machine on one plane out of
-// shared memory, and the warp writes the survivors back coalesced, with the
+// mbarrier; planes are taken in batches that fit the warp's buffer (a warp
+// prefix sum over the planes' sizes), each lane issuing the copies of its
+// planes.  Each lane then runs the reference's per-plane state machine on one
+// plane out of shared memory and writes that plane's survivors back, with the
 // new SoA stride, into the same slot.  Bytes beyond the survivors are left as
 // they were, as the reference leaves them.
 #include "or_device.cuh"
@@ -179,28 +180,46 @@ __global__ void __launch_bounds__(W * 32) er_kernel(or_hits_view_t hv, uint8_t *
         while (p0 < ER_NPLANES) {
             // batch [p0, p1): planes whose staged images fit the buffer
             int p1 = p0, off = 0, hits = 0;
-            while (p1 < ER_NPLANES) {
-                const int sz = (5 * S.n[p1] + 3) & ~3;
-                if (off + sz > ER_BUF_FLOATS) break;
-                if (lane == 0) {
-                    S.soff[p1] = off;
-                    S.hoff[p1] = hits;
+            // 32 planes at a time: prefix sums of the staged sizes and hit
+            // counts over the lanes; the planes that fit form a prefix
+            for (;;) {
+                const int p = p1 + lane;
+                const int n_l = p < ER_NPLANES ? S.n[p] : 0;
+                const int sz_l = p < ER_NPLANES ? ((5 * n_l + 3) & ~3) : ER_BUF_FLOATS + 1;
+                int csz = sz_l, cn = n_l;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const int a = __shfl_up_sync(0xffffffffu, csz, d);
+                    const int b = __shfl_up_sync(0xffffffffu, cn, d);
+                    if (lane >= d) {
+                        csz += a;
+                        cn += b;
+                    }
                 }
-                off += sz;
-                hits += S.n[p1];
-                ++p1;
+                const bool fit = off + csz <= ER_BUF_FLOATS;
+                const int nfit = __popc(__ballot_sync(0xffffffffu, fit));
+                if (fit) {
+                    S.soff[p] = off + csz - sz_l;
+                    S.hoff[p] = hits + cn - n_l;
+                }
+                if (nfit == 0) break;
+                off += __shfl_sync(0xffffffffu, csz, nfit - 1);
+                hits += __shfl_sync(0xffffffffu, cn, nfit - 1);
+                p1 += nfit;
+                if (nfit < 32 || p1 >= ER_NPLANES) break;
             }
             __syncwarp();
             if (off > 0) {
-                if (lane == 0) {
-                    fence_proxy_async_smem();  // buffer was read by the generic proxy
-                    mbar_arrive_expect_tx(&S.bar, (uint32_t)off * 4u);
-                    for (int p = p0; p < p1; ++p) {
-                        const int sz = (5 * S.n[p] + 3) & ~3;
-                        if (sz == 0) continue;
-                        const PlaneRef r = er_plane(hv, e, c_er_det[p]);
-                        tma_load_1d(S.buf + S.soff[p], r.slot, (uint32_t)sz * 4u, &S.bar);
-                    }
+                // lane 0 announces the batch's bytes before any copy is
+                // issued; then every lane issues the copies of its planes
+                if (lane == 0) mbar_arrive_expect_tx(&S.bar, (uint32_t)off * 4u);
+                __syncwarp();
+                fence_proxy_async_smem();  // buffer was read by the generic proxy
+                for (int p = p0 + lane; p < p1; p += 32) {
+                    const int sz = (5 * S.n[p] + 3) & ~3;
+                    if (sz == 0) continue;
+                    const PlaneRef r = er_plane(hv, e, c_er_det[p]);
+                    tma_load_1d(S.buf + S.soff[p], r.slot, (uint32_t)sz * 4u, &S.bar);
                 }
                 if (!mbar_wait_bounded(&S.bar, phase, ER_WAIT_LIMIT)) {
                     if (lane == 0) atomicOr(errw, ERRW_TMA_TIMEOUT);
@@ -213,17 +232,15 @@ __global__ void __launch_bounds__(W * 32) er_kernel(or_hits_view_t hv, uint8_t *
                                             S.surv + S.hoff[p], S.seen[lane]);
             }
             __syncwarp();
-            for (int p = p0; p < p1; ++p) {
+            // each lane writes back the planes it reduced
+            for (int p = p0 + lane; p < p1; p += 32) {
                 const int n = S.n[p], nk = S.kept[p];
                 const PlaneRef r = er_plane(hv, e, c_er_det[p]);
                 const float *src = S.buf + S.soff[p];
                 const uint16_t *sv = S.surv + S.hoff[p];
-                for (int i = lane; i < 5 * nk; i += 32) {
-                    const int f = i / nk;
-                    const int k = i - f * nk;
-                    r.slot[i] = src[f * n + sv[k]];
-                }
-                if (lane == 0) *r.count = (uint32_t)nk;
+                for (int f = 0; f < 5; ++f)
+                    for (int k = 0; k < nk; ++k) r.slot[f * nk + k] = src[f * n + sv[k]];
+                *r.count = (uint32_t)nk;
             }
             __syncwarp();
             p0 = p1;
