@@ -425,20 +425,20 @@ __device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gp
     // last inner combination writing each offset m, and its hit
     int lastc[4] = {-1, -1, -1, -1};
     unsigned long long lasth[4] = {0, 0, 0, 0};
-#pragma unroll 1
+#pragma unroll
     for (int b0 = 0; b0 < C2; b0 += 32) {
         const int c = b0 + lane;
         int mine[4] = {-1, -1, -1, -1};
         unsigned long long mh[4] = {0, 0, 0, 0};
         if (c < C2) {
             const S2Writes w = s2_writes(S, base, c % nu2, c / nu2);
-#pragma unroll 1
+#pragma unroll
             for (int k = 0; k < w.n; ++k) {
                 mine[w.off[k]] = c;
                 mh[w.off[k]] = (unsigned long long)w.hit[k];
             }
         }
-#pragma unroll 1
+#pragma unroll
         for (int m = 0; m < 4; ++m) {
             const int l = last_lane(__ballot_sync(0xffffffffu, mine[m] >= 0));
             if (l >= 0) {
@@ -454,14 +454,14 @@ __device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gp
         const YzHit *r = (const YzHit *)lasth[m];
         return Stale{r->det, r->pos, r->drift};
     };
-#pragma unroll 1
+#pragma unroll
     for (int b0 = 0; b0 < G; b0 += 32) {
         const int g = b0 + lane;
         int mk[4] = {-1, -1, -1, -1};
         if (g < G) {
             bool valid;
             const int n3 = s3_count(S, base, g % nu3, g / nu3, valid);
-#pragma unroll 1
+#pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int mm = k + 4 - n3;
                 if (valid && mm >= 0 && mm < 4 && lastc[mm] >= 0) mk[k] = mm;
@@ -469,7 +469,7 @@ __device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gp
         }
         const bool ustart = units && g < G && (g % gper) == 0;
         Stale ent[4];
-#pragma unroll 1
+#pragma unroll
         for (int k = 0; k < 4; ++k) {
             const unsigned wm = __ballot_sync(0xffffffffu, mk[k] >= 0);
             const int src = last_lane(wm & lanemask_lt());
