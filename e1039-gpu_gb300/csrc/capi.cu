@@ -164,7 +164,14 @@ int or_create(int device, or_ctx_t **out) {
 #ifndef OR_YZ_WARPS_SM
 #define OR_YZ_WARPS_SM 16
 #endif
-    c->yz_garena_warps = c->sm_count * OR_YZ_WARPS_SM;
+#ifndef OR_YZ_SPLIT
+#define OR_YZ_SPLIT 1
+#endif
+#ifndef OR_YZ_FIRST_WARPS_SM
+#define OR_YZ_FIRST_WARPS_SM 28
+#endif
+    // per-warp arenas and queues for the most warps a YZ kernel launches
+    c->yz_garena_warps = c->sm_count * (OR_YZ_SPLIT ? OR_YZ_FIRST_WARPS_SM : OR_YZ_WARPS_SM);
     if ((e = cudaMalloc(&c->yz_scratch,
                         orgpu::yz_scratch_bytes_ctx(c->yz_cap_units, c->yz_cap_heavy, c->yz_garena_warps))) !=
         cudaSuccess) {

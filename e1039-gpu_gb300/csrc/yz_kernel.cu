@@ -24,7 +24,16 @@
 //                    and acceptance of every windowed hit for this tracklet);
 //                    evaluates light tracklets itself, and cuts heavy ones
 //                    into units of whole (u3,v3) iterations on a device queue;
-//   yz_work_kernel   persistent warps drain the queue;
+//   yz_first_kernel  persistent warps (28 per SM, 80 registers) drain the
+//                    queue with the first cut only: fit of the station-3 and
+//                    station-2 y hits, 2-sigma cut, scratch-entry scan; each
+//                    unit's survivors (about 6 %) go in order to a device pool;
+//   yz_second_kernel per unit, the survivors replayed in order with the sign
+//                    carry: left/right walk, prop and hodoscope gates, chi2
+//                    (126 registers, 16 warps per SM); a unit whose survivors
+//                    did not fit runs whole, first cut and survivors together
+//                    (yz_work_kernel's path, which also serves contexts
+//                    without a pool, such as the no-allocation entry);
 //   yz_apply_kernel  writes each heavy tracklet's best combination.
 // Inside a range, lanes evaluate 32 combinations at a time in the reference
 // order; ballot/shuffle scans recover the sign state and the scratch entry.
@@ -45,6 +54,19 @@ constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's
 #ifndef OR_YZ_WARPS_SM
 #define OR_YZ_WARPS_SM 16
 #endif
+#ifndef OR_YZ_SPLIT
+#define OR_YZ_SPLIT 1
+#endif
+#ifndef OR_YZ_FIRST_WARPS_SM
+#define OR_YZ_FIRST_WARPS_SM 28
+#endif
+#ifndef OR_YZ_POOL_MI
+#define OR_YZ_POOL_MI 192
+#endif
+// survivor entries in the pool (32 B each): the 100,000-event uneven batch
+// queues between 64 Mi and 128 Mi survivors; units that do not fit run on
+// the combined path
+constexpr long long YZ_POOL_CAP = (long long)OR_YZ_POOL_MI << 20;
 constexpr int YZ_ARENA_HITS = OR_YZ_ARENA;      // windowed hits kept in shared memory per warp
 #ifndef OR_YZ_LIGHT
 #define OR_YZ_LIGHT 128
@@ -65,7 +87,10 @@ constexpr int YZ_GARENA_HITS = 8 * YZ_MAXWIN;  // per-warp global overflow arena
 // phases do not alternate every 32 survivors (each switch refetches the
 // other phase's instructions)
 constexpr int YZ_QCAP_MIN = 64;     // queue entries per warp: the static (no-allocation) scratch
-constexpr int YZ_QCAP_CTX = 2048;   // ... and a context's scratch
+#ifndef OR_YZ_QCAP_CTX
+#define OR_YZ_QCAP_CTX 2048
+#endif
+constexpr int YZ_QCAP_CTX = OR_YZ_QCAP_CTX;   // ... and a context's scratch
 
 struct __align__(16) YzHit {
     float Y, eY, pos, drift;
@@ -110,6 +135,11 @@ struct YzScratch {
     YzHit *garena;           // per-warp overflow arenas
     struct PassEntryStore *qbuf;  // per-warp survivor queues (qcap entries each)
     int cap_units, cap_heavy, garena_warps, qcap;
+    // split first-cut / survivor kernels: each unit's survivors in order in
+    // pool[useg[u].x .. + useg[u].y); useg[u].x < 0: the unit runs combined
+    struct PassEntryStore *pool;
+    int2 *useg;
+    long long pool_cap;  // 0: no pool, the combined kernel runs
 };
 
 // optional pruning: tracklet rows (row_off, as the scorer's) and keep flags
@@ -788,8 +818,10 @@ __device__ __forceinline__ int next_alive_outer(const YzAlive &m, int nu3, int i
     return (v < 0 || u < 0) ? -1 : u + v * nu3;
 }
 
-__device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l, long c1l, Stale st[4],
-                                       const or_plane_t &P, PassEntryStore *Q, int qcap) {
+template <bool FIRST_ONLY>
+__device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l, long c1l,
+                                         Stale st[4], const or_plane_t &P, PassEntryStore *Q, int qcap,
+                                         int *nsurv) {
     const int lane = lane_id();
     const int nu2 = S.np[0], nu3 = S.np[2];
     const int C2 = S.np[0] * S.np[1];
@@ -840,6 +872,12 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
             }
         }
         const bool more = basec < c1;
+        if constexpr (FIRST_ONLY) {
+            if (!more) {
+                *nsurv = qn;
+                return ~0ull;
+            }
+        }
         if (!more && qn == qh) break;
         if (more) {
             const int c = basec + lane;
@@ -985,7 +1023,14 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
             d2 -= cy ? nu3 : 0;
             d3 += s3 + cy;
         }
-        if (qn > qcap - 32 || (!more && qn > qh)) {
+        if constexpr (FIRST_ONLY) {
+            // survivors stay queued for the survivor kernel; a queue that
+            // could overflow gives the unit back to the combined path
+            if (qn > qcap - 32) {
+                *nsurv = -1;
+                return ~0ull;
+            }
+        } else if (qn > qcap - 32 || (!more && qn > qh)) {
             // a full queue (the next chunk could add 32) or the end of the
             // range: evaluate every waiting survivor, 32 at a time, in order
             while (qh < qn) {
@@ -998,6 +1043,12 @@ __device__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit 
         }
     }
     return cs.best;
+}
+
+__device__ __forceinline__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l,
+                                                      long c1l, Stale st[4], const or_plane_t &P, PassEntryStore *Q,
+                                                      int qcap) {
+    return yz_range_t<false>(S, E, base, c0l, c1l, st, P, Q, qcap, nullptr);
 }
 
 // write the best combination into the track record (K:1804-1825)
@@ -1210,6 +1261,139 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_
     }
 }
 
+
+// Split path, first kernel: the first cut of every queued unit (no survivor
+// evaluation, so it needs far fewer registers and no per-lane hit arrays);
+// a unit's survivors go, in order, to one contiguous piece of the pool.
+template <int W>
+__global__ void __launch_bounds__(W * 32, (OR_YZ_FIRST_WARPS_SM / W > 0 ? OR_YZ_FIRST_WARPS_SM / W : 1))
+    yz_first_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv, YzScratch sc) {
+    extern __shared__ __align__(16) unsigned char yz_smem[];
+    or_plane_t &P = *reinterpret_cast<or_plane_t *>(yz_smem);
+    YzWarp *warps = reinterpret_cast<YzWarp *>(yz_smem + ((sizeof(or_plane_t) + 15) & ~size_t(15)));
+    load_plane_smem(&P, gplane);
+    __syncthreads();
+    const int w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    YzWarp &S = warps[w];
+    const int gw = blockIdx.x * W + w;
+    if (gw >= sc.garena_warps) return;  // queues and arenas exist for garena_warps warps
+    YzHit *garena = yz_garena(sc, gw);
+    PassEntryStore *Q = sc.qbuf + (long)gw * sc.qcap;
+    unsigned long long *pool_ctr = reinterpret_cast<unsigned long long *>(sc.counters + 8);
+    const int nunits = min((int)sc.counters[0], sc.cap_units);
+    for (;;) {
+        int u = 0;
+        if (lane == 0) u = (int)atomicAdd(&sc.counters[2], 1u);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= nunits) break;
+        const YzUnit un = sc.units[u];
+        if (un.heavy < 0) continue;
+        const YzHeavy hv2 = sc.heavy[un.heavy];
+        const float *T = trk_rec(tv, hv2.e, hv2.slot, hv2.k);
+        const int st3 = 3 + (hv2.slot & 1);
+        YzEvent &E = S.ev;
+        __syncwarp();
+        if (lane == 0) yz_event_planes(E, hv, hv2.e, st3);
+        __syncwarp();
+        const YzHit *base;
+        yz_build(S, E, T, P, st3, base, garena);
+        Stale *st = S.st;
+        __syncwarp();
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) st[k] = un.entry[k];
+        __syncwarp();
+        const long C2 = (long)S.np[0] * S.np[1];
+        int ns = -1;
+        yz_range_t<true>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, Q, sc.qcap, &ns);
+        __syncwarp();
+        long long off = -1;
+        if (lane == 0 && ns >= 0) {
+            const unsigned long long o = atomicAdd(pool_ctr, (unsigned long long)ns);
+            if (o + (unsigned long long)ns <= (unsigned long long)sc.pool_cap) off = (long long)o;
+        }
+        off = __shfl_sync(0xffffffffu, off, 0);
+        if (off >= 0) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(Q);
+            uint4 *dst = reinterpret_cast<uint4 *>(sc.pool + off);
+#pragma unroll 1
+            for (int i = lane; i < ns * 2; i += 32) dst[i] = src[i];
+        }
+        if (lane == 0) sc.useg[u] = make_int2(off >= 0 ? (int)off : -1, off >= 0 ? ns : 0);
+        __syncwarp();
+    }
+}
+
+// Split path, second kernel: per unit, the windows again and then its
+// survivors replayed in order with the sign carry (or the whole unit on the
+// combined path when its survivors did not fit); writes the unit's best.
+template <int W>
+__global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_SM / W : 1))
+    yz_second_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv, YzScratch sc) {
+    extern __shared__ __align__(16) unsigned char yz_smem[];
+    or_plane_t &P = *reinterpret_cast<or_plane_t *>(yz_smem);
+    YzWarp *warps = reinterpret_cast<YzWarp *>(yz_smem + ((sizeof(or_plane_t) + 15) & ~size_t(15)));
+    load_plane_smem(&P, gplane);
+    __syncthreads();
+    const int w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    YzWarp &S = warps[w];
+    const int gw = blockIdx.x * W + w;
+    if (gw >= sc.garena_warps) return;
+    YzHit *garena = yz_garena(sc, gw);
+    PassEntryStore *Q = sc.qbuf + (long)gw * sc.qcap;
+    const int nunits = min((int)sc.counters[0], sc.cap_units);
+    for (;;) {
+        int u = 0;
+        if (lane == 0) u = (int)atomicAdd(&sc.counters[3], 1u);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= nunits) break;
+        const YzUnit un = sc.units[u];
+        if (un.heavy < 0) continue;
+        const int2 seg = sc.useg[u];
+        const YzHeavy hv2 = sc.heavy[un.heavy];
+        const float *T = trk_rec(tv, hv2.e, hv2.slot, hv2.k);
+        const int st3 = 3 + (hv2.slot & 1);
+        YzEvent &E = S.ev;
+        __syncwarp();
+        if (lane == 0) yz_event_planes(E, hv, hv2.e, st3);
+        __syncwarp();
+        const YzHit *base;
+        yz_build(S, E, T, P, st3, base, garena);
+        yz_xhits(S, T, P);
+        const long C2 = (long)S.np[0] * S.np[1];
+        unsigned long long bk;
+        if (seg.x < 0) {
+            Stale *st = S.st;
+            __syncwarp();
+#pragma unroll 1
+            for (int k = 0; k < 4; ++k) st[k] = un.entry[k];
+            __syncwarp();
+            bk = yz_range(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, Q, sc.qcap);
+        } else {
+            Phase2Carry cs;
+#pragma unroll 1
+            for (int i = 0; i < seg.y; i += 32) {
+                yz_phase2(S, E, base, (int)C2, P, sc.pool + seg.x + i, min(seg.y - i, 32), cs);
+                __syncwarp();
+            }
+            bk = cs.best;
+        }
+        __syncwarp();
+        YzBest *dst = sc.best + u;
+        if (bk == ~0ull) {
+            if (lane == 0) dst->key = ~0ull;
+        } else {
+            const unsigned *src = reinterpret_cast<const unsigned *>(&S.b);
+            unsigned *d = reinterpret_cast<unsigned *>(dst);
+#pragma unroll 1
+            for (int i = lane; i < (int)(sizeof(YzBest) / 4); i += 32) d[i] = src[i];
+        }
+        __syncwarp();
+    }
+}
+
+
 // one warp per heavy tracklet: its units' minimum key wins
 __global__ void __launch_bounds__(128) yz_apply_kernel(or_tracks_view_t tv, YzScratch sc) {
     const int lane = threadIdx.x & 31;
@@ -1250,11 +1434,20 @@ size_t yz_smem_bytes(int warps) {
 
 // Scratch the YZ stage needs: queue of units, per-unit best records, heavy
 // tracklets, per-warp overflow arenas.
+static long long yz_pool_cap(int qcap) { return (OR_YZ_SPLIT && qcap == YZ_QCAP_CTX) ? YZ_POOL_CAP : 0; }
+
 size_t yz_scratch_bytes_q(int cap_units, int cap_heavy, int garena_warps, int qcap) {
     size_t b = 256 + (sizeof(YzUnit) + sizeof(YzBest)) * (size_t)cap_units + sizeof(YzHeavy) * (size_t)cap_heavy;
     b = (b + 255) & ~size_t(255);
     b += sizeof(YzHit) * YZ_GARENA_HITS * (size_t)garena_warps;
-    return b + sizeof(PassEntryStore) * (size_t)qcap * (size_t)garena_warps;
+    b += sizeof(PassEntryStore) * (size_t)qcap * (size_t)garena_warps;
+    if (yz_pool_cap(qcap) > 0) {
+        b = (b + 255) & ~size_t(255);
+        b += sizeof(int2) * (size_t)cap_units;
+        b = (b + 255) & ~size_t(255);
+        b += sizeof(PassEntryStore) * (size_t)yz_pool_cap(qcap);
+    }
+    return b;
 }
 
 // the static (no-allocation) scratch: survivor queues of YZ_QCAP_MIN entries
@@ -1293,6 +1486,17 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
     sc.garena = reinterpret_cast<YzHit *>(p);
     p += sizeof(YzHit) * YZ_GARENA_HITS * (size_t)garena_warps;
     sc.qbuf = reinterpret_cast<PassEntryStore *>(p);
+    p += sizeof(PassEntryStore) * (size_t)qcap * (size_t)garena_warps;
+    sc.pool_cap = yz_pool_cap(qcap);
+    sc.useg = nullptr;
+    sc.pool = nullptr;
+    if (sc.pool_cap > 0) {
+        p = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
+        sc.useg = reinterpret_cast<int2 *>(p);
+        p += sizeof(int2) * (size_t)cap_units;
+        p = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
+        sc.pool = reinterpret_cast<PassEntryStore *>(p);
+    }
     sc.cap_units = cap_units;
     sc.cap_heavy = cap_heavy;
     sc.garena_warps = garena_warps;
@@ -1303,7 +1507,16 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
     yz_plan_kernel<W><<<(unsigned)blocks_plan, W * 32, smem, stream>>>(d_plane, hv, tv, toomany, n_events, sc, errw,
                                                                        prune);
     if ((err = cudaGetLastError())) return err;
-    yz_work_kernel<W><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, sc);
+    if (sc.pool_cap > 0) {
+        if ((err = smem_attr_once((const void *)yz_first_kernel<W>, (int)smem))) return err;
+        if ((err = smem_attr_once((const void *)yz_second_kernel<W>, (int)smem))) return err;
+        yz_first_kernel<W><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, sc);
+        if ((err = cudaGetLastError())) return err;
+        const long res = (long)sm_count * (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_SM / W : 1);
+        yz_second_kernel<W><<<(unsigned)min(blocks, res), W * 32, smem, stream>>>(d_plane, hv, tv, sc);
+    } else {
+        yz_work_kernel<W><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, sc);
+    }
     if ((err = cudaGetLastError())) return err;
     yz_apply_kernel<<<(unsigned)(sm_count * 4), 128, 0, stream>>>(tv, sc);
     return cudaGetLastError();
