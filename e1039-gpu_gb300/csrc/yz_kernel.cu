@@ -30,7 +30,8 @@
 //                    unit's survivors (about 6 %) go in order to a device pool;
 //   yz_second_kernel per unit, the survivors replayed in order with the sign
 //                    carry: left/right walk, prop and hodoscope gates, chi2
-//                    (126 registers, 16 warps per SM); a unit whose survivors
+//                    (24 warps per SM, registers capped at 85: its spills
+//                    cost less than the extra warps gain); a unit whose survivors
 //                    did not fit runs whole, first cut and survivors together
 //                    (yz_work_kernel's path, which also serves contexts
 //                    without a pool, such as the no-allocation entry);
@@ -56,6 +57,9 @@ constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's
 #endif
 #ifndef OR_YZ_SPLIT
 #define OR_YZ_SPLIT 1
+#endif
+#ifndef OR_YZ_PLAN_WARPS_SM
+#define OR_YZ_PLAN_WARPS_SM 20
 #endif
 #ifndef OR_YZ_FIRST_WARPS_SM
 #define OR_YZ_FIRST_WARPS_SM 28
@@ -1082,7 +1086,7 @@ __device__ __forceinline__ YzHit *yz_garena(const YzScratch &sc, int gwarp) {
 }
 
 template <int W>
-__global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_SM / W : 1))
+__global__ void __launch_bounds__(W * 32, (OR_YZ_PLAN_WARPS_SM / W > 0 ? OR_YZ_PLAN_WARPS_SM / W : 1))
     yz_plan_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
                    const uint8_t *__restrict__ toomany, int n_events, YzScratch sc, uint32_t *__restrict__ errw,
                    YzPrune prune) {
@@ -1327,8 +1331,11 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_FIRST_WARPS_SM / W > 0 ? OR_YZ_
 // Split path, second kernel: per unit, the windows again and then its
 // survivors replayed in order with the sign carry (or the whole unit on the
 // combined path when its survivors did not fit); writes the unit's best.
+#ifndef OR_YZ_SECOND_WARPS_SM
+#define OR_YZ_SECOND_WARPS_SM 24
+#endif
 template <int W>
-__global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_SM / W : 1))
+__global__ void __launch_bounds__(W * 32, (OR_YZ_SECOND_WARPS_SM / W > 0 ? OR_YZ_SECOND_WARPS_SM / W : 1))
     yz_second_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv, YzScratch sc) {
     extern __shared__ __align__(16) unsigned char yz_smem[];
     or_plane_t &P = *reinterpret_cast<or_plane_t *>(yz_smem);
@@ -1512,7 +1519,7 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
         if ((err = smem_attr_once((const void *)yz_second_kernel<W>, (int)smem))) return err;
         yz_first_kernel<W><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, sc);
         if ((err = cudaGetLastError())) return err;
-        const long res = (long)sm_count * (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_SM / W : 1);
+        const long res = (long)sm_count * (OR_YZ_SECOND_WARPS_SM / W > 0 ? OR_YZ_SECOND_WARPS_SM / W : 1);
         yz_second_kernel<W><<<(unsigned)min(blocks, res), W * 32, smem, stream>>>(d_plane, hv, tv, sc);
     } else {
         yz_work_kernel<W><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, sc);
