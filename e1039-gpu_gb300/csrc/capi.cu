@@ -12,7 +12,7 @@ cudaError_t launch_event_reduce(or_hits_view_t, uint8_t *, int, uint32_t *, cuda
 cudaError_t launch_xz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, int32_t *, uint8_t *, int, cudaStream_t,
                       int, int);
 cudaError_t launch_yz_tuned(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
-                            void *, int, int, int, cudaStream_t, int, int);
+                            void *, int, int, int, cudaStream_t, int, int, long long);
 cudaError_t launch_yz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *, void *,
                       int, int, int, cudaStream_t, int);
 size_t yz_scratch_bytes_ctx(int, int, int);
@@ -33,7 +33,8 @@ cudaError_t launch_rt_apply(const or_rt_table_t *, or_hits_view_t, int, cudaStre
 cudaError_t launch_collect(or_tracks_view_t, const uint8_t *, int, float, float *, long long, unsigned long long *,
                            cudaStream_t);
 cudaError_t launch_yz_pruned(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
-                             void *, int, int, int, cudaStream_t, int, const int32_t *, const uint8_t *, long, int);
+                             void *, int, int, int, cudaStream_t, int, const int32_t *, const uint8_t *, long, int,
+                             long long);
 cudaError_t launch_rows(const uint16_t *, const uint8_t *, int, int32_t *, cudaStream_t);
 cudaError_t launch_features(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int,
                             const int32_t *, float *, long, cudaStream_t, int, int);
@@ -64,6 +65,7 @@ struct or_ctx {
     // YZ work queue: units of heavy tracklets, their best records, overflow arenas
     void *yz_scratch;
     int yz_cap_units, yz_cap_heavy, yz_garena_warps;
+    long long yz_pool_limit;  // survivor-pool entries the split YZ path may use (-1: all)
     int warps[OR_K_COUNT];  // events (work units) per CTA of each tunable kernel
     // per-event row counts and offsets of or_output_rows, grown on demand
     void *out_scratch = nullptr;
@@ -172,6 +174,7 @@ int or_create(int device, or_ctx_t **out) {
 #endif
     // per-warp arenas and queues for the most warps a YZ kernel launches
     c->yz_garena_warps = c->sm_count * (OR_YZ_SPLIT ? OR_YZ_FIRST_WARPS_SM : OR_YZ_WARPS_SM);
+    c->yz_pool_limit = -1;
     if ((e = cudaMalloc(&c->yz_scratch,
                         orgpu::yz_scratch_bytes_ctx(c->yz_cap_units, c->yz_cap_heavy, c->yz_garena_warps))) !=
         cudaSuccess) {
@@ -182,6 +185,12 @@ int or_create(int device, or_ctx_t **out) {
         return fail(OR_ERR_NOMEM, "cudaMalloc YZ work queue");
     }
     *out = c;
+    return OR_OK;
+}
+
+int or_set_yz_pool_limit(or_ctx_t *ctx, int64_t entries) {
+    if (!ctx) return fail(OR_ERR_ARG, "null context");
+    ctx->yz_pool_limit = entries < 0 ? -1 : (long long)entries;
     return OR_OK;
 }
 
@@ -270,7 +279,8 @@ int or_yz(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uin
     if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
     cudaError_t e = orgpu::launch_yz_tuned(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw,
                                            ctx->yz_scratch, ctx->yz_cap_units, ctx->yz_cap_heavy,
-                                           ctx->yz_garena_warps, S(stream), ctx->sm_count, ctx->warps[OR_K_YZ]);
+                                           ctx->yz_garena_warps, S(stream), ctx->sm_count, ctx->warps[OR_K_YZ],
+                                           ctx->yz_pool_limit);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "YZ launch");
 }
 
@@ -516,7 +526,8 @@ int or_yz_pruned(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, co
     if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
     cudaError_t e = orgpu::launch_yz_pruned(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw, ctx->yz_scratch,
                                             ctx->yz_cap_units, ctx->yz_cap_heavy, ctx->yz_garena_warps, S(stream),
-                                            ctx->sm_count, row_off, keep, (long)max_rows, ctx->warps[OR_K_YZ]);
+                                            ctx->sm_count, row_off, keep, (long)max_rows, ctx->warps[OR_K_YZ],
+                                            ctx->yz_pool_limit);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "pruned YZ launch");
 }
 

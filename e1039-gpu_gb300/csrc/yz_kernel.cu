@@ -1471,7 +1471,7 @@ template <int W>
 static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
                                   const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
                                   int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, YzPrune prune,
-                                  int qcap) {
+                                  int qcap, long long pool_limit) {
     if (n_events <= 0) return cudaSuccess;
     const size_t smem = yz_smem_bytes(W);
     cudaError_t err;
@@ -1495,6 +1495,7 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
     sc.qbuf = reinterpret_cast<PassEntryStore *>(p);
     p += sizeof(PassEntryStore) * (size_t)qcap * (size_t)garena_warps;
     sc.pool_cap = yz_pool_cap(qcap);
+    if (pool_limit >= 0 && pool_limit < sc.pool_cap) sc.pool_cap = pool_limit;  // the rest of the pool goes unused
     sc.useg = nullptr;
     sc.pool = nullptr;
     if (sc.pool_cap > 0) {
@@ -1532,18 +1533,18 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
 static cudaError_t launch_yz_w(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
                                const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
                                int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, YzPrune prune,
-                               int warps, int qcap) {
+                               int warps, int qcap, long long pool_limit) {
     switch (warps) {
     case 1: return launch_yz_impl<1>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                     garena_warps, stream, sm_count, prune, qcap);
+                                     garena_warps, stream, sm_count, prune, qcap, pool_limit);
     case 2: return launch_yz_impl<2>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                     garena_warps, stream, sm_count, prune, qcap);
+                                     garena_warps, stream, sm_count, prune, qcap, pool_limit);
     case 8: return launch_yz_impl<8>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                     garena_warps, stream, sm_count, prune, qcap);
+                                     garena_warps, stream, sm_count, prune, qcap, pool_limit);
     case 16: return launch_yz_impl<16>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                       garena_warps, stream, sm_count, prune, qcap);
+                                       garena_warps, stream, sm_count, prune, qcap, pool_limit);
     default: return launch_yz_impl<4>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                      garena_warps, stream, sm_count, prune, qcap);
+                                      garena_warps, stream, sm_count, prune, qcap, pool_limit);
     }
 }
 
@@ -1551,15 +1552,16 @@ cudaError_t launch_yz(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_vi
                       int n_events, uint32_t *errw, void *scratch, int cap_units, int cap_heavy, int garena_warps,
                       cudaStream_t stream, int sm_count) {
     return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
-                       sm_count, YzPrune{nullptr, nullptr, 0}, 4, YZ_QCAP_MIN);
+                       sm_count, YzPrune{nullptr, nullptr, 0}, 4, YZ_QCAP_MIN, -1);
 }
 
 // with `warps` events (work units) per CTA: 1, 2, 4, 8 or 16
 cudaError_t launch_yz_tuned(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
                             const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
-                            int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, int warps) {
+                            int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, int warps,
+                            long long pool_limit) {
     return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
-                       sm_count, YzPrune{nullptr, nullptr, 0}, warps, YZ_QCAP_CTX);
+                       sm_count, YzPrune{nullptr, nullptr, 0}, warps, YZ_QCAP_CTX, pool_limit);
 }
 
 // YZ with the scorer's keep flags: pruned tracklets are left as tracklets no
@@ -1567,9 +1569,10 @@ cudaError_t launch_yz_tuned(const or_plane_t *d_plane, or_hits_view_t hv, or_tra
 cudaError_t launch_yz_pruned(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
                              const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
                              int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count,
-                             const int32_t *row_off, const uint8_t *keep, long max_rows, int warps) {
+                             const int32_t *row_off, const uint8_t *keep, long max_rows, int warps,
+                             long long pool_limit) {
     return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
-                       sm_count, YzPrune{row_off, keep, max_rows}, warps, YZ_QCAP_CTX);
+                       sm_count, YzPrune{row_off, keep, max_rows}, warps, YZ_QCAP_CTX, pool_limit);
 }
 
 }  // namespace orgpu

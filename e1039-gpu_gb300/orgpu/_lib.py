@@ -23,7 +23,7 @@ EXPORTS = ("or_version", "or_last_error", "or_status_string", "or_geometry_load"
            "or_mlp_adam", "or_prop_matching", "or_global_clean", "or_run_selection", "or_set_launch",
            "or_get_launch", "or_vertexing", "or_dimuons", "or_fill_histograms", "or_hist_table_init",
            "or_run_physics", "or_output_rows", "or_rt_load", "or_rt_set_plane", "or_rt_table_bytes",
-           "or_pack_hits_rt", "or_rt_apply")
+           "or_pack_hits_rt", "or_rt_apply", "or_set_yz_pool_limit")
 
 # tunable kernels (or_kernel_id_t)
 KERNELS = {"event_reduce": 0, "xz": 1, "yz": 2, "back_clean": 3, "global": 4, "select": 5, "features": 6}
@@ -110,6 +110,7 @@ def lib():
     lb.or_rt_table_bytes.restype = C.c_size_t
     lb.or_pack_hits_rt.argtypes = [vp, vp, vp, i32, vp, vp, L.OrHitsView, vp]
     lb.or_rt_apply.argtypes = [vp, vp, L.OrHitsView, i32, vp]
+    lb.or_set_yz_pool_limit.argtypes = [vp, i64]
     for name in EXPORTS:
         getattr(lb, name)
     _lib = lb

@@ -290,6 +290,11 @@ class Reconstruction:
                                           d_wire_pos_f.data_ptr(), b.hits_view(), self._stream(stream)),
                    "or_pack_hits")
 
+    def set_yz_pool_limit(self, entries):
+        """Survivor-pool entries the split YZ path may use (-1: all); units
+        that do not fit run whole, with the same results."""
+        _lib.check(self.lib.or_set_yz_pool_limit(self.ctx, int(entries)), "or_set_yz_pool_limit")
+
     def pack_rt(self, b, d_records, d_offsets, d_wire_pos_f, d_rt, stream=None):
         """Device packer with the drift distance from the R-T calibration
         (d_rt: device uint8 tensor holding an OrRtTable, see rt_to_device)."""

@@ -85,6 +85,13 @@ int or_destroy(or_ctx_t *ctx);
  * the autotuner (orgpu/autotune.py); or_get_launch returns the current one. */
 int or_set_launch(or_ctx_t *ctx, int kernel, int events_per_cta);
 int or_get_launch(or_ctx_t *ctx, int kernel);
+/* The YZ stage runs as a first-cut kernel that keeps each work unit's
+ * surviving combinations, in order, in a survivor pool of the context, and a
+ * second kernel that evaluates them; a unit whose survivors do not fit runs
+ * whole in the second kernel, with the same results.  Limit the pool to
+ * `entries` survivors (< 0: the whole pool, 192 Mi).  A tuning and test
+ * knob: results do not depend on it. */
+int or_set_yz_pool_limit(or_ctx_t *ctx, int64_t entries);
 /* Copy a host or_plane_t to the device (online_reconstruction.cu:754). */
 int or_set_geometry(or_ctx_t *ctx, const or_plane_t *plane);
 /* Wait for `stream` and report the device-side error words raised since the

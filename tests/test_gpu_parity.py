@@ -72,6 +72,27 @@ def test_yz(setup):
     assert count_tracks(snap.tracks_yz, 5) > 0
 
 
+@pytest.mark.parametrize("limit", [0, 300, 5000])
+def test_yz_survivor_pool_fallback(setup, limit):
+    """The split YZ path with the survivor pool limited: units whose
+    survivors do not fit run whole in the second kernel (limit 0: every unit;
+    300: some), and the tracks stay bit-exact with the oracle."""
+    import torch
+    from orgpu import pipeline
+    plane, geo, rec, off, hits0, snap, rc = setup
+    b = _batch(rc, hits0.n, pipeline)
+    b.upload_hits(snap.hits_er)
+    b.toomany.copy_(torch.from_numpy(snap.toomany_xz))
+    b.upload_tracks(snap.tracks_xz)
+    rc.set_yz_pool_limit(limit)
+    try:
+        rc.yz_tracking(b)
+        rc.sync()
+    finally:
+        rc.set_yz_pool_limit(-1)
+    assert track_mismatches(b.download_tracks(), snap.tracks_yz, snap.toomany_xz) == []
+
+
 def test_back_clean(setup):
     import torch
     from orgpu import pipeline
