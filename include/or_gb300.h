@@ -77,8 +77,10 @@ const char *or_status_string(int status);
  * otherwise it must hold OR_NDET*OR_WIREPOS_STRIDE doubles.  Host only. */
 int or_geometry_load(const char *path, or_plane_t *plane, double *wire_pos);
 
-/* Context: one per device.  or_create() selects `device`, allocates the
- * context's small device state, and records a copy of nothing else. */
+/* Context: one per device.  or_create() selects `device` and allocates the
+ * context's device state: the geometry, error words, and the YZ scratch
+ * (work queue, per-warp arenas and survivor queues, and the 6 GB survivor
+ * pool of the split YZ path: about 7.9 GB in all). */
 int or_create(int device, or_ctx_t **out);
 int or_destroy(or_ctx_t *ctx);
 /* Events per CTA of `kernel` (1, 2, 4, 8 or 16; default 4), e.g. as chosen by
