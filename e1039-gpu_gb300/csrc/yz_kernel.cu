@@ -73,7 +73,7 @@ constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's
 constexpr long long YZ_POOL_CAP = (long long)OR_YZ_POOL_MI << 20;
 constexpr int YZ_ARENA_HITS = OR_YZ_ARENA;      // windowed hits kept in shared memory per warp
 #ifndef OR_YZ_LIGHT
-#define OR_YZ_LIGHT 64
+#define OR_YZ_LIGHT 32
 #endif
 constexpr long YZ_LIGHT = OR_YZ_LIGHT;         // combinations a planning warp evaluates itself per tracklet
 constexpr long YZ_CHUNK_INLINE = OR_YZ_LIGHT;  // ... and per planning unit
