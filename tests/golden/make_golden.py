@@ -30,7 +30,7 @@ Outputs (under --out):
                           configuration and the reference's output of every
                           stage for them, for both images
 
-Usage: python tests/golden/make_golden.py --out gpurun_out/golden
+Usage: python tests/golden/make_golden.py --out <output directory>
 """
 import argparse
 import json
@@ -207,7 +207,7 @@ def compare(snap, ref, rtol):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--out", default=os.path.join(REPO, "gpurun_out", "golden"))
+    ap.add_argument("--out", default=os.path.join(REPO, "out", "golden"))
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     from oracle.ref import refrun

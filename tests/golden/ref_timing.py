@@ -27,7 +27,7 @@ fmad1 is the reference as its Makefile builds it (nvcc's default
 -fmad=true), fmad0 the build the library is bit-exact with.
 
 Output: <out>/ref_timing.json.  Usage:
-    python tests/golden/ref_timing.py --out gpurun_out/ref_timing
+    python tests/golden/ref_timing.py --out <output directory>
 """
 import argparse
 import json
@@ -255,7 +255,7 @@ def b_tracks(b, snap):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--out", default=os.path.join(REPO, "gpurun_out", "ref_timing"))
+    ap.add_argument("--out", default=os.path.join(REPO, "out", "ref_timing"))
     ap.add_argument("--uneven-events", type=int, default=100000)
     ap.add_argument("--images", default="fmad1,fmad0")
     ap.add_argument("--configs", default="small,uneven,high_occupancy")
