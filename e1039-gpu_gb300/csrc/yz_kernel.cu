@@ -49,6 +49,18 @@ namespace orgpu {
 
 constexpr int YZ_MAXWIN = 100;          // windowed hits per plane (the reference's hitidx arrays)
 constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's hitpairs arrays)
+// Build-time tunables (-D...), with the values measured best on the
+// 100,000-event uneven batch; results do not depend on any of them:
+//   OR_YZ_ARENA          windowed hit records per warp in shared memory
+//   OR_YZ_WARPS_SM       warps per SM of the combined work kernel
+//   OR_YZ_SPLIT          first-cut / survivor kernels (1) or the combined one (0)
+//   OR_YZ_PLAN_WARPS_SM, OR_YZ_FIRST_WARPS_SM, OR_YZ_SECOND_WARPS_SM
+//                        warps per SM (register caps) of the other kernels
+//   OR_YZ_POOL_MI        survivor-pool entries, in Mi
+//   OR_YZ_LIGHT          combinations a planning warp evaluates itself
+//   OR_YZ_PLAN_CHUNK     slots per planning unit
+//   OR_YZ_UNIT           live combinations per queued unit
+//   OR_YZ_QCAP_CTX       per-warp survivor queue entries of a context
 #ifndef OR_YZ_ARENA
 #define OR_YZ_ARENA 64
 #endif
