@@ -7,7 +7,10 @@ through properties that do not need the oracle at that size:
     planning units and the overflow arenas differ between the two);
   - well-formed output: every global track has 5-18 hits with detector ids
     in the chamber range, charge +-1, a finite chi2 and 1/p in the window
-    the global stage enforces.
+    the global stage enforces;
+  - R-T conversion: the packer with the calibration fused in equals the
+    plain packer followed by the in-place conversion, bit for bit, and
+    changes only the chamber and prop-tube drift fields.
 
 Bit-exactness against the oracle is tested on smaller batches
 (test_gpu_parity.py); this adds the full-size behaviour of the queue and
@@ -95,3 +98,49 @@ def test_full_batch_tracks_well_formed(full):
     assert np.isfinite(g[:, L.TRK_CHI2]).all()
     invp = g[:, L.TRK_INVP]
     assert ((invp > 0.0) & (invp < 0.25)).all()
+
+
+def test_full_batch_rt_fused_equals_apply(full):
+    """R-T conversion at full size: the packer with the calibration fused in
+    gives the same hit buffers, bit for bit, as the plain packer followed by
+    the in-place conversion; and only the drift field of chamber and
+    prop-tube hits changes against the plain packer."""
+    import torch
+    from orgpu import CALIBRATION_E906, _lib, layout as L, pipeline
+    plane, geo, rec, off = full
+    n = len(off) - 1
+    rc = pipeline.Reconstruction(plane, 0)
+    d_rec = torch.from_numpy(rec.view(np.uint8)).cuda()
+    d_off = torch.from_numpy(off).cuda()
+    d_wp = torch.from_numpy(geo.wire_pos_f32().reshape(-1)).cuda()
+    rt, _ = _lib.rt_load(CALIBRATION_E906, plane)
+    d_rt = pipeline.rt_to_device(rt)
+    fused = pipeline.DeviceBatch(n, with_tracks=False)
+    applied = pipeline.DeviceBatch(n, with_tracks=False)
+    plain = pipeline.DeviceBatch(n, with_tracks=False)
+    for b in (fused, applied, plain):
+        for t in (b.hits_cham, b.hits_hodo, b.hits_prop):
+            t.zero_()
+    rc.pack_rt(fused, d_rec, d_off, d_wp, d_rt)
+    rc.pack(applied, d_rec, d_off, d_wp)
+    rc.rt_apply(applied, d_rt)
+    rc.pack(plain, d_rec, d_off, d_wp)
+    rc.sync()
+    for name in ("nhits_cham", "hits_cham", "nhits_hodo", "hits_hodo", "nhits_prop", "hits_prop"):
+        a, b = getattr(fused, name), getattr(applied, name)
+        assert torch.equal(a.view(torch.int32), b.view(torch.int32)), name
+    # hodoscopes untouched; chambers and prop tubes differ only in the drift field
+    assert torch.equal(fused.hits_hodo.view(torch.int32), plain.hits_hodo.view(torch.int32))
+    for name, per, cap in (("cham", L.NCHAM, L.MAXHITS_CHAM), ("prop", L.NPROP, L.MAXHITS_PROP)):
+        f = getattr(fused, "hits_" + name).view(n, per, L.NHITSPARAM, cap)
+        p = getattr(plain, "hits_" + name).view(n, per, L.NHITSPARAM, cap)
+        # with the slot stride = count, the drift field is the last count
+        # floats of each slot's 5*count head; the first four fields match
+        cnt = getattr(plain, "nhits_" + name).view(n, per).long()
+        flat_f = f.reshape(n * per, -1)
+        flat_p = p.reshape(n * per, -1)
+        idx = torch.arange(L.NHITSPARAM * cap, device=f.device)[None, :]
+        head = idx < 4 * cnt.reshape(-1, 1)
+        assert torch.equal(flat_f[head].view(torch.int32), flat_p[head].view(torch.int32)), name
+        changed = (flat_f.view(torch.int32) != flat_p.view(torch.int32)).any(dim=1)
+        assert bool(changed.any()), name
