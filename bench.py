@@ -133,11 +133,20 @@ def run_cpu(plane, wp, rec, off, n, threads):
 def main():
     args = parse()
     world, rank, local = dist_setup(args)
-    import __graft_entry__
-    __graft_entry__.build()
-    from orgpu import GEOMETRY_E906, _lib, layout as L, synth as S
-
-    plane, wp = _lib.geometry_load(GEOMETRY_E906)
+    from orgpu import GEOMETRY_E906, layout as L, synth as S
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        # the reference arm loads the oracle only (oracle/liborc.so): the
+        # geometry is parsed by the oracle's restatement of the reference's
+        # reader, and the library is neither built nor loaded
+        from oracle import pyoracle as O
+        plane, wp = O.parse_geometry(GEOMETRY_E906)
+    else:
+        import __graft_entry__
+        __graft_entry__.build()
+        from orgpu import _lib
+        plane, wp = _lib.geometry_load(GEOMETRY_E906)
     n = args.events
     from orgpu import shard
     cfg = S.config_uneven(n, shard.rank_seed(args.seed, rank))
@@ -149,8 +158,6 @@ def main():
         rec.nbytes / 1e6)
 
     if args.impl == "reference":
-        if rank != 0:
-            return
         # each step: the CPU restatement on a bounded sample, all host threads
         ns = args.cpu_sample or min(n, 12000)
         times = []
