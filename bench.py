@@ -382,9 +382,9 @@ def main():
     print(json.dumps(line))
 
 
-# kernels one step launches: pack, event reducer, XZ, YZ plan / first cut /
-# survivors / apply, cleaning, global tracking
-LAUNCHES_PER_STEP = 9
+# kernels one step launches: pack, event reducer, XZ, YZ fit table / plan /
+# first cut / survivors / apply, cleaning, global tracking
+LAUNCHES_PER_STEP = 10
 
 
 def rt_leg(args, rc, b, plane, rec, d_rec, d_off, d_wp, dev):

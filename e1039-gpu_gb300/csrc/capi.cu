@@ -28,7 +28,8 @@ cudaError_t launch_back_clean(or_tracks_view_t, const uint8_t *, int, cudaStream
 cudaError_t launch_global(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
                           unsigned long long *, cudaStream_t, int, int);
 cudaError_t launch_pack(const or_hit_record_t *, const int64_t *, int, const float *, const or_rt_table_t *,
-                        or_hits_view_t, cudaStream_t, int);
+                        or_hits_view_t, uint32_t *, cudaStream_t, int);
+cudaError_t launch_wait_selftest(uint32_t *, uint32_t, cudaStream_t);
 cudaError_t launch_rt_apply(const or_rt_table_t *, or_hits_view_t, int, cudaStream_t, int);
 cudaError_t launch_collect(or_tracks_view_t, const uint8_t *, int, float, float *, long long, unsigned long long *,
                            cudaStream_t);
@@ -245,8 +246,18 @@ int or_stream_sync(or_ctx_t *ctx, void *stream) {
         if (w & orgpu::ERRW_TMA_TIMEOUT) return fail(OR_ERR_TIMEOUT, "a bounded bulk-copy wait gave up");
         if (w & orgpu::ERRW_CAPACITY)
             return fail(OR_ERR_CAPACITY, "a hit-pair window exceeded its capacity (128 pairs); tracklet skipped");
+        if (w & orgpu::ERRW_INPUT)
+            return fail(OR_ERR_ARG, "hit records of an event are not sorted by (det, elem, tdc); its hits are undefined");
     }
     return OR_OK;
+}
+
+int or_selftest_bounded_wait(or_ctx_t *ctx, int polls, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (polls < 1 || polls > 1000000) return fail(OR_ERR_ARG, "polls must be in 1..1000000");
+    cudaError_t e = orgpu::launch_wait_selftest(ctx->d_errw, (uint32_t)polls, S(stream));
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "wait self-test launch");
 }
 
 int or_event_reduce(or_ctx_t *ctx, or_hits_view_t hits, uint8_t *toomany, int n_events, void *stream) {
@@ -298,7 +309,10 @@ int or_yz_noalloc(const or_plane_t *d_plane, or_hits_view_t hits, or_tracks_view
     const char *why = nullptr;
     cudaError_t e = orgpu::launch_yz_noalloc(d_plane, hits, tracks, toomany, n_events, d_errw, S(stream), &why);
     if (e == cudaSuccess) return OR_OK;
-    if (why) return fail(OR_ERR_CAPACITY, std::string("or_yz_noalloc: ") + why);
+    // a device outside the per-device table is an argument error (splitting
+    // the batch would not help); a static area smaller than its queue is one
+    // of capacity
+    if (why) return fail(e == cudaErrorInvalidDevice ? OR_ERR_ARG : OR_ERR_CAPACITY, std::string("or_yz_noalloc: ") + why);
     return cuda_fail(e, "or_yz_noalloc");
 }
 
@@ -657,7 +671,8 @@ int or_pack_hits(or_ctx_t *ctx, const or_hit_record_t *records, const int64_t *r
     if (n_events < 0 || !rec_offsets || !wire_pos_f) return fail(OR_ERR_ARG, "bad packer arguments");
     if ((rc = check_hits(hits))) return rc;
     cudaError_t e =
-        orgpu::launch_pack(records, rec_offsets, n_events, wire_pos_f, nullptr, hits, S(stream), ctx->sm_count);
+        orgpu::launch_pack(records, rec_offsets, n_events, wire_pos_f, nullptr, hits, ctx->d_errw, S(stream),
+                           ctx->sm_count);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "packer launch");
 }
 
@@ -668,7 +683,8 @@ int or_pack_hits_rt(or_ctx_t *ctx, const or_hit_record_t *records, const int64_t
     if (n_events < 0 || !rec_offsets || !wire_pos_f || !rt_dev) return fail(OR_ERR_ARG, "bad packer arguments");
     if ((rc = check_hits(hits))) return rc;
     cudaError_t e =
-        orgpu::launch_pack(records, rec_offsets, n_events, wire_pos_f, rt_dev, hits, S(stream), ctx->sm_count);
+        orgpu::launch_pack(records, rec_offsets, n_events, wire_pos_f, rt_dev, hits, ctx->d_errw, S(stream),
+                           ctx->sm_count);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "packer launch");
 }
 

@@ -22,6 +22,7 @@ constexpr int ER_BUF_FLOATS = 2048;                 // 8 KB staging buffer per w
 constexpr int ER_MAX_STAGED_HITS = ER_BUF_FLOATS / 5 + 8;
 constexpr int ER_NPLANES = 48;
 constexpr uint32_t ER_WAIT_LIMIT = 1u << 26;        // bounded mbarrier wait
+constexpr uint32_t ER_DRAIN_LIMIT = 1u << 28;       // ... and the wait for copies in flight after it gave up
 
 // the 48 planes the reducer touches: the 24 chambers of the E1039 set
 // (reconstruction_constants.h:60), 16 hodoscopes, 8 prop tubes (K:25-57)
@@ -221,8 +222,13 @@ __global__ void __launch_bounds__(W * 32) er_kernel(or_hits_view_t hv, uint8_t *
                     const PlaneRef r = er_plane(hv, e, c_er_det[p]);
                     tma_load_1d(S.buf + S.soff[p], r.slot, (uint32_t)sz * 4u, &S.bar);
                 }
-                if (!mbar_wait_bounded(&S.bar, phase, ER_WAIT_LIMIT)) {
+                if (!__all_sync(0xffffffffu, mbar_wait_bounded(&S.bar, phase, ER_WAIT_LIMIT))) {
+                    // the wait gave up: raise the error word, then wait (again
+                    // bounded) for this batch's copies still in flight, so that
+                    // the warp leaves no bulk copy writing into shared memory
                     if (lane == 0) atomicOr(errw, ERRW_TMA_TIMEOUT);
+                    mbar_wait_bounded(&S.bar, phase, ER_DRAIN_LIMIT);
+                    __syncwarp();
                     return;
                 }
                 phase ^= 1u;
@@ -270,6 +276,25 @@ static cudaError_t er_launch(or_hits_view_t hv, uint8_t *toomany, int n_events, 
     const long cap = (long)sm_count * (48 / W > 0 ? 48 / W : 1);  // up to 48 resident warps per SM
     if (blocks > cap) blocks = cap;
     er_kernel<W><<<(unsigned)blocks, W * 32, smem, stream>>>(hv, toomany, n_events, errw);
+    return cudaGetLastError();
+}
+
+// Self-test of the bounded wait: one warp waits on an mbarrier that nothing
+// arrives at and no bulk copy targets, `polls` polls at most.  The wait runs
+// out, the kernel raises ERRW_TMA_TIMEOUT as the reducer does, invalidates the
+// barrier and returns; the context stays usable.
+__global__ void __launch_bounds__(32) wait_selftest_kernel(uint32_t *__restrict__ errw, uint32_t polls) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncwarp();
+    const bool done = __all_sync(0xffffffffu, mbar_wait_bounded(&bar, 0u, polls));
+    if (!done && threadIdx.x == 0) atomicOr(errw, ERRW_TMA_TIMEOUT);
+    __syncwarp();
+    if (threadIdx.x == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&bar)) : "memory");
+}
+
+cudaError_t launch_wait_selftest(uint32_t *errw, uint32_t polls, cudaStream_t stream) {
+    wait_selftest_kernel<<<1, 32, 0, stream>>>(errw, polls);
     return cudaGetLastError();
 }
 

@@ -404,10 +404,14 @@ __device__ __forceinline__ int last_lane(unsigned m) { return m ? 31 - __clz(m) 
 
 // Raise a kernel's dynamic shared-memory limit once per device; the
 // attribute persists, so later launches -- also those recorded into a CUDA
-// graph by stream capture -- make no further runtime calls for it.
+// graph by stream capture -- make no further runtime calls for it.  The
+// table holds SMEM_ATTR_FUNCS kernels per device, above the library's count
+// of kernel instantiations that use it (about 40: the launch-shape templates
+// of every stage); a kernel beyond it would set the attribute on each launch.
+constexpr int SMEM_ATTR_FUNCS = 128;
 inline cudaError_t smem_attr_once(const void *func, int bytes) {
     static std::mutex mu;
-    static const void *fn[64][32];
+    static const void *fn[64][SMEM_ATTR_FUNCS];
     static int nfn[64];
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -417,7 +421,7 @@ inline cudaError_t smem_attr_once(const void *func, int bytes) {
     for (int i = 0; i < nfn[dev]; ++i)
         if (fn[dev][i] == func) return cudaSuccess;
     e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (e == cudaSuccess && nfn[dev] < 32) fn[dev][nfn[dev]++] = func;
+    if (e == cudaSuccess && nfn[dev] < SMEM_ATTR_FUNCS) fn[dev][nfn[dev]++] = func;
     return e;
 }
 
@@ -426,6 +430,7 @@ enum : uint32_t {
     ERRW_NONE = 0u,
     ERRW_TMA_TIMEOUT = 1u,
     ERRW_CAPACITY = 2u,
+    ERRW_INPUT = 4u,  // hit records of an event not sorted by (det, elem, tdc)
 };
 
 // ---------------------------------------------------------------------------

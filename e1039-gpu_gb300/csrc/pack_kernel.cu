@@ -7,7 +7,10 @@
 // drift] with stride = count, pos = (float)wire_position[det][elem].
 // Records of an event must be sorted by (det, elem, tdc); hits beyond a
 // plane's slot capacity are dropped (the reference host would write past the
-// slot).  One warp per event: a shared-memory histogram per plane, an
+// slot).  An event whose records are out of that order raises ERRW_INPUT
+// (or_stream_sync reports it as an argument error); its slots are then
+// undefined but every write stays inside them.  Records whose det is outside
+// 1..54 (they sort first or last) are skipped.  One warp per event: a shared-memory histogram per plane, an
 // exclusive scan, then coalesced field writes.
 //
 // With an R-T table the drift field is computed from the tdc as the
@@ -59,7 +62,8 @@ static __device__ __forceinline__ bool rt_plane(int det) {
 template <bool RT>
 __global__ void __launch_bounds__(PK_WARPS * 32)
     pack_kernel(const or_hit_record_t *__restrict__ rec, const int64_t *__restrict__ off, int n_events,
-                const float *__restrict__ wire_pos_f, const or_rt_table_t *__restrict__ rt, or_hits_view_t hv) {
+                const float *__restrict__ wire_pos_f, const or_rt_table_t *__restrict__ rt, or_hits_view_t hv,
+                uint32_t *__restrict__ errw) {
     __shared__ int cnt[PK_WARPS][64];
     __shared__ int start[PK_WARPS][64];
     const int w = threadIdx.x >> 5;
@@ -98,8 +102,13 @@ __global__ void __launch_bounds__(PK_WARPS * 32)
             else
                 hv.nhits_prop[e * OR_NPROP + d - OR_NCHAM - OR_NHODO - 1] = (uint32_t)min(n, OR_MAXHITS_PROP);
         }
+        bool unsorted = false;
         for (int r = lane; r < nrec; r += 32) {
             const or_hit_record_t h = rec[r0 + r];
+            if (r > 0) {
+                const or_hit_record_t q = rec[r0 + r - 1];
+                unsorted |= h.det < q.det || (h.det == q.det && (h.elem < q.elem || (h.elem == q.elem && h.tdc < q.tdc)));
+            }
             const int d = h.det;
             if (d < 1 || d >= OR_NDET) continue;
             const int k = r - start[w][d];
@@ -117,7 +126,7 @@ __global__ void __launch_bounds__(PK_WARPS * 32)
                 cap = OR_MAXHITS_PROP;
             }
             const int n = min(cnt[w][d], cap);
-            if (k >= n) continue;
+            if (k < 0 || k >= n) continue;  // k < 0 only for records out of order
             const int el = h.elem;
             const float pos = (el >= 0 && el < OR_WIREPOS_STRIDE) ? wire_pos_f[d * OR_WIREPOS_STRIDE + el] : 0.f;
             slot[k] = (float)el;
@@ -126,6 +135,7 @@ __global__ void __launch_bounds__(PK_WARPS * 32)
             slot[3 * n + k] = (float)h.flag;
             slot[4 * n + k] = (RT && rt_plane(d)) ? rt_drift(rt, d, h.tdc, h.drift) : h.drift;
         }
+        if (__any_sync(0xffffffffu, unsorted) && lane == 0) atomicOr(errw, ERRW_INPUT);
         __syncwarp();
     }
 }
@@ -162,13 +172,14 @@ static long pack_blocks(int n_events, int sm_count) {
 }
 
 cudaError_t launch_pack(const or_hit_record_t *rec, const int64_t *off, int n_events, const float *wire_pos_f,
-                        const or_rt_table_t *rt, or_hits_view_t hv, cudaStream_t stream, int sm_count) {
+                        const or_rt_table_t *rt, or_hits_view_t hv, uint32_t *errw, cudaStream_t stream,
+                        int sm_count) {
     if (n_events <= 0) return cudaSuccess;
     const unsigned blocks = (unsigned)pack_blocks(n_events, sm_count);
     if (rt)
-        pack_kernel<true><<<blocks, PK_WARPS * 32, 0, stream>>>(rec, off, n_events, wire_pos_f, rt, hv);
+        pack_kernel<true><<<blocks, PK_WARPS * 32, 0, stream>>>(rec, off, n_events, wire_pos_f, rt, hv, errw);
     else
-        pack_kernel<false><<<blocks, PK_WARPS * 32, 0, stream>>>(rec, off, n_events, wire_pos_f, nullptr, hv);
+        pack_kernel<false><<<blocks, PK_WARPS * 32, 0, stream>>>(rec, off, n_events, wire_pos_f, nullptr, hv, errw);
     return cudaGetLastError();
 }
 

@@ -143,7 +143,33 @@ struct YzBest {
     int pad;
 };
 
+// The first y fit of a combination (fit_2D_track over its accepted u/v hits,
+// K:1602, AM:32-74) weighs every hit by its plane's error (calculate_y_uvhit,
+// H:98: resolution * |dp_y / dp_x|) at its plane's z, so the normal matrix,
+// its inverse and the parameter errors depend only on which of the eight
+// planes (u3 u3' v3 v3' u2 u2' v2 v2', added in that order) gave a hit.  The
+// fit needs at least one hit in each of the four projections: 3^4 = 81 plane
+// sets per station-3 half.  yz_tab_kernel computes each entry with the same
+// operations in the same order as the per-combination fit did (Fit2 then
+// matinv_2x2 and sqrtf), so a combination's fit keeps only the right-hand
+// side (B0, B1) and two dot products, bit for bit the same result.
+constexpr int YZ_TAB_SETS = 81;
+struct __align__(16) YzTab {
+    float ai0, ai1, ai2, ai3;  // inverse of the normal matrix
+    float thr_y0, thr_ty;      // Y0_MAX + 2 err_y0, TY_MAX + 2 err_ty (the first cut, K:1611)
+    float ey0, ety;            // err_y0, err_ty
+};
+static_assert(sizeof(YzTab) == 32, "YzTab is two 16-byte words");
+constexpr size_t YZ_TAB_BYTES = (2 * YZ_TAB_SETS * sizeof(YzTab) + 255) & ~size_t(255);
+
+// index of a plane set: group values g = (second plane << 1 | first plane)
+// in 1..3 for u3, v3, u2, v2
+__device__ __forceinline__ int yz_tab_index(int gu3, int gv3, int gu2, int gv2) {
+    return ((gu3 - 1) * 3 + (gv3 - 1)) * 9 + (gu2 - 1) * 3 + (gv2 - 1);
+}
+
 struct YzScratch {
+    const YzTab *tab;        // 2 x YZ_TAB_SETS entries: station-3 half 0 (D3p) then 1 (D3m)
     YzUnit *units;
     YzHeavy *heavy;
     YzBest *best;
@@ -836,8 +862,8 @@ __device__ __forceinline__ int next_alive_outer(const YzAlive &m, int nu3, int i
 
 template <bool FIRST_ONLY>
 __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l, long c1l,
-                                         Stale st[4], const or_plane_t &P, PassEntryStore *Q, int qcap,
-                                         int *nsurv) {
+                                         Stale st[4], const or_plane_t &P, const YzTab *__restrict__ tab,
+                                         PassEntryStore *Q, int qcap, int *nsurv) {
     const int lane = lane_id();
     const int nu2 = S.np[0], nu3 = S.np[2];
     const int C2 = S.np[0] * S.np[1];
@@ -867,10 +893,12 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
     }
     const YzAlive alive = yz_alive(S, base);
     // station-3 part of the lane's current outer iteration (iu3, iv3): the
-    // fit sums over its accepted hits in the reference order, their count,
-    // and whether both u3 and v3 gave one (K:1326-1390); recomputed only
-    // when the outer digits move.
-    Fit2 f3;
+    // fit's right-hand side over its accepted hits in the reference order,
+    // their count, the table offset of its plane set, and whether both u3
+    // and v3 gave one (K:1326-1390); recomputed only when the outer digits
+    // move.
+    float b0_3 = 0.f, b1_3 = 0.f;
+    int tab3 = 0;
     int n3 = 0;
     bool alive3 = false, need3 = true;
     int basec = c0;
@@ -913,8 +941,9 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
                         ((unsigned long long)(pu.y >= 0 ? S.woff[5] + pu.y : 0xFFFF) << 16) |
                         ((unsigned long long)(pv.x >= 0 ? S.woff[6] + pv.x : 0xFFFF) << 32) |
                         ((unsigned long long)(pv.y >= 0 ? S.woff[7] + pv.y : 0xFFFF) << 48);
-                    Fit2 f;
-                    int nu = 0, nv = 0;
+                    // B0 += w*y, B1 += w*y*z per accepted hit, as Fit2::add
+                    float b0 = 0.f, b1 = 0.f;
+                    int nu = 0, nv = 0, gu = 0, gv = 0;
 #pragma unroll 1
                     for (int a = 0; a < 4; ++a) {
                         if (a == 2 && nu == 0) break;  // no u3 hit: v3 is not loaded
@@ -922,12 +951,22 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
                         if (off == 0xFFFF) continue;
                         const YzHit &r = base[off];
                         if (!r.acc) continue;
-                        f.add(r.Y, r.z, r.eY);
-                        if (a < 2) ++nu; else ++nv;
+                        const float t = r.eY * r.Y;
+                        b0 += t;
+                        b1 += t * r.z;
+                        if (a < 2) {
+                            ++nu;
+                            gu |= 1 << a;
+                        } else {
+                            ++nv;
+                            gv |= 1 << (a - 2);
+                        }
                     }
-                    f3 = f;
+                    b0_3 = b0;
+                    b1_3 = b1;
                     n3 = nu + nv;
                     alive3 = nu > 0 && nv > 0;
+                    tab3 = alive3 ? yz_tab_index(gu, gv, 1, 1) : 0;
                     need3 = false;
                 }
                 if (alive3) {
@@ -935,10 +974,11 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
                     // every attempted hit writes the scratch entry at the
                     // running count (4..7 at most: n3 <= 4, four attempts),
                     // accepted ones enter the fit
-                    Fit2 f = f3;
+                    float b0 = b0_3, b1 = b1_3;
+                    int g2 = 0;  // plane bits u2 u2' v2 v2' of the accepted hits
                     nuv = n3;
                     const short2 pu = S.pair[0][d0];
-                    auto attempt = [&](int off) {
+                    auto attempt = [&](int off, int a) {
                         const YzHit &r = base[off];
                         const int k = nuv - 4;
                         if (k >= 0) {
@@ -947,7 +987,10 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
                             wmask |= 1u << k;
                         }
                         if (r.acc) {
-                            f.add(r.Y, r.z, r.eY);
+                            const float t = r.eY * r.Y;
+                            b0 += t;
+                            b1 += t * r.z;
+                            g2 |= 1 << a;
                             ++nuv;
                         }
                     };
@@ -967,11 +1010,25 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
                             if (nu2hits == n3) break;  // the u2 group gave no hit
                         }
                         const int off = (int)((offs >> (16 * a)) & 0xFFFFull);
-                        if (off != 0xFFFF) attempt(off);
+                        if (off != 0xFFFF) attempt(off, a);
                     }
                     if (nu2hits > n3 && nuv > nu2hits) {  // the v2 group gave a hit: the fit is reached
-                        f.solve(y0, ty, ey0, ety);
-                        pass1 = !(fabsf(y0) > Y0_MAX + 2 * ey0 || fabsf(ty) > TY_MAX + 2 * ety);
+                        // Fit2::solve with the plane set's tabulated inverse
+                        const YzTab *te = tab + tab3 + (g2 & 3) * 3 - 4 + (g2 >> 2);
+                        const float4 ai = __ldg(reinterpret_cast<const float4 *>(te));
+                        const float2 thr = __ldg(reinterpret_cast<const float2 *>(&te->thr_y0));
+                        y0 = 0.0f;
+                        y0 += ai.x * b0;
+                        y0 += ai.y * b1;
+                        ty = 0.0f;
+                        ty += ai.z * b0;
+                        ty += ai.w * b1;
+                        pass1 = !(fabsf(y0) > thr.x || fabsf(ty) > thr.y);
+                        if (pass1) {
+                            const float2 er = __ldg(reinterpret_cast<const float2 *>(&te->ey0));
+                            ey0 = er.x;
+                            ety = er.y;
+                        }
                     }
 
                 }
@@ -1062,9 +1119,9 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
 }
 
 __device__ __forceinline__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l,
-                                                      long c1l, Stale st[4], const or_plane_t &P, PassEntryStore *Q,
-                                                      int qcap) {
-    return yz_range_t<false>(S, E, base, c0l, c1l, st, P, Q, qcap, nullptr);
+                                                      long c1l, Stale st[4], const or_plane_t &P,
+                                                      const YzTab *tab, PassEntryStore *Q, int qcap) {
+    return yz_range_t<false>(S, E, base, c0l, c1l, st, P, tab, Q, qcap, nullptr);
 }
 
 // write the best combination into the track record (K:1804-1825)
@@ -1214,7 +1271,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_PLAN_WARPS_SM / W > 0 ? OR_YZ_P
                 }
                 if (inline_it) {
                     budget -= Cl;
-                    const unsigned long long bk = yz_range(S, E, base, 0, C, st, P, Q, sc.qcap);
+                    const unsigned long long bk =
+                        yz_range(S, E, base, 0, C, st, P, sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap);
                     __syncwarp();
                     if (bk != ~0ull) yz_store(T, S.b, S.nhx);
                 }
@@ -1262,7 +1320,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_
         for (int k = 0; k < 4; ++k) st[k] = un.entry[k];
         __syncwarp();
         const long C2 = (long)S.np[0] * S.np[1];
-        const unsigned long long bk = yz_range(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, Q, sc.qcap);
+        const unsigned long long bk = yz_range(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P,
+                                               sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap);
         __syncwarp();
         YzBest *dst = sc.best + u;
         if (bk == ~0ull) {
@@ -1321,7 +1380,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_FIRST_WARPS_SM / W > 0 ? OR_YZ_
         __syncwarp();
         const long C2 = (long)S.np[0] * S.np[1];
         int ns = -1;
-        yz_range_t<true>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, Q, sc.qcap, &ns);
+        yz_range_t<true>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, sc.tab + YZ_TAB_SETS * (st3 - 3), Q,
+                         sc.qcap, &ns);
         __syncwarp();
         long long off = -1;
         if (lane == 0 && ns >= 0) {
@@ -1388,7 +1448,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_SECOND_WARPS_SM / W > 0 ? OR_YZ
 #pragma unroll 1
             for (int k = 0; k < 4; ++k) st[k] = un.entry[k];
             __syncwarp();
-            bk = yz_range(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, Q, sc.qcap);
+            bk = yz_range(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, sc.tab + YZ_TAB_SETS * (st3 - 3), Q,
+                          sc.qcap);
         } else {
             Phase2Carry cs;
 #pragma unroll 1
@@ -1447,6 +1508,41 @@ __global__ void __launch_bounds__(128) yz_apply_kernel(or_tracks_view_t tv, YzSc
     }
 }
 
+// The 2 x 81 plane-set entries of the first y fit (see YzTab): for every
+// set, Fit2's normal matrix accumulated over the set's planes in the order
+// u3 u3' v3 v3' u2 u2' v2 v2' with the plane's weight and z, then
+// matinv_2x2 and the errors as in Fit2::solve, and the first cut's bounds.
+__global__ void __launch_bounds__(256) yz_tab_kernel(const or_plane_t *__restrict__ gplane, YzTab *__restrict__ tab) {
+    const int t = threadIdx.x;
+    if (t >= 2 * YZ_TAB_SETS) return;
+    const or_plane_t &P = *gplane;
+    const int st3 = 3 + t / YZ_TAB_SETS;
+    const int i = t % YZ_TAB_SETS;
+    const int g[4] = {i / 27 + 1, (i / 9) % 3 + 1, (i / 3) % 3 + 1, i % 3 + 1};  // u3 v3 u2 v2
+    const int det[8] = {det_u3(st3), det_u3(st3) - 1, det_v3(st3), det_v3(st3) - 1, DET_U2, DET_UP2, DET_V2, DET_VP2};
+    Fit2 f;
+#pragma unroll 1
+    for (int k = 0; k < 8; ++k) {
+        if (!((g[k >> 1] >> (k & 1)) & 1)) continue;
+        const int d = det[k];
+        const float w = P.resolution[d] * fabsf(P.deltapy[d] / P.deltapx[d]);  // calculate_y_uvhit's err_y, H:98
+        f.add(0.f, P.z[d], w);
+    }
+    const float A[4] = {f.A0, f.A1, f.A2, f.A3};
+    float Ai[4];
+    matinv_2x2(A, Ai);
+    YzTab e;
+    e.ai0 = Ai[0];
+    e.ai1 = Ai[1];
+    e.ai2 = Ai[2];
+    e.ai3 = Ai[3];
+    e.ey0 = sqrtf(fabsf(Ai[0]));
+    e.ety = sqrtf(fabsf(Ai[3]));
+    e.thr_y0 = Y0_MAX + 2 * e.ey0;
+    e.thr_ty = TY_MAX + 2 * e.ety;
+    tab[t] = e;
+}
+
 size_t yz_smem_bytes(int warps) {
     return ((sizeof(or_plane_t) + 15) & ~size_t(15)) + sizeof(YzWarp) * (size_t)warps;
 }
@@ -1456,7 +1552,8 @@ size_t yz_smem_bytes(int warps) {
 static long long yz_pool_cap(int qcap) { return (OR_YZ_SPLIT && qcap == YZ_QCAP_CTX) ? YZ_POOL_CAP : 0; }
 
 size_t yz_scratch_bytes_q(int cap_units, int cap_heavy, int garena_warps, int qcap) {
-    size_t b = 256 + (sizeof(YzUnit) + sizeof(YzBest)) * (size_t)cap_units + sizeof(YzHeavy) * (size_t)cap_heavy;
+    size_t b = 256 + YZ_TAB_BYTES + (sizeof(YzUnit) + sizeof(YzBest)) * (size_t)cap_units +
+               sizeof(YzHeavy) * (size_t)cap_heavy;
     b = (b + 255) & ~size_t(255);
     b += sizeof(YzHit) * YZ_GARENA_HITS * (size_t)garena_warps;
     b += sizeof(PassEntryStore) * (size_t)qcap * (size_t)garena_warps;
@@ -1495,6 +1592,9 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
     YzScratch sc;
     sc.counters = reinterpret_cast<unsigned int *>(p);
     p += 256;
+    YzTab *tab = reinterpret_cast<YzTab *>(p);
+    sc.tab = tab;
+    p += YZ_TAB_BYTES;
     sc.units = reinterpret_cast<YzUnit *>(p);
     p += sizeof(YzUnit) * (size_t)cap_units;
     sc.best = reinterpret_cast<YzBest *>(p);
@@ -1522,6 +1622,8 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
     sc.garena_warps = garena_warps;
     sc.qcap = qcap;
     if ((err = cudaMemsetAsync(sc.counters, 0, 256, stream))) return err;
+    yz_tab_kernel<<<1, 256, 0, stream>>>(d_plane, tab);
+    if ((err = cudaGetLastError())) return err;
     const long blocks = garena_warps / W;
     const long blocks_plan = min(((long)n_events * (OR_NSLOTS / YZ_PLAN_CHUNK) + W - 1) / W, blocks);
     yz_plan_kernel<W><<<(unsigned)blocks_plan, W * 32, smem, stream>>>(d_plane, hv, tv, toomany, n_events, sc, errw,

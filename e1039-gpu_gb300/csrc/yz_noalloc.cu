@@ -1,12 +1,13 @@
 // yz_noalloc.cu -- the YZ tracklet stage on a statically reserved scratch area.
 //
-// or_yz() runs on the work queue that or_create() allocates (about 390 MB on
-// a 152-SM GPU).  Some callers cannot allocate device memory when they call:
-// a trigger or serving process that hands all free HBM to its own pool at
-// start-up, or a latency-critical loop that must not call cudaMalloc/cudaFree
-// (both synchronise the device).  or_yz_noalloc() serves them: it needs no
-// library context, allocates nothing, and runs the same plan/work/apply
-// kernels as or_yz() on a fixed area reserved in this file:
+// or_yz() runs on the scratch that or_create() allocates (about 7.9 GB: the
+// work queue, per-warp arenas and the survivor pool).  Some callers cannot
+// allocate device memory when they call: a trigger or serving process that
+// hands all free HBM to its own pool at start-up, or a latency-critical loop
+// that must not call cudaMalloc/cudaFree (both synchronise the device).
+// or_yz_noalloc() serves them: it needs no library context, allocates
+// nothing, and runs the same plan/work/apply kernels as or_yz() on a fixed
+// area reserved in this file:
 //
 //   - the area is a file-scope __device__ array of OR_YZ_NOALLOC_SCRATCH_BYTES
 //     (56 MiB), reserved by the CUDA runtime when this module is loaded on a
@@ -14,7 +15,11 @@
 //   - the first call on a device, with that device current, looks the
 //     array's address up once (cudaGetSymbolAddress) and caches it per
 //     device; later calls reuse it.  Make that first call before any stream
-//     capture;
+//     capture.  The cached address is that of the device's context at the
+//     first call: cudaDeviceReset() reloads the module, the array may move,
+//     and later calls on that device would use a stale address, so a
+//     process that resets a device must not call or_yz_noalloc() on it
+//     again;
 //   - a call takes at most OR_YZ_NOALLOC_MAX_EVENTS events; larger batches are
 //     rejected with OR_ERR_CAPACITY before anything is launched;
 //   - the queue counters, the only part that must start at zero, are cleared
@@ -23,10 +28,11 @@
 //     streams, or two host threads) race on it and corrupt each other's
 //     results.  Serialise them.
 //
-// The queue is smaller than or_yz()'s (65,536 units of 4,096 combinations,
-// 16,384 heavy tracklets, 1,216 work warps).  A tracklet that finds the queue
-// full is evaluated by its planning warp instead, so the results are the same
-// as or_yz()'s for every batch; only the time changes.
+// The queue is smaller than or_yz()'s (65,536 units and 16,384 heavy
+// tracklets against a context's 4 Mi and 2 Mi; 1,216 work warps).  A
+// tracklet that finds the queue full is evaluated by its planning warp
+// instead, so the results are the same as or_yz()'s for every batch; only the
+// time changes.
 #include <mutex>
 
 #include "../../include/or_gb300.h"
@@ -56,15 +62,16 @@ DeviceScratch g_dev[NOALLOC_MAX_DEVICES];
 }  // namespace
 
 // Look the static area up on the current device (first call only).
-// Returns the cudaError_t of the failing call, or cudaErrorInvalidValue with
-// *why set when the device index or the area's size does not fit.
+// Returns the cudaError_t of the failing call; cudaErrorInvalidDevice with
+// *why set when the device index is above the per-device table, and
+// cudaErrorInvalidValue with *why set when the area is smaller than the queue.
 cudaError_t yz_noalloc_scratch(int *device, DeviceScratch **out, const char **why) {
     *why = nullptr;
     cudaError_t e = cudaGetDevice(device);
     if (e != cudaSuccess) return e;
     if (*device < 0 || *device >= NOALLOC_MAX_DEVICES) {
-        *why = "device index above the static scratch table";
-        return cudaErrorInvalidValue;
+        *why = "device index above the static scratch table (64 devices)";
+        return cudaErrorInvalidDevice;
     }
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     DeviceScratch &d = g_dev[*device];

@@ -23,7 +23,7 @@ EXPORTS = ("or_version", "or_last_error", "or_status_string", "or_geometry_load"
            "or_mlp_adam", "or_prop_matching", "or_global_clean", "or_run_selection", "or_set_launch",
            "or_get_launch", "or_vertexing", "or_dimuons", "or_fill_histograms", "or_hist_table_init",
            "or_run_physics", "or_output_rows", "or_rt_load", "or_rt_set_plane", "or_rt_table_bytes",
-           "or_pack_hits_rt", "or_rt_apply", "or_set_yz_pool_limit")
+           "or_pack_hits_rt", "or_rt_apply", "or_set_yz_pool_limit", "or_selftest_bounded_wait")
 
 # tunable kernels (or_kernel_id_t)
 KERNELS = {"event_reduce": 0, "xz": 1, "yz": 2, "back_clean": 3, "global": 4, "select": 5, "features": 6}
@@ -77,6 +77,7 @@ def lib():
     lb.or_pack_hits.argtypes = [vp, vp, vp, C.c_int, vp, L.OrHitsView, vp]
     lb.or_collect_tracks.argtypes = [vp, L.OrTracksView, vp, C.c_int, C.c_float, vp, C.c_int64, vp, vp]
     lb.or_yz_noalloc.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, C.c_int, vp, vp]
+    lb.or_selftest_bounded_wait.argtypes = [vp, C.c_int, vp]
     i64, f32, i32 = C.c_int64, C.c_float, C.c_int
     lb.or_tracklet_rows.argtypes = [vp, L.OrTracksView, vp, i32, vp, vp]
     lb.or_tracklet_features.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, i32, vp, vp, i64, vp]

@@ -100,9 +100,19 @@ int or_set_geometry(or_ctx_t *ctx, const or_plane_t *plane);
  * last call: OR_ERR_TIMEOUT when a bounded bulk-copy wait gave up,
  * OR_ERR_CAPACITY when a hit window overflowed its fixed list (100 windowed
  * hits or pairs per projection in YZ, 128 pairs in global tracking; that
- * tracklet or track is left unextended).  The reference has no such report;
- * its kernels write past their arrays instead. */
+ * tracklet or track is left unextended), OR_ERR_ARG when the packer met an
+ * event whose hit records are not sorted by (det, elem, tdc).  The error
+ * words are cleared by the call.  The reference has no such report; its
+ * kernels write past their arrays instead, and its host aborts on CUDA
+ * errors (online_reconstruction.cu:50-64). */
 int or_stream_sync(or_ctx_t *ctx, void *stream);
+/* Self-test of the bounded device waits: launches one warp that waits on a
+ * shared-memory mbarrier nothing arrives at (no bulk copy targets it) for at
+ * most `polls` polls (1..1000000).  The wait runs out and raises the same
+ * error word as a bulk-copy wait of the event reducer that gave up, so the
+ * next or_stream_sync() returns OR_ERR_TIMEOUT; the context stays usable.
+ * No counterpart in the reference, which has no bounded waits. */
+int or_selftest_bounded_wait(or_ctx_t *ctx, int polls, void *stream);
 
 /* Stage entry points on device buffers (see the table above). */
 int or_event_reduce(or_ctx_t *ctx, or_hits_view_t hits, uint8_t *toomany, int n_events, void *stream);
@@ -181,7 +191,12 @@ size_t or_tracks_view_bytes(int n_events);
  * sorted by (det, elem, tdc) inside each event, into the reference hit
  * layout, with pos = (float)wire_pos[det][elem] (online_reconstruction.cu
  * :589-636).  rec_offsets[e]..rec_offsets[e+1] are event e's records.
- * wire_pos_f is a device float table [OR_NDET*OR_WIREPOS_STRIDE]. */
+ * wire_pos_f is a device float table [OR_NDET*OR_WIREPOS_STRIDE].  Records
+ * with det outside 1..54 (they sort first or last) are skipped, an elem
+ * outside the wire table gives pos 0, and hits past a plane's slot capacity
+ * are dropped.  An event whose records are out of order is reported by the
+ * next or_stream_sync() as OR_ERR_ARG; its slots are then undefined, but no
+ * write leaves them. */
 int or_pack_hits(or_ctx_t *ctx, const or_hit_record_t *records, const int64_t *rec_offsets, int n_events,
                  const float *wire_pos_f, or_hits_view_t hits, void *stream);
 
@@ -282,7 +297,7 @@ int or_mlp_adam(or_ctx_t *ctx, float *param, float *m1, float *m2, const float *
  *
  * It is for callers that cannot allocate device memory when they call: a
  * trigger or serving process that gives all free HBM to its own pool at
- * start-up (or_create() would need about 390 MB for or_yz()'s work queue), or
+ * start-up (or_create() would need about 7.9 GB for its YZ scratch), or
  * a latency-critical loop that must not call cudaMalloc/cudaFree because they
  * synchronise the device.  Results are those of or_yz() on the same buffers.
  *
@@ -298,12 +313,23 @@ int or_mlp_adam(or_ctx_t *ctx, float *param, float *m1, float *m2, const float *
  * reserved by the CUDA runtime when the library's module is loaded.  The
  * first call on a device, with that device current, looks its address up
  * (cudaGetSymbolAddress) and caches it: make that first call before any
- * stream capture.  Each call clears the queue counters on `stream`.
+ * stream capture.  The cached address belongs to the device's context of
+ * that moment: after cudaDeviceReset() the module is loaded again and the
+ * array may move, so a process that resets a device must not call
+ * or_yz_noalloc() on it again.  Each call clears the queue counters on
+ * `stream`.
  * Calls that overlap on one device (several streams or host threads) share
  * the array and race: serialise them.
  *
  * n_events above OR_YZ_NOALLOC_MAX_EVENTS (the reference's batch, EstnEvtMax
- * in reconstruction_constants.h:20) returns OR_ERR_CAPACITY before any launch. */
+ * in reconstruction_constants.h:20) returns OR_ERR_CAPACITY before any launch;
+ * a current device whose index is above the library's per-device table
+ * (64 devices) returns OR_ERR_ARG.
+ *
+ * Its work queue is smaller than a context's (65,536 units and 16,384 heavy
+ * tracklets, against 4 Mi and 2 Mi): on large, busy batches a tracklet that
+ * finds the queue full is evaluated by its planning warp, which gives the
+ * same result more slowly. */
 #define OR_YZ_NOALLOC_MAX_EVENTS 10000
 #define OR_ERRW_CAPACITY 2u
 #define OR_YZ_NOALLOC_SCRATCH_BYTES (56u << 20)

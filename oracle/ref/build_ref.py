@@ -27,7 +27,10 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
-REF_SRC = os.environ.get("OR_REFERENCE_SRC", "/root/reference/OnlineReconstruction")
+# the reference tree: OR_REFERENCE_SRC, else a checkout named `reference`
+# beside this repository
+REF_SRC = os.environ.get("OR_REFERENCE_SRC",
+                         os.path.join(os.path.dirname(ORACLE), "..", "reference", "OnlineReconstruction"))
 WRAP = os.path.join(HERE, "ref_kernels.cu")
 VARIANTS = {"fmad0": ["-fmad=false"], "fmad1": []}
 

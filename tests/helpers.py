@@ -146,3 +146,59 @@ def output_rows_oracle(hits, tracks, dims, toomany, raw_hits=None, event_ids=Non
             "tracks": np.array(tr, f32).reshape(-1, L.OUT_TRACK_FIELDS),
             "track_hits": np.array(th, f32).reshape(-1, L.OUT_TRACKHIT_FIELDS),
             "dimuons": np.array(dr, f32).reshape(-1, L.OUT_DIMUON_FIELDS)}
+
+
+def device_mismatches(b, e0, hits, tracks, state):
+    """Compare events e0 .. e0 + hits.n of DeviceBatch `b` (after or_run_batch)
+    with the oracle's buffers of the same events (after run_all), on the
+    device.  Returns a dict of mismatch counts: hit lists per (event, plane)
+    over the occupied head of each slot, the HasTooManyHits flag, nTracklets,
+    slot counts and track records (all 148 floats, bitwise) of events the
+    oracle did not reject."""
+    import torch
+    dev = b.toomany.device
+    n = hits.n
+    e1 = e0 + n
+    out = {}
+
+    def up(a):
+        return torch.from_numpy(a.view(np.int32) if a.dtype == np.uint32 else a).to(dev)
+
+    for name, per, cap in (("cham", L.NCHAM, L.MAXHITS_CHAM), ("hodo", L.NHODO, L.MAXHITS_HODO),
+                           ("prop", L.NPROP, L.MAXHITS_PROP)):
+        dc = getattr(b, "nhits_" + name)[e0 * per:e1 * per]
+        oc = up(getattr(hits, "nhits_" + name))
+        w = L.NHITSPARAM * cap
+        dd = getattr(b, "hits_" + name)[e0 * per * w:e1 * per * w].view(torch.int32).view(-1, w)
+        od = up(getattr(hits, "hits_" + name)).view(torch.int32).view(-1, w)
+        head = torch.arange(w, device=dev)[None, :] < (L.NHITSPARAM * oc.long())[:, None]
+        bad_data = ((dd != od) & head).any(dim=1)
+        out["hit_count_" + name] = int((dc != oc).sum())
+        out["hit_data_" + name] = int((bad_data & (dc == oc)).sum())
+    flags = b.toomany[e0:e1].cpu().numpy()
+    out["toomany"] = int((flags != state.toomany).sum())
+    out["ntracklets"] = int((b.ntracklets[e0:e1].cpu().numpy() != state.ntracklets).sum())
+    keep = torch.from_numpy(state.toomany == 0).to(dev)
+    dn = b.ntracks[e0 * L.NSLOTS:e1 * L.NSLOTS].view(n, L.NSLOTS)
+    on = torch.from_numpy(tracks.ntracks.view(np.int16)).to(dev).view(n, L.NSLOTS)
+    out["slot_counts"] = int(((dn != on).any(dim=1) & keep).sum())
+    rec = L.NSLOTS * L.SLOTCAP * L.NTRKPARAM
+    dt = b.tracks[e0 * rec:e1 * rec].view(torch.int32).view(n, L.NSLOTS, L.SLOTCAP, L.NTRKPARAM)
+    ot = up(tracks.tracks).view(torch.int32).view(n, L.NSLOTS, L.SLOTCAP, L.NTRKPARAM)
+    valid = torch.arange(L.SLOTCAP, device=dev)[None, None, :] < on.long()[:, :, None]
+    valid &= keep[:, None, None]
+    out["track_records"] = int(((dt != ot).any(dim=3) & valid).sum())
+    out["tracks_compared"] = int(valid.sum())
+    out["global_tracks"] = int(((ot[..., L.TRK_STID] == int(np.float32(6).view(np.int32))) & valid).sum())
+    return out
+
+
+def oracle_chunk(plane, geo, rec, off, e0, e1, n_threads=0):
+    """The oracle's run_all on events e0..e1 of a record batch."""
+    r = rec[off[e0]:off[e1]]
+    o = (off[e0:e1 + 1] - off[e0]).astype(off.dtype)
+    h = S.pack(r, o, geo.wire_pos_f32())
+    t = L.HostTracks(e1 - e0)
+    st = O.OracleState(e1 - e0)
+    O.run_all(plane, h, t, st, n_threads)
+    return h, t, st

@@ -1,5 +1,16 @@
-"""The plain path at the benchmark's full size (100,000 uneven-noise events),
-through properties that do not need the oracle at that size:
+"""The plain path at the configurations' full sizes.
+
+Against the oracle, bit for bit (hit lists after the event reducer, the
+HasTooManyHits flag, nTracklets, slot counts, every track record):
+
+  - all 100,000 events of the uneven batch (seed 906002), run by one
+    or_run_batch call on the whole batch; the oracle runs in chunks of
+    5,000 events (events are independent), each chunk compared on the
+    device with its rows of the GPU batch;
+  - the small configuration at exactly its size: 1,000 one-dimuon events
+    with Poisson(150) noise, seed 906001.
+
+And through properties that do not need the oracle:
 
   - determinism: the same batch run twice gives the same buffers, bit for bit;
   - event independence: the batch run as four chunks gives, event by event,
@@ -12,8 +23,8 @@ through properties that do not need the oracle at that size:
     plain packer followed by the in-place conversion, bit for bit, and
     changes only the chamber and prop-tube drift fields.
 
-Bit-exactness against the oracle is tested on smaller batches
-(test_gpu_parity.py); this adds the full-size behaviour of the queue and
+Stage-by-stage parity (each stage fed the oracle's previous stage) is in
+test_gpu_parity.py; this file adds the full-size behaviour of the queue and
 the scratch limits.
 """
 import numpy as np
@@ -49,6 +60,57 @@ def _run(plane, geo, rec, off):
     rc.sync()
     t = b.download_tracks()
     return t.ntracks.reshape(n, -1).copy(), t.tracks.reshape(n, -1).copy(), b.toomany.cpu().numpy().copy()
+
+
+def _run_device(plane, geo, rec, off):
+    """or_run_batch on the whole batch; the DeviceBatch stays on the device."""
+    import torch
+    from orgpu import pipeline
+    n = len(off) - 1
+    rc = pipeline.Reconstruction(plane, 0)
+    b = pipeline.DeviceBatch(n)
+    rc.pack(b, torch.from_numpy(rec.view(np.uint8)).cuda(), torch.from_numpy(off).cuda(),
+            torch.from_numpy(geo.wire_pos_f32().reshape(-1)).cuda())
+    rc.run_batch(b)
+    rc.sync()
+    return b
+
+
+def _assert_oracle_equal(plane, geo, rec, off, chunk):
+    from helpers import device_mismatches, oracle_chunk
+    n = len(off) - 1
+    b = _run_device(plane, geo, rec, off)
+    total = {}
+    for e0 in range(0, n, chunk):
+        e1 = min(n, e0 + chunk)
+        h, t, st = oracle_chunk(plane, geo, rec, off, e0, e1)
+        m = device_mismatches(b, e0, h, t, st)
+        for k, v in m.items():
+            total[k] = total.get(k, 0) + v
+        bad = {k: v for k, v in m.items() if v and k not in ("tracks_compared", "global_tracks")}
+        assert not bad, f"events {e0}..{e1}: {bad}"
+    return total
+
+
+def test_full_batch_bit_exact_with_oracle(full):
+    plane, geo, rec, off = full
+    total = _assert_oracle_equal(plane, geo, rec, off, 5000)
+    assert total["global_tracks"] > 100000
+    print("uneven batch, 100,000 events:", total)
+
+
+def test_small_config_1000_events_bit_exact_with_oracle(geometry):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from orgpu import synth as S
+    plane, wp = geometry
+    geo = S.Geometry(plane, wp)
+    rec, off, _ = S.generate(geo, S.config_small(1000, 906001))
+    rec, off = S.cap_records(rec, off)
+    total = _assert_oracle_equal(plane, geo, rec, off, 1000)
+    assert total["global_tracks"] > 1000
+    print("small configuration, 1,000 events:", total)
 
 
 def _valid_tracks(nt, tr):
