@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-rt", action="store_true", help="skip the R-T calibration packer leg")
+    ap.add_argument("--no-config4", action="store_true", help="skip the high-occupancy leg")
     return ap.parse_args()
 
 
@@ -240,6 +241,13 @@ def main():
     barrier()
     clk = clocks.stop()
     rc.sync()
+    # the YZ work of a step (every step runs the same batch): counted on one
+    # more, untimed step, so that the timed ones run without the counters
+    rc.set_yz_work_counting(True)
+    step()
+    rc.sync()
+    yz_counts = rc.yz_work_counts()
+    rc.set_yz_work_counting(False)
     ms = t_start.elapsed_time(t_end) / args.steps
     for evs in all_evs:
         for k, s in enumerate(stages):
@@ -320,7 +328,7 @@ def main():
     if rank != 0:
         return
 
-    # ---- roofline of the dominant kernel -------------------------------------
+    # ---- roofline of the dominant stage (YZ) and of the event reducer --------
     peaks = {}
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
@@ -329,29 +337,24 @@ def main():
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    prof = profile_figures()
+    dominant = max(stage_ms, key=stage_ms.get)
+    roofline = yz_roofline(yz_counts, stage_ms["yz"], n, clk, dev, prof)
+    roofline["dominant_stage"] = "%s (%.2f of %.2f ms per step)" % (dominant, stage_ms[dominant], ms)
     # event reducer: algorithmic bytes = 20 B per raw hit read + 20 B per kept
     # hit written + 48 counts read and written + the flag, per event
-    ev = np.repeat(np.arange(n), np.diff(off))
     path_det = np.isin(rec["det"], np.array(L.PATH_PLANES))
     raw = int(path_det.sum())
     kept = int(cnt["cham"].reshape(n, L.NCHAM)[:, [d - 1 for d in L.EFF_DETID_CHAMBERS]].sum() +
                cnt["hodo"].sum() + cnt["prop"].sum())
     er_bytes = 20 * raw + 20 * kept + n * (48 * 8 + 1)
-    dominant = max(stage_ms, key=stage_ms.get)
     er_gbs = er_bytes / (stage_ms["event_reduce"] / 1000.0) / 1e9
-    traffic = None
-    try:
-        with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get("event_reduce_bytes_per_event")
-            traffic = traffic * n if traffic else None
-    except (OSError, ValueError):
-        traffic = None
-    roofline = {"bound": "hbm", "kernel": "er_kernel (event reducer)", "achieved": er_gbs, "peak": hbm_peak,
-                "unit": "GB/s", "frac": er_gbs / hbm_peak, "traffic": traffic,
-                "peak_source": peak_src,
-                "algorithmic_bytes_per_launch": er_bytes,
-                "note": "dominant stage is %s (%.2f ms of %.2f ms); its bound is FP32/INT issue, not HBM or "
-                        "tensor -- see stage_ms and profiles/" % (dominant, stage_ms[dominant], ms)}
+    er_prof = prof.get("kernels", {}).get("er_kernel", {})
+    er_traffic = er_prof.get("dram_bytes_per_event")
+    roofline_er = {"bound": "hbm", "kernel": "er_kernel (event reducer)", "achieved": er_gbs, "peak": hbm_peak,
+                   "unit": "GB/s", "frac": er_gbs / hbm_peak, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
+                   "traffic": None if er_traffic is None else er_traffic * n,
+                   "traffic_source": prof.get("source"), "algorithmic_bytes_per_launch": er_bytes}
 
     # ---- CPU baseline ---------------------------------------------------------
     cpu = None
@@ -363,6 +366,7 @@ def main():
 
     rt_res = None if args.no_rt else rt_leg(args, rc, b, plane, rec, d_rec, d_off, d_wp, dev)
     learned_res = None if args.no_learned else learned_leg(args, rc, b, rec, off, d_rec, d_off, d_wp, value, dev)
+    config4_res = None if args.no_config4 else config4_leg(args, rc, b, plane, wp, dev, with_learned=not args.no_learned)
     serving_res = None if args.no_serving else serving_leg(plane, wp, tuned)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -372,14 +376,71 @@ def main():
                     "d2h_bytes_per_step": int(statistics.mean(d2h_bytes)) if d2h_bytes else 0,
                     "copies": "records H2D double-buffered (the next step's during this step's compute), "
                               "result D2H each step after its compute"},
-            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "roofline": roofline, "roofline_event_reducer": roofline_er, "cpu_baseline": cpu, "clocks": clk,
             "gpu_launches": LAUNCHES_PER_STEP * args.steps,
             "stage_ms": stage_ms,
             "events_rejected_frac": float(toomany.mean()), "global_tracks_last_step": ntrk,
-            "learned": learned_res, "serving": serving_res, "rt_calibration": rt_res,
+            "learned": learned_res, "serving": serving_res, "rt_calibration": rt_res, "config4": config4_res,
             "autotune": None if tuned is None else {"events_per_cta": tuned["best"], "sample_events": tuned["events"],
                                                     "stage_ms_by_shape": tuned["ms"]}}
     print(json.dumps(line))
+
+
+def opcounts():
+    """The frozen per-unit FP32 operation counts (include/or_opcount.h)."""
+    import re
+    with open(os.path.join(REPO, "include", "or_opcount.h")) as f:
+        return {m.group(1): int(m.group(2)) for m in re.finditer(r"#define (OR_OPS_[A-Z0-9_]+) (\d+)", f.read())}
+
+
+def profile_figures():
+    """Per-kernel figures of the committed ncu captures (profiles/traffic.json):
+    DRAM bytes per event, issue activity, tensor-pipe activity."""
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def yz_roofline(counts, yz_ms, n, clk, dev, prof, nx=4):
+    """The YZ stage (the dominant one) against the FP32 issue peak: the
+    algorithmic FP32 operations of its combinations (frozen counts of
+    include/or_opcount.h times the device work counters of the step) per
+    second.  The stage is bound by instruction issue on the FP32/INT pipes,
+    not by HBM or the tensor cores, so the measured issue activity of its
+    kernels (ncu) is given beside it."""
+    import torch
+    ops = opcounts()
+    fitted, hitsum, surv = counts
+    n_avg = hitsum / fitted if fitted else 0.0
+    first = fitted * (ops["OR_OPS_FIT_FIXED"] + ops["OR_OPS_YZ_CUT1"]) + hitsum * (ops["OR_OPS_CALC_Y"] +
+                                                                                  ops["OR_OPS_FIT_POINT"])
+    per_surv = ((n_avg / 2) * ops["OR_OPS_LR_PAIR"] + n_avg * ops["OR_OPS_LR_SINGLE"] +
+                n_avg * ops["OR_OPS_FIT_POINT"] + ops["OR_OPS_FIT_FIXED"] + ops["OR_OPS_YZ_CUT2"] +
+                ops["OR_OPS_PROP_MATCH"] + ops["OR_OPS_HODO_MATCH"] + (n_avg + nx) * ops["OR_OPS_CHI2_HIT"])
+    total = first + surv * per_surv
+    secs = yz_ms / 1000.0
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = clk.get("sm_max_mhz") or 2070.0
+    peak = sms * 128 * 2 * mhz * 1e6 / 1e12  # FP32 lanes x (FMA = 2 flops) x clock
+    achieved = total / secs / 1e12
+    kp = prof.get("kernels", {})
+    yz_k = ("yz_plan_kernel", "yz_first_kernel", "yz_second_kernel")
+    per_ev = [kp.get(k, {}).get("dram_bytes_per_event") for k in yz_k]
+    return {"bound": "issue (FP32/INT pipes; neither HBM nor tensor)",
+            "kernel": "YZ stage: yz_tab, yz_plan, yz_first, yz_second, yz_apply kernels",
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_source": "nominal FP32 non-tensor peak: %d SMs x 128 lanes x 2 (FMA) x %.0f MHz" % (sms, mhz),
+            "traffic": None if None in per_ev else sum(per_ev) * n,
+            "traffic_source": prof.get("source"),
+            "algorithmic_flops_per_launch": total,
+            "fitted_combinations": fitted, "first_cut_survivors": surv, "mean_uv_hits": n_avg,
+            "fitted_combinations_per_s": fitted / secs, "survivors_per_s": surv / secs,
+            "flops_per_fitted_combination": (first / fitted) if fitted else None,
+            "flops_per_survivor": per_surv, "x_hits_assumed": nx,
+            "issue_active_ncu": {k: kp.get(k, {}).get("issue_active") for k in yz_k},
+            "op_counts": "include/or_opcount.h"}
 
 
 # kernels one step launches: pack, event reducer, XZ, YZ fit table / plan /
@@ -460,17 +521,97 @@ def learned_leg(args, rc, b_plain, rec, off, d_rec, d_off, d_wp, plain_value, de
             "model": "e1039-gpu_gb300/data/scorer_e906.npz", "t_keep": sp.t_keep, "t_unc": sp.t_unc}
 
 
+def config4_leg(args, rc, b, plane, wp, dev, with_learned=True, chunks=5, seed=906004):
+    """High occupancy: 5 x the batch size (500,000 events at the default
+    100,000) with two muons, Poisson(1000) noise uniform over the (plane,
+    element) pairs of the 48 planes the path reads, and after-pulse
+    duplicates of 10 % of the hits (same element, tdc + U(50, 200) ns).
+    Generated in chunks of one batch (other seeds per chunk) by a spawned
+    process pool; each chunk is packed and reconstructed on the device with
+    its records already in HBM (CUDA events around pack + the plain chain,
+    and around pack + the learned chain).  The event reducer's station
+    limits (210/120/90/90 reduced chamber hits) reject every event of this
+    workload, as the reference's would; the rejection rate is reported."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    import torch
+    from orgpu import learned, synth as S
+    n = b.n
+    jobs = [(bytes(plane.to_bytes()), wp, S.config_high_occupancy(n, seed + i)) for i in range(chunks)]
+    with cf.ProcessPoolExecutor(max_workers=min(chunks, os.cpu_count() or 1),
+                                mp_context=mp.get_context("spawn")) as ex:
+        parts = list(ex.map(S.generate_capped, jobs))
+    stream = torch.cuda.current_stream(dev)
+    d_wp = torch.from_numpy(wp.astype(np.float32).reshape(-1)).to(dev)
+    lrn = sp = model = r = bl = None
+    if with_learned:
+        sp = learned.ScorerParams.load()
+        lrn = learned.Learned(rc)
+        model = learned.DeviceModel(sp, dev.index)
+        r = learned.TrackletRows(n, device=dev.index)
+        bl = pipeline_batch(n, dev)
+    ms_plain, ms_learned, rejected, records, tracks = 0.0, 0.0, 0, 0, 0
+    agree = [0, 0, 0]
+    for rec4, off4 in parts:
+        d_rec = torch.from_numpy(rec4.view(np.uint8)).to(dev)
+        d_off = torch.from_numpy(off4).to(dev)
+        records += len(rec4)
+        legs = [("plain", lambda: (rc.pack(b, d_rec, d_off, d_wp), b.ntracklets.zero_(), rc.run_batch(b)))]
+        if with_learned:
+            legs.append(("learned", lambda: (rc.pack(bl, d_rec, d_off, d_wp),
+                                             lrn.run_batch(bl, r, model, sp.t_keep, sp.t_unc))))
+        for name, fn in legs:
+            fn()  # warm-up on this chunk
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if name == "plain":
+                ms_plain += e0.elapsed_time(e1)
+            else:
+                ms_learned += e0.elapsed_time(e1)
+        rc.sync()
+        rejected += int(b.toomany.sum().item())
+        if with_learned:
+            a = lrn.agreement(b, bl)
+            agree = [x + y for x, y in zip(agree, a)]
+        del d_rec, d_off
+    total = n * len(parts)
+    out = {"events": total, "chunks": len(parts), "records": records,
+           "workload": ("two muons, Poisson(1000) noise uniform over the (plane, element) pairs of the 48 path "
+                        "planes, after-pulses on 10 percent of hits; seeds %d..%d" % (seed, seed + len(parts) - 1)),
+           "value": total / (ms_plain / 1000.0), "unit": UNIT, "ms_total": ms_plain,
+           "rejected_frac": rejected / total,
+           "rejection_rule": "reduced chamber hits per station above 210/120/90/90 (D0/D2/D3p/D3m)"}
+    if with_learned:
+        out["learned"] = {"value": total / (ms_learned / 1000.0), "unit": UNIT, "ms_total": ms_learned,
+                          "ratio_vs_plain": ms_plain / ms_learned, "plain_global_tracks": agree[0],
+                          "reproduced": agree[1], "learned_global_tracks": agree[2],
+                          "recall": (agree[1] / agree[0]) if agree[0] else None}
+    return out
+
+
+def pipeline_batch(n, dev):
+    from orgpu import pipeline
+    return pipeline.DeviceBatch(n, dev.index)
+
+
 def serving_leg(plane, wp, tuned=None, pool_events=40000, burst_s=4.0, seed=906005):
     """Spill-structured Poisson arrivals of batches of U(1, 10000) one-dimuon
     events (the learned-scorer / small-batch distribution) at three offered
     loads, through the continuous-batching server: p50/p99 latency and
     sustained events/s per load.  Each 4 s burst starts on an idle server:
-    the 56 s gap between spills is the drain."""
-    from orgpu import serving, synth as S
+    the 56 s gap between spills is the drain.  The same schedules run again
+    on a server whose slots take the learned path (scorer + pruned YZ, plain
+    fallback for uncertain events)."""
+    import gc
+    import torch
+    from orgpu import learned, serving, synth as S
     geo = S.Geometry(plane, wp)
     rec, off, _ = S.generate(geo, S.config_small(pool_events, seed))
     rec, off = S.cap_records(rec, off)
-    srv = serving.Server(plane, wp, slot_events=10000, max_slots=4, rec_per_event=400, launch_config=tuned)
     rng = np.random.default_rng(seed)
 
     def take(n):
@@ -478,10 +619,11 @@ def serving_leg(plane, wp, tuned=None, pool_events=40000, burst_s=4.0, seed=9060
         r0 = off[e0]
         return rec[r0:off[e0 + n]], (off[e0:e0 + n + 1] - r0).astype(np.int64)
 
+    srv = serving.Server(plane, wp, slot_events=10000, max_slots=4, rec_per_event=400, launch_config=tuned)
     # capacity: a saturating queue of full-size batches
     cal = srv.serve([(0.0,) + take(10000) for _ in range(12)])
     cap = serving.latency_stats(cal)["events_per_s"]
-    loads = {}
+    schedules = {}
     for frac in (0.5, 0.8, 1.1):
         rate = frac * cap / 5000.5  # batches per second (mean batch 5000.5 events)
         sched, t = [], 0.0
@@ -490,12 +632,33 @@ def serving_leg(plane, wp, tuned=None, pool_events=40000, burst_s=4.0, seed=9060
             if t > burst_s:
                 break
             sched.append((t,) + take(int(rng.integers(1, 10001))))
-        done = srv.serve(sched)
-        st = serving.latency_stats(done) if done else {}
-        st["offered_events_per_s"] = frac * cap
-        loads["%.1fx" % frac] = st
-    return {"slots": len(srv.slots), "slot_events": 10000, "graphs": True, "burst_s": burst_s,
-            "capacity_events_per_s": cap, "workload": "one dimuon + Poisson(150) noise per event", "loads": loads}
+        schedules["%.1fx" % frac] = (frac, sched)
+
+    def run_loads(server):
+        loads = {}
+        for key, (frac, sched) in schedules.items():
+            done = server.serve(sched)
+            st = serving.latency_stats(done) if done else {}
+            st["offered_events_per_s"] = frac * cap
+            loads[key] = st
+        return loads
+
+    loads = run_loads(srv)
+    nslots = len(srv.slots)
+    del srv
+    gc.collect()
+    torch.cuda.empty_cache()
+    lsrv = serving.Server(plane, wp, slot_events=10000, max_slots=4, rec_per_event=400, launch_config=tuned,
+                          scorer=learned.ScorerParams.load())
+    lcal = lsrv.serve([(0.0,) + take(10000) for _ in range(12)])
+    learned_res = {"slots": len(lsrv.slots), "capacity_events_per_s": serving.latency_stats(lcal)["events_per_s"],
+                   "loads": run_loads(lsrv)}
+    del lsrv
+    gc.collect()
+    torch.cuda.empty_cache()
+    return {"slots": nslots, "slot_events": 10000, "graphs": True, "burst_s": burst_s,
+            "capacity_events_per_s": cap, "workload": "one dimuon + Poisson(150) noise per event", "loads": loads,
+            "learned": learned_res}
 
 
 if __name__ == "__main__":

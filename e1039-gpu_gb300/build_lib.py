@@ -2,6 +2,11 @@
 
 Every CUDA source is compiled with -fmad=false: the kernels round each float
 operation once, like the CPU oracle and a reference build at -fmad=false.
+
+build(fmad=True) makes a second image, liborgpu_fmad1.so, with nvcc's default
+multiply-add contraction -- the arithmetic of the reference as its Makefile
+builds it.  It is a measurement variant for the parity report against that
+build (tests/golden/make_golden.py), not the product.
 """
 import concurrent.futures as cf
 import os
@@ -12,6 +17,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "liborgpu.so")
+OUT_FMAD1 = os.path.join(HERE, "liborgpu_fmad1.so")
 BUILD = os.path.join(HERE, "_build")
 CU = ["er_kernel.cu", "xz_kernel.cu", "yz_kernel.cu", "clean_kernel.cu", "global_kernel.cu", "pack_kernel.cu",
       "collect_kernel.cu", "learned_kernel.cu", "mlp_kernel.cu", "select_kernel.cu", "physics_kernel.cu", "output_kernel.cu",
@@ -36,24 +42,27 @@ def _deps():
     return files + [os.path.abspath(__file__)]
 
 
-def up_to_date():
-    if not os.path.exists(OUT):
+def up_to_date(out=OUT):
+    if not os.path.exists(out):
         return False
-    t = os.path.getmtime(OUT)
+    t = os.path.getmtime(out)
     return all(os.path.getmtime(f) <= t for f in _deps())
 
 
-def build(force=False, verbose=False):
-    if not force and up_to_date():
-        return OUT
+def build(force=False, verbose=False, fmad=False):
+    out = OUT_FMAD1 if fmad else OUT
+    if not force and up_to_date(out):
+        return out
     nvcc = _nvcc()
-    os.makedirs(BUILD, exist_ok=True)
+    bdir = BUILD + ("_fmad1" if fmad else "")
+    flags = [f.replace("-fmad=false", "-fmad=true") for f in NVCC_FLAGS] if fmad else NVCC_FLAGS
+    os.makedirs(bdir, exist_ok=True)
     jobs = []
     for f in CU:
-        jobs.append([nvcc] + NVCC_FLAGS + ["-c", os.path.join(CSRC, f), "-o", os.path.join(BUILD, f + ".o")])
+        jobs.append([nvcc] + flags + ["-c", os.path.join(CSRC, f), "-o", os.path.join(bdir, f + ".o")])
     for f in CPP:
         jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", os.path.join(CSRC, f),
-                     "-o", os.path.join(BUILD, f + ".o")])
+                     "-o", os.path.join(bdir, f + ".o")])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -64,10 +73,10 @@ def build(force=False, verbose=False):
 
     with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
         list(ex.map(run, jobs))
-    objs = [os.path.join(BUILD, f + ".o") for f in CU + CPP]
-    run([nvcc] + ARCH + ["-shared", "-o", OUT + ".tmp"] + objs)
-    os.replace(OUT + ".tmp", OUT)
-    return OUT
+    objs = [os.path.join(bdir, f + ".o") for f in CU + CPP]
+    run([nvcc] + ARCH + ["-shared", "-o", out + ".tmp"] + objs)
+    os.replace(out + ".tmp", out)
+    return out
 
 
 if __name__ == "__main__":

@@ -4,6 +4,9 @@
 #include <cstring>
 #include <string>
 
+#include <mutex>
+
+#include "../../include/or_dropin.h"
 #include "../../include/or_gb300.h"
 #include "or_device.cuh"
 
@@ -12,7 +15,7 @@ cudaError_t launch_event_reduce(or_hits_view_t, uint8_t *, int, uint32_t *, cuda
 cudaError_t launch_xz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, int32_t *, uint8_t *, int, cudaStream_t,
                       int, int);
 cudaError_t launch_yz_tuned(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
-                            void *, int, int, int, cudaStream_t, int, int, long long);
+                            void *, int, int, int, cudaStream_t, int, int, long long, int);
 cudaError_t launch_yz(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *, void *,
                       int, int, int, cudaStream_t, int);
 size_t yz_scratch_bytes_ctx(int, int, int);
@@ -30,12 +33,13 @@ cudaError_t launch_global(const or_plane_t *, or_hits_view_t, or_tracks_view_t, 
 cudaError_t launch_pack(const or_hit_record_t *, const int64_t *, int, const float *, const or_rt_table_t *,
                         or_hits_view_t, uint32_t *, cudaStream_t, int);
 cudaError_t launch_wait_selftest(uint32_t *, uint32_t, cudaStream_t);
+cudaError_t yz_read_counts(const void *, long long[3]);
 cudaError_t launch_rt_apply(const or_rt_table_t *, or_hits_view_t, int, cudaStream_t, int);
 cudaError_t launch_collect(or_tracks_view_t, const uint8_t *, int, float, float *, long long, unsigned long long *,
                            cudaStream_t);
 cudaError_t launch_yz_pruned(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
                              void *, int, int, int, cudaStream_t, int, const int32_t *, const uint8_t *, long, int,
-                             long long);
+                             long long, int);
 cudaError_t launch_rows(const uint16_t *, const uint8_t *, int, int32_t *, cudaStream_t);
 cudaError_t launch_features(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int,
                             const int32_t *, float *, long, cudaStream_t, int, int);
@@ -67,6 +71,7 @@ struct or_ctx {
     void *yz_scratch;
     int yz_cap_units, yz_cap_heavy, yz_garena_warps;
     long long yz_pool_limit;  // survivor-pool entries the split YZ path may use (-1: all)
+    int yz_count_work = 0;    // YZ calls add up their work counters (or_set_yz_work_counting)
     int warps[OR_K_COUNT];  // events (work units) per CTA of each tunable kernel
     // per-event row counts and offsets of or_output_rows, grown on demand
     void *out_scratch = nullptr;
@@ -291,8 +296,26 @@ int or_yz(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uin
     cudaError_t e = orgpu::launch_yz_tuned(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw,
                                            ctx->yz_scratch, ctx->yz_cap_units, ctx->yz_cap_heavy,
                                            ctx->yz_garena_warps, S(stream), ctx->sm_count, ctx->warps[OR_K_YZ],
-                                           ctx->yz_pool_limit);
+                                           ctx->yz_pool_limit, ctx->yz_count_work);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "YZ launch");
+}
+
+int or_set_yz_work_counting(or_ctx_t *ctx, int enabled) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    ctx->yz_count_work = enabled ? 1 : 0;
+    return OR_OK;
+}
+
+int or_yz_work_counts(or_ctx_t *ctx, int64_t counts[3]) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (!counts) return fail(OR_ERR_ARG, "null counts");
+    long long c[3];
+    cudaError_t e = orgpu::yz_read_counts(ctx->yz_scratch, c);
+    if (e != cudaSuccess) return cuda_fail(e, "read YZ work counters");
+    for (int i = 0; i < 3; ++i) counts[i] = (int64_t)c[i];
+    return OR_OK;
 }
 
 int or_yz_noalloc(const or_plane_t *d_plane, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany,
@@ -541,7 +564,7 @@ int or_yz_pruned(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, co
     cudaError_t e = orgpu::launch_yz_pruned(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw, ctx->yz_scratch,
                                             ctx->yz_cap_units, ctx->yz_cap_heavy, ctx->yz_garena_warps, S(stream),
                                             ctx->sm_count, row_off, keep, (long)max_rows, ctx->warps[OR_K_YZ],
-                                            ctx->yz_pool_limit);
+                                            ctx->yz_pool_limit, ctx->yz_count_work);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "pruned YZ launch");
 }
 
@@ -710,3 +733,98 @@ int or_collect_tracks(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *too
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Drop-in calls on the reference's structs (include/or_dropin.h)
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int DROPIN_MAX_DEVICES = 64;
+std::mutex g_dropin_mutex;
+or_ctx_t *g_dropin[DROPIN_MAX_DEVICES];
+
+// the current device's drop-in context, created at its first use
+int dropin_ctx(or_ctx_t **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= DROPIN_MAX_DEVICES) return fail(OR_ERR_ARG, "device index above the drop-in table (64)");
+    std::lock_guard<std::mutex> lock(g_dropin_mutex);
+    if (!g_dropin[dev]) {
+        int rc = or_create(dev, &g_dropin[dev]);
+        if (rc) return rc;
+    }
+    *out = g_dropin[dev];
+    return OR_OK;
+}
+}  // namespace
+
+extern "C" int or_gkernel_eR(gEventHitCollections *hitcolls, bool *hastoomanyhits) {
+    or_ctx_t *ctx = nullptr;
+    int rc = dropin_ctx(&ctx);
+    if (rc) return rc;
+    if (!hitcolls || !hastoomanyhits) return fail(OR_ERR_ARG, "or_gkernel_eR: null struct or flag array");
+    return or_event_reduce(ctx, or_hits_view_from_collection(hitcolls), reinterpret_cast<uint8_t *>(hastoomanyhits),
+                           OR_REF_EVTMAX, nullptr);
+}
+
+extern "C" int or_gKernel_XZ_tracking(gEventHitCollections *hitcolls, gEventTrackCollection *tklcoll,
+                                      const gPlane *planes, int *nTracklets, bool *hastoomanyhits) {
+    or_ctx_t *ctx = nullptr;
+    int rc = dropin_ctx(&ctx);
+    if (rc) return rc;
+    if (!hitcolls || !tklcoll || !planes || !nTracklets || !hastoomanyhits)
+        return fail(OR_ERR_ARG, "or_gKernel_XZ_tracking: null argument");
+    const cudaError_t e = orgpu::launch_xz(reinterpret_cast<const or_plane_t *>(planes),
+                                           or_hits_view_from_collection(hitcolls),
+                                           or_tracks_view_from_collection(tklcoll), nTracklets,
+                                           reinterpret_cast<uint8_t *>(hastoomanyhits), OR_REF_EVTMAX, nullptr,
+                                           ctx->sm_count, ctx->warps[OR_K_XZ]);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "or_gKernel_XZ_tracking launch");
+}
+
+extern "C" int or_gKernel_YZ_tracking(gEventHitCollections *hitcolls, gEventTrackCollection *tklcoll,
+                                      const gPlane *planes, bool *hastoomanyhits) {
+    or_ctx_t *ctx = nullptr;
+    int rc = dropin_ctx(&ctx);
+    if (rc) return rc;
+    if (!hitcolls || !tklcoll || !planes || !hastoomanyhits)
+        return fail(OR_ERR_ARG, "or_gKernel_YZ_tracking: null argument");
+    const cudaError_t e = orgpu::launch_yz_tuned(
+        reinterpret_cast<const or_plane_t *>(planes), or_hits_view_from_collection(hitcolls),
+        or_tracks_view_from_collection(tklcoll), reinterpret_cast<const uint8_t *>(hastoomanyhits), OR_REF_EVTMAX,
+        ctx->d_errw, ctx->yz_scratch, ctx->yz_cap_units, ctx->yz_cap_heavy, ctx->yz_garena_warps, nullptr,
+        ctx->sm_count, ctx->warps[OR_K_YZ], ctx->yz_pool_limit, 0);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "or_gKernel_YZ_tracking launch");
+}
+
+extern "C" int or_gKernel_BackTrackCleaning(gEventTrackCollection *tklcoll, const bool *hastoomanyhits) {
+    or_ctx_t *ctx = nullptr;
+    int rc = dropin_ctx(&ctx);
+    if (rc) return rc;
+    if (!tklcoll || !hastoomanyhits) return fail(OR_ERR_ARG, "or_gKernel_BackTrackCleaning: null argument");
+    return or_back_clean(ctx, or_tracks_view_from_collection(tklcoll),
+                         reinterpret_cast<const uint8_t *>(hastoomanyhits), OR_REF_EVTMAX, nullptr);
+}
+
+extern "C" int or_gKernel_Global_tracking(gEventHitCollections *hitcolls, gEventTrackCollection *tklcoll,
+                                          const gPlane *planes, bool *hastoomanyhits) {
+    or_ctx_t *ctx = nullptr;
+    int rc = dropin_ctx(&ctx);
+    if (rc) return rc;
+    if (!hitcolls || !tklcoll || !planes || !hastoomanyhits)
+        return fail(OR_ERR_ARG, "or_gKernel_Global_tracking: null argument");
+    const cudaError_t e = orgpu::launch_global(reinterpret_cast<const or_plane_t *>(planes),
+                                               or_hits_view_from_collection(hitcolls),
+                                               or_tracks_view_from_collection(tklcoll),
+                                               reinterpret_cast<const uint8_t *>(hastoomanyhits), OR_REF_EVTMAX,
+                                               ctx->d_errw, ctx->d_sched, nullptr, ctx->sm_count,
+                                               ctx->warps[OR_K_GLOBAL]);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "or_gKernel_Global_tracking launch");
+}
+
+extern "C" int or_dropin_sync(void) {
+    or_ctx_t *ctx = nullptr;
+    int rc = dropin_ctx(&ctx);
+    if (rc) return rc;
+    return or_stream_sync(ctx, nullptr);
+}

@@ -133,6 +133,11 @@ struct YzUnit {
 struct YzHeavy {
     int e, slot, k;
     int unit0, nunits;
+    // outer-iteration scoring: the tracklet's first score row (-1: no rows,
+    // nothing pruned), its row count (the live outer iterations), the inner
+    // combinations per outer iteration, and the outer index of its best
+    // combination (written by yz_apply_kernel; -1: none)
+    int orow0, nrows, c2, best_g;
 };
 // best combination of one unit
 struct YzBest {
@@ -168,12 +173,18 @@ __device__ __forceinline__ int yz_tab_index(int gu3, int gv3, int gu2, int gv2) 
     return ((gu3 - 1) * 3 + (gv3 - 1)) * 9 + (gu2 - 1) * 3 + (gv2 - 1);
 }
 
+// Work counters of one YZ call (64-bit, in the counters area): combinations
+// that reach the first y fit, the sum of their hit counts, and combinations
+// that pass its 2-sigma cut (the survivors of the first cut).
+constexpr int YZ_CTR_FITTED = 16, YZ_CTR_HITSUM = 18, YZ_CTR_SURVIVORS = 20;
+
 struct YzScratch {
     const YzTab *tab;        // 2 x YZ_TAB_SETS entries: station-3 half 0 (D3p) then 1 (D3m)
     YzUnit *units;
     YzHeavy *heavy;
     YzBest *best;
-    unsigned int *counters;  // [0] units reserved, [1] heavy reserved, [2] queue head, [4..5] planning units
+    unsigned int *counters;  // [0] units reserved, [1] heavy reserved, [2] queue head, [3] survivor-kernel
+                             // head, [4..5] planning units, [8..9] pool entries, [16..21] work counters
     YzHit *garena;           // per-warp overflow arenas
     struct PassEntryStore *qbuf;  // per-warp survivor queues (qcap entries each)
     int cap_units, cap_heavy, garena_warps, qcap;
@@ -182,14 +193,28 @@ struct YzScratch {
     struct PassEntryStore *pool;
     int2 *useg;
     long long pool_cap;  // 0: no pool, the combined kernel runs
+    int count_work;      // nonzero: the kernels add up the work counters
 };
 
 // optional pruning: tracklet rows (row_off, as the scorer's) and keep flags
 struct YzPrune {
+    // tracklet keep flags of the tracklet scorer
     const int32_t *row_off;
     const uint8_t *keep;  // nullptr: plain
     long max_rows;
+    // the combination scorer: one feature row per live (u3, v3) outer
+    // iteration of every queued (heavy) tracklet, written by the planning
+    // pass; scores filled before the first cut; an outer iteration scoring
+    // below t_keep is skipped, unless its event is uncertain (unc[e])
+    float *ofeat;         // [cap_orows * OR_NFEAT]; nullptr: no outer rows
+    int32_t *og;          // [cap_orows] outer index g of each row
+    const float *oscore;  // [cap_orows]; nullptr: rows written, nothing pruned
+    uint32_t *orows;      // row counter
+    const uint8_t *unc;   // [n_events] uncertain events
+    long cap_orows;
+    float t_keep;
 };
+
 
 struct PassEntryStore {
     int c;
@@ -216,6 +241,8 @@ struct YzWarp {
     int nhx;
     float xdd[4], xres[4], xp1x[4], xp1y[4], xp1z[4], xdpx[4], xdpy[4], xdpz[4];
     short xhs[4];
+    // survivors this warp evaluated (work counter)
+    unsigned long long nsurv;
     YzBest b;
 };
 
@@ -663,6 +690,7 @@ __device__ __noinline__ void yz_phase2(YzWarp &S, const YzEvent &E, const YzHit 
     const int lane = lane_id();
     const float x0 = S.x0, tx = S.tx, ex0 = S.ex0, etx = S.etx;
     const int nhx = S.nhx;
+    if (lane == 0) S.nsurv += (unsigned long long)n;
     // --- one chunk of survivors ------------------------------------------
     const bool valid = lane < n;
     PassEntry q;
@@ -858,6 +886,97 @@ __device__ __forceinline__ int next_alive_outer(const YzAlive &m, int nu3, int i
     const int v = next_bit128(m.v, iv + 1);
     const int u = next_bit128(m.u, 0);
     return (v < 0 || u < 0) ? -1 : u + v * nu3;
+}
+
+// index of the k-th set bit (k from 0) of a 128-bit mask, or -1
+__device__ __forceinline__ int nth_bit128(const unsigned m[4], int k) {
+#pragma unroll 1
+    for (int w = 0; w < 4; ++w) {
+        const int c = __popc(m[w]);
+        if (k < c) {
+            unsigned v = m[w];
+#pragma unroll 1
+            for (int i = 0; i < k; ++i) v &= v - 1u;
+            return w * 32 + __ffs(v) - 1;
+        }
+        k -= c;
+    }
+    return -1;
+}
+
+// set bits of a 128-bit mask below index i
+__device__ __forceinline__ int bits_below128(const unsigned m[4], int i) {
+    int c = 0;
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        if (w < (i >> 5)) c += __popc(m[w]);
+        else if (w == (i >> 5)) c += __popc(m[w] & ((1u << (i & 31)) - 1u));
+    }
+    return c;
+}
+
+// Distance from the hits of a prop-tube y plane at z = zp to the window of
+// y the track can have there: through y3 at z3 with |ty| <= TY_MAX and
+// |y0| <= Y0_MAX (the bounds the YZ hard cut enforces, K:1638), widened by
+// the prop-tube match tolerance (K:1640-1702); 30 cm when there is no hit or
+// no such line.
+__device__ __forceinline__ float prop_gap(const HitPlane &h, float zp, float y3, float z3, float lo_t, float hi_t,
+                                          float tol) {
+    float d = 30.f;
+    if (lo_t > hi_t) return d;
+    const float ya = y3 + lo_t * (zp - z3), yb = y3 + hi_t * (zp - z3);
+    const float lo = fminf(ya, yb) - tol, hi = fmaxf(ya, yb) + tol;
+#pragma unroll 1
+    for (int i = 0; i < h.n; ++i) {
+        const float p = h.pos(i);
+        d = fminf(d, fmaxf(fmaxf(lo - p, p - hi), 0.f));
+    }
+    return d;
+}
+
+// The combination scorer's 16 features of live outer iteration (iu, iv) of
+// the current tracklet: the tracklet's x fit, the y of its u3 and v3 hits
+// (mean of the accepted hits of each pair) and their difference against the
+// x fit's error at station 3 -- the x error moves the two stereo estimates
+// of y apart -- the distance of the P1 and P2 y-tube hits from the window
+// the track's y can reach there, hit counts, the inner and outer loop sizes,
+// the station-3 half and the tracklet's x-hit count.
+__device__ void yz_outer_features(const YzWarp &S, const YzEvent &E, const YzHit *base, const or_plane_t &P, int iu,
+                                  int iv, int st3, long C2, long Ga, float *f) {
+    const short2 pu = S.pair[2][iu], pv = S.pair[3][iv];
+    const YzHit *l4 = yz_list(S, base, 4), *l5 = yz_list(S, base, 5);
+    const YzHit *l6 = yz_list(S, base, 6), *l7 = yz_list(S, base, 7);
+    float su = 0.f, sv = 0.f;
+    int nu = 0, nv = 0;
+    if (pu.x >= 0 && l4[pu.x].acc) { su += l4[pu.x].Y; ++nu; }
+    if (pu.y >= 0 && l5[pu.y].acc) { su += l5[pu.y].Y; ++nu; }
+    if (pv.x >= 0 && l6[pv.x].acc) { sv += l6[pv.x].Y; ++nv; }
+    if (pv.y >= 0 && l7[pv.y].acc) { sv += l7[pv.y].Y; ++nv; }
+    const float yu = su / (float)max(nu, 1), yv = sv / (float)max(nv, 1);
+    const float z3 = P.z[E.dl[4]];
+    const float sig = fmaxf(S.ex0 + S.etx * z3, 1e-3f);
+    const float y3 = 0.5f * (yu + yv);
+    const float lo_t = fmaxf(-TY_MAX, (y3 - Y0_MAX) / z3), hi_t = fminf(TY_MAX, (y3 + Y0_MAX) / z3);
+    const float d1 = fminf(prop_gap(E.p1y1, P.z[DET_P1Y1], y3, z3, lo_t, hi_t, 5.08f),
+                           prop_gap(E.p1y2, P.z[DET_P1Y2], y3, z3, lo_t, hi_t, 5.08f));
+    const float d2 = fminf(prop_gap(E.p2y1, P.z[DET_P2Y1], y3, z3, lo_t, hi_t, 10.16f),
+                           prop_gap(E.p2y2, P.z[DET_P2Y2], y3, z3, lo_t, hi_t, 10.16f));
+    f[0] = S.x0 * 0.01f;
+    f[1] = S.tx * 10.f;
+    f[2] = S.ex0;
+    f[3] = S.etx * 100.f;
+    f[4] = yu * 0.02f;
+    f[5] = yv * 0.02f;
+    f[6] = fminf(fmaxf((yu - yv) / sig, -20.f), 20.f) * 0.1f;
+    f[7] = log1pf(fabsf(yu - yv));
+    f[8] = d1 * 0.1f;
+    f[9] = d2 * 0.1f;
+    f[10] = (float)nu;
+    f[11] = (float)nv;
+    f[12] = log1pf((float)C2);
+    f[13] = log1pf((float)Ga);
+    f[14] = (float)(st3 - 3);
+    f[15] = (float)S.nhx;
 }
 
 template <bool FIRST_ONLY>
@@ -1154,6 +1273,42 @@ __device__ __forceinline__ YzHit *yz_garena(const YzScratch &sc, int gwarp) {
     return sc.garena + (long)(gwarp % sc.garena_warps) * YZ_GARENA_HITS;
 }
 
+// Work of a tracklet's first cut, from its pair lists: a combination reaches
+// the first y fit when each of the u3, v3, u2 and v2 pairs gives an accepted
+// hit, so the fitted combinations are the product of the four counts of such
+// pairs, and the sum of their hit counts follows from each projection's
+// accepted hits.  Returned on every lane.
+__device__ void yz_fit_counts(const YzWarp &S, const YzHit *base, unsigned long long &fitted,
+                              unsigned long long &hitsum) {
+    const int lane = lane_id();
+    unsigned long long A[4], H[4];
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        const YzHit *la = yz_list(S, base, 2 * q), *lb = yz_list(S, base, 2 * q + 1);
+        unsigned a = 0, h = 0;
+#pragma unroll 1
+        for (int i = lane; i < S.np[q]; i += 32) {
+            const short2 p = S.pair[q][i];
+            const unsigned k = (p.x >= 0 && la[p.x].acc ? 1u : 0u) + (p.y >= 0 && lb[p.y].acc ? 1u : 0u);
+            a += k > 0;
+            h += k;
+        }
+        A[q] = __reduce_add_sync(0xffffffffu, a);
+        H[q] = __reduce_add_sync(0xffffffffu, h);
+    }
+    fitted = A[0] * A[1] * A[2] * A[3];
+    hitsum = H[0] * A[1] * A[2] * A[3] + A[0] * H[1] * A[2] * A[3] + A[0] * A[1] * H[2] * A[3] +
+             A[0] * A[1] * A[2] * H[3];
+}
+
+__device__ __forceinline__ void yz_flush_counts(const YzScratch &sc, unsigned long long fitted,
+                                                unsigned long long hitsum, unsigned long long nsurv) {
+    unsigned long long *c = reinterpret_cast<unsigned long long *>(sc.counters);
+    if (fitted) atomicAdd(c + YZ_CTR_FITTED / 2, fitted);
+    if (hitsum) atomicAdd(c + YZ_CTR_HITSUM / 2, hitsum);
+    if (nsurv) atomicAdd(c + YZ_CTR_SURVIVORS / 2, nsurv);
+}
+
 template <int W>
 __global__ void __launch_bounds__(W * 32, (OR_YZ_PLAN_WARPS_SM / W > 0 ? OR_YZ_PLAN_WARPS_SM / W : 1))
     yz_plan_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv,
@@ -1169,6 +1324,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_PLAN_WARPS_SM / W > 0 ? OR_YZ_P
     YzWarp &S = warps[w];
     YzHit *garena = yz_garena(sc, blockIdx.x * W + w);
     PassEntryStore *Q = sc.qbuf + (long)((blockIdx.x * W + w) % sc.garena_warps) * sc.qcap;
+    if (lane == 0) S.nsurv = 0ull;
+    unsigned long long n_fitted = 0ull, n_hitsum = 0ull;  // lane 0's work counters
 
     // planning units (event, YZ_PLAN_CHUNK slots) from a device counter: slots
     // are independent (one reference thread each), events very uneven
@@ -1234,6 +1391,12 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_PLAN_WARPS_SM / W > 0 ? OR_YZ_P
                 const YzAlive al = yz_alive(S, base);
                 const long Ga = (long)bits128(al.u) * bits128(al.v);  // live outer iterations
                 if (Ga == 0) continue;  // no candidate and no scratch entry past 3 written
+                if (sc.count_work) {
+                    unsigned long long f, h;
+                    yz_fit_counts(S, base, f, h);
+                    n_fitted += f;
+                    n_hitsum += h;
+                }
                 yz_xhits(S, T, P);
                 const long C = G * C2;
                 const long Cl = Ga * C2 + G;  // live combinations, plus one step per outer iteration
@@ -1257,6 +1420,28 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_PLAN_WARPS_SM / W > 0 ? OR_YZ_P
                         if (lane == 0 && hid < sc.cap_heavy) sc.heavy[hid].nunits = 0;
                         inline_it = true;
                     } else {
+                        // the combination scorer's rows: one per live outer iteration
+                        int orow0 = -1;
+                        if (prune.ofeat) {
+                            unsigned r0 = 0u;
+                            if (lane == 0) r0 = atomicAdd(prune.orows, (unsigned)Ga);
+                            r0 = __shfl_sync(0xffffffffu, r0, 0);
+                            if ((long)r0 + Ga <= prune.cap_orows) {
+                                orow0 = (int)r0;
+                                const int Au = bits128(al.u);
+#pragma unroll 1
+                                for (long r = lane; r < Ga; r += 32) {
+                                    const int iu = nth_bit128(al.u, (int)(r % Au)), iv = nth_bit128(al.v, (int)(r / Au));
+                                    float f[OR_NFEAT];
+                                    yz_outer_features(S, E, base, P, iu, iv, st3, C2, Ga, f);
+                                    float4 *dst = reinterpret_cast<float4 *>(prune.ofeat + (r0 + r) * OR_NFEAT);
+#pragma unroll
+                                    for (int q = 0; q < OR_NFEAT / 4; ++q)
+                                        dst[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+                                    prune.og[r0 + r] = iu + iv * nu3;
+                                }
+                            }
+                        }
                         if (lane == 0) {
                             YzHeavy hv2;
                             hv2.e = (int)e;
@@ -1264,6 +1449,10 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_PLAN_WARPS_SM / W > 0 ? OR_YZ_P
                             hv2.k = it;
                             hv2.unit0 = u0;
                             hv2.nunits = nunits;
+                            hv2.orow0 = orow0;
+                            hv2.nrows = (int)Ga;
+                            hv2.c2 = (int)C2;
+                            hv2.best_g = -1;
                             sc.heavy[hid] = hv2;
                         }
                         yz_unit_states(S, base, (int)G, (int)gper, st, sc.units + u0, hid);
@@ -1280,6 +1469,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_PLAN_WARPS_SM / W > 0 ? OR_YZ_P
             }
         }
     }
+    __syncwarp();
+    if (lane == 0 && sc.count_work) yz_flush_counts(sc, n_fitted, n_hitsum, S.nsurv);
 }
 
 // persistent warps drain the unit queue
@@ -1296,6 +1487,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_
     YzWarp &S = warps[w];
     YzHit *garena = yz_garena(sc, blockIdx.x * W + w);
     PassEntryStore *Q = sc.qbuf + (long)((blockIdx.x * W + w) % sc.garena_warps) * sc.qcap;
+    if (lane == 0) S.nsurv = 0ull;
+    __syncwarp();
     const int nunits = min((int)sc.counters[0], sc.cap_units);
     for (;;) {
         int u = 0;
@@ -1334,6 +1527,7 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_
         }
         __syncwarp();
     }
+    if (lane == 0 && sc.count_work) yz_flush_counts(sc, 0ull, 0ull, S.nsurv);
 }
 
 
@@ -1421,6 +1615,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_SECOND_WARPS_SM / W > 0 ? OR_YZ
     if (gw >= sc.garena_warps) return;
     YzHit *garena = yz_garena(sc, gw);
     PassEntryStore *Q = sc.qbuf + (long)gw * sc.qcap;
+    if (lane == 0) S.nsurv = 0ull;
+    __syncwarp();
     const int nunits = min((int)sc.counters[0], sc.cap_units);
     for (;;) {
         int u = 0;
@@ -1471,6 +1667,7 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_SECOND_WARPS_SM / W > 0 ? OR_YZ
         }
         __syncwarp();
     }
+    if (lane == 0 && sc.count_work) yz_flush_counts(sc, 0ull, 0ull, S.nsurv);
 }
 
 
@@ -1576,11 +1773,22 @@ size_t yz_scratch_bytes_ctx(int cap_units, int cap_heavy, int garena_warps) {
     return yz_scratch_bytes_q(cap_units, cap_heavy, garena_warps, YZ_QCAP_CTX);
 }
 
+// the work counters of the last YZ call on `scratch` (synchronous copy)
+cudaError_t yz_read_counts(const void *scratch, long long out[3]) {
+    unsigned long long c[32];
+    const cudaError_t e = cudaMemcpy(c, scratch, sizeof(c), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return e;
+    out[0] = (long long)c[YZ_CTR_FITTED / 2];
+    out[1] = (long long)c[YZ_CTR_HITSUM / 2];
+    out[2] = (long long)c[YZ_CTR_SURVIVORS / 2];
+    return cudaSuccess;
+}
+
 template <int W>
 static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
                                   const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
                                   int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, YzPrune prune,
-                                  int qcap, long long pool_limit) {
+                                  int qcap, long long pool_limit, int count_work) {
     if (n_events <= 0) return cudaSuccess;
     const size_t smem = yz_smem_bytes(W);
     cudaError_t err;
@@ -1621,6 +1829,7 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
     sc.cap_heavy = cap_heavy;
     sc.garena_warps = garena_warps;
     sc.qcap = qcap;
+    sc.count_work = count_work;
     if ((err = cudaMemsetAsync(sc.counters, 0, 256, stream))) return err;
     yz_tab_kernel<<<1, 256, 0, stream>>>(d_plane, tab);
     if ((err = cudaGetLastError())) return err;
@@ -1647,35 +1856,34 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
 static cudaError_t launch_yz_w(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
                                const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
                                int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, YzPrune prune,
-                               int warps, int qcap, long long pool_limit) {
+                               int warps, int qcap, long long pool_limit, int count_work) {
+#define OR_YZ_LAUNCH(W)                                                                                         \
+    launch_yz_impl<W>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream, \
+                      sm_count, prune, qcap, pool_limit, count_work)
     switch (warps) {
-    case 1: return launch_yz_impl<1>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                     garena_warps, stream, sm_count, prune, qcap, pool_limit);
-    case 2: return launch_yz_impl<2>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                     garena_warps, stream, sm_count, prune, qcap, pool_limit);
-    case 8: return launch_yz_impl<8>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                     garena_warps, stream, sm_count, prune, qcap, pool_limit);
-    case 16: return launch_yz_impl<16>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                       garena_warps, stream, sm_count, prune, qcap, pool_limit);
-    default: return launch_yz_impl<4>(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy,
-                                      garena_warps, stream, sm_count, prune, qcap, pool_limit);
+    case 1: return OR_YZ_LAUNCH(1);
+    case 2: return OR_YZ_LAUNCH(2);
+    case 8: return OR_YZ_LAUNCH(8);
+    case 16: return OR_YZ_LAUNCH(16);
+    default: return OR_YZ_LAUNCH(4);
     }
+#undef OR_YZ_LAUNCH
 }
 
 cudaError_t launch_yz(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv, const uint8_t *toomany,
                       int n_events, uint32_t *errw, void *scratch, int cap_units, int cap_heavy, int garena_warps,
                       cudaStream_t stream, int sm_count) {
     return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
-                       sm_count, YzPrune{nullptr, nullptr, 0}, 4, YZ_QCAP_MIN, -1);
+                       sm_count, YzPrune{}, 4, YZ_QCAP_MIN, -1, 0);
 }
 
 // with `warps` events (work units) per CTA: 1, 2, 4, 8 or 16
 cudaError_t launch_yz_tuned(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
                             const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
                             int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, int warps,
-                            long long pool_limit) {
+                            long long pool_limit, int count_work) {
     return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
-                       sm_count, YzPrune{nullptr, nullptr, 0}, warps, YZ_QCAP_CTX, pool_limit);
+                       sm_count, YzPrune{}, warps, YZ_QCAP_CTX, pool_limit, count_work);
 }
 
 // YZ with the scorer's keep flags: pruned tracklets are left as tracklets no
@@ -1684,9 +1892,13 @@ cudaError_t launch_yz_pruned(const or_plane_t *d_plane, or_hits_view_t hv, or_tr
                              const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
                              int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count,
                              const int32_t *row_off, const uint8_t *keep, long max_rows, int warps,
-                             long long pool_limit) {
+                             long long pool_limit, int count_work) {
+    YzPrune pr{};
+    pr.row_off = row_off;
+    pr.keep = keep;
+    pr.max_rows = max_rows;
     return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
-                       sm_count, YzPrune{row_off, keep, max_rows}, warps, YZ_QCAP_CTX, pool_limit);
+                       sm_count, pr, warps, YZ_QCAP_CTX, pool_limit, count_work);
 }
 
 }  // namespace orgpu

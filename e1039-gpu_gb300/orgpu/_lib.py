@@ -23,7 +23,9 @@ EXPORTS = ("or_version", "or_last_error", "or_status_string", "or_geometry_load"
            "or_mlp_adam", "or_prop_matching", "or_global_clean", "or_run_selection", "or_set_launch",
            "or_get_launch", "or_vertexing", "or_dimuons", "or_fill_histograms", "or_hist_table_init",
            "or_run_physics", "or_output_rows", "or_rt_load", "or_rt_set_plane", "or_rt_table_bytes",
-           "or_pack_hits_rt", "or_rt_apply", "or_set_yz_pool_limit", "or_selftest_bounded_wait")
+           "or_pack_hits_rt", "or_rt_apply", "or_set_yz_pool_limit", "or_selftest_bounded_wait",
+           "or_yz_work_counts", "or_set_yz_work_counting", "or_gkernel_eR", "or_gKernel_XZ_tracking", "or_gKernel_YZ_tracking",
+           "or_gKernel_BackTrackCleaning", "or_gKernel_Global_tracking", "or_dropin_sync")
 
 # tunable kernels (or_kernel_id_t)
 KERNELS = {"event_reduce": 0, "xz": 1, "yz": 2, "back_clean": 3, "global": 4, "select": 5, "features": 6}
@@ -44,11 +46,17 @@ _lib = None
 def lib():
     """Load liborgpu.so (built by build_lib.build()); raise if it is absent."""
     global _lib
-    if _lib is not None:
-        return _lib
-    if not os.path.exists(LIB_PATH):
-        raise OrError(-1, f"liborgpu.so not built at {LIB_PATH}; run __graft_entry__.build()")
-    lb = C.CDLL(LIB_PATH)
+    if _lib is None:
+        _lib = load(LIB_PATH)
+    return _lib
+
+
+def load(path):
+    """Load a build of the library at `path` with the C-ABI signatures set
+    (lib() is load(LIB_PATH), once per process)."""
+    if not os.path.exists(path):
+        raise OrError(-1, f"liborgpu.so not built at {path}; run __graft_entry__.build()")
+    lb = C.CDLL(path)
     P = C.POINTER
     vp = C.c_void_p
     lb.or_version.restype = C.c_char_p
@@ -78,6 +86,15 @@ def lib():
     lb.or_collect_tracks.argtypes = [vp, L.OrTracksView, vp, C.c_int, C.c_float, vp, C.c_int64, vp, vp]
     lb.or_yz_noalloc.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, C.c_int, vp, vp]
     lb.or_selftest_bounded_wait.argtypes = [vp, C.c_int, vp]
+    lb.or_yz_work_counts.argtypes = [vp, vp]
+    lb.or_set_yz_work_counting.argtypes = [vp, C.c_int]
+    # include/or_dropin.h: the reference's launches on its own structs
+    lb.or_gkernel_eR.argtypes = [vp, vp]
+    lb.or_gKernel_XZ_tracking.argtypes = [vp, vp, vp, vp, vp]
+    lb.or_gKernel_YZ_tracking.argtypes = [vp, vp, vp, vp]
+    lb.or_gKernel_BackTrackCleaning.argtypes = [vp, vp]
+    lb.or_gKernel_Global_tracking.argtypes = [vp, vp, vp, vp]
+    lb.or_dropin_sync.argtypes = []
     i64, f32, i32 = C.c_int64, C.c_float, C.c_int
     lb.or_tracklet_rows.argtypes = [vp, L.OrTracksView, vp, i32, vp, vp]
     lb.or_tracklet_features.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, i32, vp, vp, i64, vp]
@@ -114,8 +131,7 @@ def lib():
     lb.or_set_yz_pool_limit.argtypes = [vp, i64]
     for name in EXPORTS:
         getattr(lb, name)
-    _lib = lb
-    return _lib
+    return lb
 
 
 def check(rc, what="call"):

@@ -292,3 +292,10 @@ class HostTracks:
                 base = e * EVT_TRK_FLOATS + (s * SLOTCAP + k) * NTRKPARAM
                 out.append((s, k, self.tracks[base:base + NTRKPARAM]))
         return out
+
+
+# byte sizes of the reference's fixed-capacity structs (REF_EVTMAX events):
+# gEventHitCollections (reconstruction_classes.cuh:76-87, 4-byte members, no
+# padding) and gEventTrackCollection (:542-544: uint16 counts, then floats)
+REF_HITS_BYTES = REF_EVTMAX * (4 * (NCHAM + NHODO + NPROP) + 4 * (EVT_CHAM_FLOATS + EVT_HODO_FLOATS + EVT_PROP_FLOATS))
+REF_TRACKS_BYTES = REF_EVTMAX * (2 * NSLOTS + 4 * EVT_TRK_FLOATS)

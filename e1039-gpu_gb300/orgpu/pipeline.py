@@ -156,10 +156,12 @@ class DeviceHists:
 class Reconstruction:
     """One library context (one device) with its geometry."""
 
-    def __init__(self, plane, device=0):
+    def __init__(self, plane, device=0, lib=None):
+        """lib: a library handle from _lib.load() (default: the product
+        build, _lib.lib())."""
         torch = _torch()
         self.device = device
-        self.lib = _lib.lib()
+        self.lib = lib if lib is not None else _lib.lib()
         self.ctx = C.c_void_p()
         _lib.check(self.lib.or_create(device, C.byref(self.ctx)), "or_create")
         self.plane = plane
@@ -314,6 +316,18 @@ class Reconstruction:
         _lib.check(self.lib.or_collect_tracks(self.ctx, b.tracks_view(), b.toomany.data_ptr(), b.n, float(stid),
                                               d_out.data_ptr(), cap, d_count.data_ptr(), self._stream(stream)),
                    "or_collect_tracks")
+
+    def set_yz_work_counting(self, enabled):
+        """Let YZ calls on this context add up their work counters (costs
+        about 2 % of the stage; off by default)."""
+        _lib.check(self.lib.or_set_yz_work_counting(self.ctx, 1 if enabled else 0), "or_set_yz_work_counting")
+
+    def yz_work_counts(self):
+        """(fitted combinations, sum of their hit counts, first-cut survivors)
+        of the last YZ call on this context; call after sync()."""
+        c = (C.c_int64 * 3)()
+        _lib.check(self.lib.or_yz_work_counts(self.ctx, c), "or_yz_work_counts")
+        return int(c[0]), int(c[1]), int(c[2])
 
     def sync(self, stream=None):
         """Wait for the stream and raise on device-side error words."""

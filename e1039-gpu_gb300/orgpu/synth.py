@@ -260,6 +260,15 @@ def generate(geo, cfg):
     return rec, offsets, truth
 
 
+def generate_capped(job):
+    """generate() + cap_records() for a process pool: job = (OrPlane bytes,
+    wire positions, EventConfig); returns (records, offsets)."""
+    plane_bytes, wire_pos, cfg = job
+    plane = L.OrPlane.from_buffer_copy(plane_bytes)
+    rec, off, _ = generate(Geometry(plane, wire_pos), cfg)
+    return cap_records(rec, off)
+
+
 def trigger_bits(n_events, seed=906010):
     """Per-event trigger words (int32): the reference reads them from the raw
     event (gEvent::TriggerBits, online_reconstruction.cu:346); here ten

@@ -106,6 +106,18 @@ int or_set_geometry(or_ctx_t *ctx, const or_plane_t *plane);
  * kernels write past their arrays instead, and its host aborts on CUDA
  * errors (online_reconstruction.cu:50-64). */
 int or_stream_sync(or_ctx_t *ctx, void *stream);
+/* Work counters of the YZ stage, for throughput accounting.  With counting
+ * enabled (or_set_yz_work_counting(ctx, 1); off by default, as it costs
+ * about 2 % of the stage), each or_yz() / or_yz_pruned() call on this
+ * context counts, and or_yz_work_counts() returns the last call's:
+ * counts[0] = combinations that reached the first y fit (fit_2D_track,
+ * reconstruction_kernels.cuh:1602), counts[1] = the sum of their hit
+ * counts, counts[2] = combinations that passed its 2-sigma cut (:1611) and
+ * went on to the left/right resolution and gates.  or_yz_work_counts() is
+ * synchronous: call it after or_stream_sync() on the stream that ran the
+ * stage.  No counterpart in the reference. */
+int or_set_yz_work_counting(or_ctx_t *ctx, int enabled);
+int or_yz_work_counts(or_ctx_t *ctx, int64_t counts[3]);
 /* Self-test of the bounded device waits: launches one warp that waits on a
  * shared-memory mbarrier nothing arrives at (no bulk copy targets it) for at
  * most `polls` polls (1..1000000).  The wait runs out and raises the same

@@ -32,6 +32,7 @@ OUT = os.path.join(ORACLE, "_ref")
 REF_SRC = os.environ.get("OR_REFERENCE_SRC",
                          os.path.join(os.path.dirname(ORACLE), "..", "reference", "OnlineReconstruction"))
 WRAP = os.path.join(HERE, "ref_kernels.cu")
+HARNESS = [os.path.join(HERE, "xz_pin.cuh")]
 VARIANTS = {"fmad0": ["-fmad=false"], "fmad1": []}
 
 
@@ -47,7 +48,7 @@ def _stale(path):
     if not os.path.exists(path):
         return True
     t = os.path.getmtime(path)
-    return any(os.path.getmtime(s) > t for s in [WRAP, __file__] + _headers())
+    return any(os.path.getmtime(s) > t for s in [WRAP, __file__] + HARNESS + _headers())
 
 
 def _compile(variant):

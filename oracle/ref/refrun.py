@@ -43,7 +43,10 @@ KERNELS = {
     "vertexing": "_Z17gKernel_VertexingP21gEventTrackCollectionPKfPb",
     "dimuons": "_Z22gKernel_DimuonBuildingP21gEventTrackCollectionP22gEventDimuonCollectionPKfPKb",
     "hists": "_Z31gKernel_fill_display_histogramsP21gEventTrackCollectionP22gEventDimuonCollectionP12gHistsArraysPKiPKb",
+    # test-only kernel of oracle/ref/xz_pin.cuh: the XZ candidates on the reference's helpers
+    "xz_pin": "xz_pin_kernel",
 }
+XZ_REC = 32  # floats per candidate record of xz_pin_kernel
 # gEventDimuonCollection (reconstruction_classes.cuh:870-872): unsigned short
 # NDimuons[E], then float DimuonsRawData[E*16*36] (4-byte aligned after 2*E bytes)
 DIM_DATA_OFF = 2 * E
@@ -238,6 +241,33 @@ class RefKernels:
         d.ndimuons[:] = self.dims[:2 * n].cpu().numpy().view(np.uint16)
         d.dimuons[:] = self.dims[DIM_DATA_OFF:DIM_DATA_OFF + 4 * n * L.EVT_DIM_FLOATS].cpu().numpy().view(np.float32)
         return d
+
+    def xz_candidates(self, n, cap=64):
+        """The XZ stage's accepted candidates of the first n events on the
+        loaded hits (put_hits: the reduced hits) and flags (put_flags: the
+        event reducer's), computed by xz_pin_kernel with the reference's
+        helpers: (records float32 [n, 32, cap, 32], counts int32 [n, 32],
+        status int32 [n, 32]) per (event, reference thread); see
+        oracle/ref/xz_pin.cuh for the record layout and status bits."""
+        t = self.torch
+        dev = self.hits.device
+        out = t.zeros(n * 32 * cap * XZ_REC, dtype=t.float32, device=dev)
+        nout = t.zeros(n * 32, dtype=t.int32, device=dev)
+        status = t.zeros(n * 32, dtype=t.int32, device=dev)
+        vals = [C.c_void_p(self.hits.data_ptr()), C.c_void_p(self.plane.data_ptr()), C.c_void_p(self.flags.data_ptr()),
+                C.c_int(n), C.c_void_p(out.data_ptr()), C.c_int(cap), C.c_void_p(nout.data_ptr()),
+                C.c_void_p(status.data_ptr())]
+        args = (C.c_void_p * len(vals))(*[C.cast(C.byref(v), C.c_void_p) for v in vals])
+        stream = C.c_void_p(t.cuda.current_stream().cuda_stream)
+        threads = 128
+        blocks = (n * 32 + threads - 1) // threads
+        if blocks:
+            self._chk(self.cu.cuLaunchKernel(self.fn["xz_pin"], blocks, 1, 1, threads, 1, 1, 0, stream, args, None),
+                      "launch xz_pin")
+        t.cuda.synchronize()
+        self._chk(self.cu.cuCtxSynchronize(), "after xz_pin")
+        return (out.view(n, 32, cap, XZ_REC).cpu().numpy(), nout.view(n, 32).cpu().numpy(),
+                status.view(n, 32).cpu().numpy())
 
     def global_tracking(self, n):
         self._launch("global", n, 32, self.hits.data_ptr(), self.tracks.data_ptr(), self.plane.data_ptr(),

@@ -186,3 +186,84 @@ def select_events(rec, off, idx):
     lens = np.array([len(p) for p in parts], np.int64)
     new_off = np.concatenate([[0], np.cumsum(lens)]).astype(off.dtype)
     return (np.concatenate(parts) if parts else rec[:0]), new_off
+
+
+# ---------------------------------------------------------------------------
+# XZ candidates (oracle/ref/xz_pin.cuh): 32 floats per accepted candidate,
+# [binId, thread, nhits, x0, tx, err_x0, err_tx, 0, then per hit n < 4:
+# det, elem, x, drift, sign, tdc]
+XZ_REC = 32
+XZ_FIT = [3, 4, 5, 6]  # x0, tx, err_x0, err_tx
+
+
+def xz_from_tracks(t, toomany):
+    """The tracklets of an XZ output (HostTracks) as candidate records:
+    (counts int32 [n], records float32 [m, 32]) in (event, slot, position)
+    order; events flagged in `toomany` hold none."""
+    cnt = np.zeros(t.n, np.int32)
+    recs = []
+    for e in range(t.n):
+        if toomany is not None and toomany[e]:
+            continue
+        for s, k, r in t.records(e):
+            v = np.zeros(XZ_REC, np.float32)
+            nh = int(r[L.TRK_NHITS])
+            v[:7] = [r[L.TRK_STID], r[L.TRK_THREAD], r[L.TRK_NHITS], r[L.TRK_X0], r[L.TRK_TX], r[L.TRK_ERR_X0],
+                     r[L.TRK_ERR_TX]]
+            for n in range(min(nh, 4)):
+                v[8 + 6 * n:14 + 6 * n] = [r[L.TRK_HIT_DETID + n], r[L.TRK_HIT_CHAN + n], r[L.TRK_HIT_POS + n],
+                                           r[L.TRK_HIT_DRIFT + n], r[L.TRK_HIT_SIGN + n], r[L.TRK_HIT_TDC + n]]
+            recs.append(v)
+            cnt[e] += 1
+    return cnt, np.array(recs, np.float32).reshape(-1, XZ_REC)
+
+
+def xz_from_pin(out, nout, events=None):
+    """Candidate records of xz_pin_kernel's output (records [n, 32, cap, 32],
+    counts [n, 32]) for the given events, in (event, thread, order) order."""
+    n = out.shape[0]
+    ev = range(n) if events is None else events
+    cnt = np.zeros(len(ev), np.int32)
+    recs = []
+    for i, e in enumerate(ev):
+        for t in range(32):
+            k = int(nout[e, t])
+            if k:
+                recs.append(out[e, t, :k])
+                cnt[i] += k
+    return cnt, (np.concatenate(recs) if recs else np.zeros((0, XZ_REC), np.float32)).astype(np.float32)
+
+
+def compare_xz(a, b, rtol=0.0):
+    """Per event, the multiset of candidates of a (counts, records) against
+    b's: candidates are matched on (binId, thread, hit ids, signs); fit fields
+    and hit floats bit for bit (rtol 0) or within rtol.  Returns a dict:
+    events, candidates, events whose candidate sets differ, candidates with a
+    fit difference, the largest relative fit difference."""
+    (ca, ra), (cb, rb) = a, b
+    oa = np.concatenate([[0], np.cumsum(ca)])
+    ob = np.concatenate([[0], np.cumsum(cb)])
+    disc = [0, 1, 2] + [8 + 6 * n + f for n in range(4) for f in (0, 1, 4)]
+    set_mismatch, value_mismatch, max_rel = [], [], 0.0
+    for e in range(len(ca)):
+        A, B = ra[oa[e]:oa[e + 1]], rb[ob[e]:ob[e + 1]]
+        ka = sorted(range(len(A)), key=lambda i: tuple(A[i, disc]))
+        kb = sorted(range(len(B)), key=lambda i: tuple(B[i, disc]))
+        if len(A) != len(B) or any(not np.array_equal(A[i, disc], B[j, disc]) for i, j in zip(ka, kb)):
+            set_mismatch.append(e)
+            continue
+        for i, j in zip(ka, kb):
+            x, y = A[i], B[j]
+            if rtol == 0.0:
+                if not np.array_equal(x.view(np.uint32), y.view(np.uint32)):
+                    value_mismatch.append((e, int(x[0])))
+            else:
+                d = np.abs(x.astype(np.float64) - y) / np.maximum(np.abs(y.astype(np.float64)), 1e-30)
+                d[(x == y)] = 0.0
+                m = float(d[XZ_FIT].max())
+                max_rel = max(max_rel, m)
+                if m > rtol:
+                    value_mismatch.append((e, int(x[0])))
+    return {"events": int(len(ca)), "candidates": int(ca.sum()), "set_mismatch": set_mismatch[:20],
+            "n_set_mismatch": len(set_mismatch), "value_mismatch": value_mismatch[:20],
+            "n_value_mismatch": len(value_mismatch), "max_rel_fit": max_rel}

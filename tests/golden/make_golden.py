@@ -9,6 +9,11 @@ oracle's state before that stage (injection), and its output is compared with
 the oracle's:
 
   ER      gkernel_eR on the packed raw hits      -> reduced hit lists, flags
+  XZ      xz_pin_kernel (oracle/ref/xz_pin.cuh) on the oracle's reduced hits:
+          the XZ candidates computed by the reference's own helpers (hit
+          pairing, x at y = 0, both fits, left/right resolution, hodoscope
+          matches), compared as per-event multisets with the oracle's
+          tracklets, since the reference's XZ kernel itself cannot be run
   YZ      gKernel_YZ_tracking on the oracle's XZ tracklets
   clean   gKernel_BackTrackCleaning + ..._crossthreads on the oracle's YZ output
   global  gKernel_Global_tracking on the oracle's cleaned tracks
@@ -20,9 +25,15 @@ the oracle's:
           with seeded trigger words, one event per launch (its "+=" from
           concurrent blocks would lose counts)
 
-The reference XZ kernel is not run (barriers in divergent code).  Events
-are first checked against the reference's array bounds with the oracle's
+The reference XZ kernel itself is not run (barriers in divergent code).
+Events are first checked against the reference's array bounds with the oracle's
 domain counters; events outside them are not given to the reference.
+
+The library is also built a second time with nvcc's default multiply-add
+contraction (build_lib.build(fmad=True), liborgpu_fmad1.so) and its stages,
+fed the same oracle states, are compared with the fmad1 image: how close the
+library comes to the reference as its Makefile builds it when compiled the
+same way ("lib_fmad1" in the report).
 
 Outputs (under --out):
   golden_report.json      per image and stage: events, matches, mismatches
@@ -133,6 +144,10 @@ def run_reference(rk, plane, snap, n):
     out["t_er"] = time.time() - t0
     out["hits_er"] = rk.get_hits(n)
     out["flags_er"] = rk.get_flags(n)
+    # XZ candidates on the reference's helpers, from the oracle's reduced hits
+    rk.put_hits(snap.hits_er)
+    rk.put_flags(snap.toomany_er)
+    out["xz"] = rk.xz_candidates(n)
     # YZ
     rk.put_hits(snap.hits_er)
     rk.put_tracks(snap.tracks_xz)
@@ -178,6 +193,7 @@ def compare(snap, ref, rtol):
     rep["er_flags"] = {"accepted_by_oracle": int((snap.toomany_er == 0).sum()),
                        "recomputed_vs_oracle_mismatch": int((flags_re != snap.toomany_er).sum()),
                        "reference_raw_vs_oracle_mismatch": int((flags_ref != snap.toomany_er).sum())}
+    rep["xz"] = compare_xz(snap, ref["xz"], rtol)
     for stage, want in (("yz", snap.tracks_yz), ("clean", snap.tracks_clean), ("global", snap.tracks_global),
                         ("sel", snap.tracks_sel)):
         a = G.compact_tracks(ref["tracks_" + stage], snap.toomany_xz)
@@ -205,6 +221,83 @@ def compare(snap, ref, rtol):
     return rep
 
 
+def run_library(rc, snap, n):
+    """The library's stages on a context `rc`, each fed the oracle's state
+    before that stage (as the reference kernels are)."""
+    import torch
+    from orgpu import pipeline
+    b = pipeline.DeviceBatch(n)
+    out = {}
+
+    def flags(f):
+        b.toomany.copy_(torch.from_numpy(np.ascontiguousarray(f, np.uint8)))
+
+    b.upload_hits(snap.hits0)
+    flags(np.zeros(n, np.uint8))
+    rc.event_reduce(b)
+    rc.sync()
+    out["hits_er"] = b.download_hits()
+    for stage, hits_in, tracks_in, flags_in, call in (
+            ("xz", snap.hits_er, None, snap.toomany_er, rc.xz_tracking),
+            ("yz", snap.hits_er, snap.tracks_xz, snap.toomany_xz, rc.yz_tracking),
+            ("clean", snap.hits_er, snap.tracks_yz, snap.toomany_xz, rc.back_track_cleaning),
+            ("global", snap.hits_er, snap.tracks_clean, snap.toomany_xz, rc.global_tracking),
+            ("sel", snap.hits_er, snap.tracks_global, snap.toomany_xz, rc.selection)):
+        b.upload_hits(hits_in)
+        if tracks_in is not None:
+            b.upload_tracks(tracks_in)
+        flags(flags_in)
+        b.ntracklets.zero_()
+        call(b)
+        rc.sync()
+        out["tracks_" + stage] = b.download_tracks()
+        out["flags_" + stage] = b.toomany.cpu().numpy()
+    return out
+
+
+def compare_library(lib_out, ref, snap, rtol):
+    """A library build's stage outputs against a reference image's, each
+    stage on the same oracle input."""
+    rep = {}
+    er = G.compare_hits(G.compact_hits(ref["hits_er"]), G.compact_hits(lib_out["hits_er"]))
+    rep["er_hits"] = {"n_mismatch": len(er)}
+    acc = np.nonzero(snap.toomany_xz == 0)[0]
+    pin = G.xz_from_pin(ref["xz"][0], ref["xz"][1], acc)
+    lib_xz = G.xz_from_tracks(_take_tracks(lib_out["tracks_xz"], acc), None)
+    r = G.compare_xz(lib_xz, pin, rtol)
+    rep["xz"] = {k: r[k] for k in ("candidates", "n_set_mismatch", "n_value_mismatch", "max_rel_fit")}
+    for stage in ("yz", "clean", "global", "sel"):
+        r = G.compare_tracks(G.compact_tracks(lib_out["tracks_" + stage], snap.toomany_xz),
+                             G.compact_tracks(ref["tracks_" + stage], snap.toomany_xz), rtol)
+        rep[stage] = {"tracks": r.get("tracks"), "n_count_mismatch": len(r["count_mismatch"]),
+                      "n_discrete_mismatch": len(r["discrete_mismatch"]),
+                      "n_value_mismatch": len(r["value_mismatch"]), "max_rel_fit": r["max_rel_fit"]}
+    return rep
+
+
+def compare_xz(snap, pin, rtol):
+    """The XZ candidates of the reference's helpers against the oracle's
+    tracklets, on the events the oracle's XZ stage accepts; and, for the
+    events it rejects, whether the reference threads see the same cause: a
+    bin with more than 20 pairs (K:359-375) or more accepted candidates than
+    the 512 tracklet slots (16 per thread, per station-3 half) hold
+    (K:719-723, K:824-839)."""
+    out, nout, st = pin
+    acc = np.nonzero(snap.toomany_xz == 0)[0]
+    a = G.xz_from_pin(out, nout, acc)
+    b = G.xz_from_tracks(_take_tracks(snap.tracks_xz, acc), None)
+    r = G.compare_xz(a, b, rtol)
+    r["threads_out_full"] = int(((st & 4) != 0).sum())
+    r["threads_out_of_domain"] = int(((st & 2) != 0).sum())
+    rej = np.nonzero((snap.toomany_xz != 0) & (snap.toomany_er == 0))[0]
+    over = ((st[rej] & 1) != 0).any(axis=1)
+    par = np.stack([nout[rej][:, 0::2].sum(1), nout[rej][:, 1::2].sum(1)], 1) if len(rej) else np.zeros((0, 2))
+    full = (par.sum(1) >= L.TRKMAX) | (par > L.NSLOTS // 2 * L.SLOTCAP).any(1)
+    r["oracle_rejected"] = int(len(rej))
+    r["rejected_same_cause"] = int((over | full).sum())
+    return r
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.join(REPO, "out", "golden"))
@@ -217,6 +310,9 @@ def main():
     report = {"configs": {}}
     fixture = {}
     images = {v: refrun.RefKernels(v) for v in ("fmad0", "fmad1")}
+    import build_lib
+    from orgpu import _lib, pipeline
+    rc_fmad1 = pipeline.Reconstruction(plane, 0, lib=_lib.load(build_lib.build(fmad=True)))
     for name, cfg, n_all, n_fix in CONFIGS:
         rec, off, _ = S.generate(geo, cfg)
         rec, off = S.cap_records(rec, off)
@@ -246,6 +342,8 @@ def main():
         for v, rk in images.items():
             ref = run_reference(rk, plane, snap, n)
             crep[v] = compare(snap, ref, 0.0 if v == "fmad0" else 1e-5)
+            if v == "fmad1":
+                crep["lib_fmad1_vs_ref_fmad1"] = compare_library(run_library(rc_fmad1, snap, n), ref, snap, 1e-5)
             sub = _subset(ref, fix)
             for key, arr in sub.items():
                 fixture[f"{name}/{v}/{key}"] = arr
@@ -259,6 +357,7 @@ def main():
         print(name, json.dumps({k: crep[k] for k in ("generated", "in_domain")}), flush=True)
     for rk in images.values():
         rk.close()
+    rc_fmad1.close()
     with open(os.path.join(args.out, "golden_report.json"), "w") as f:
         json.dump(report, f, indent=1)
     np.savez_compressed(os.path.join(args.out, "ref_e906.npz"), **fixture)
@@ -271,6 +370,7 @@ def _subset(ref, idx):
     h = _take_hits(ref["hits_er"], idx)
     out["er_counts"], out["er_hits"] = G.compact_hits(h)
     out["er_flags"] = ref["flags_er"][idx]
+    out["xz_count"], out["xz_records"] = G.xz_from_pin(ref["xz"][0], ref["xz"][1], idx)
     for stage in ("yz", "clean", "global", "sel", "vtx"):
         t = _take_tracks(ref["tracks_" + stage], idx)
         nt, w, r = G.compact_tracks(t)
@@ -307,6 +407,8 @@ def _summary(report):
                                 **{st: [r[st]["n_count_mismatch"], r[st]["n_discrete_mismatch"],
                                         r[st]["n_value_mismatch"], r[st]["max_rel_fit"]]
                                    for st in ("yz", "clean", "global", "sel", "vtx")},
+                                "xz": [r["xz"]["n_set_mismatch"], r["xz"]["n_value_mismatch"], r["xz"]["max_rel_fit"],
+                                       r["xz"]["oracle_rejected"] - r["xz"]["rejected_same_cause"]],
                                 "dim": [r["dim"]["n_count_mismatch"], r["dim"]["n_value_mismatch"]],
                                 "hist": r["hist"]["differing_tables"]}
     return s

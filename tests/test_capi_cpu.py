@@ -10,7 +10,7 @@ from conftest import REPO
 
 def _declared_functions():
     names = set()
-    for h in ("or_gb300.h", "or_layout.h"):
+    for h in ("or_gb300.h", "or_layout.h", "or_dropin.h"):
         text = open(os.path.join(REPO, "include", h)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         names |= set(re.findall(r"^[A-Za-z_][\w \*]*?\b(or_\w+)\s*\(", text, flags=re.M))
@@ -21,7 +21,7 @@ def test_library_exports_every_declared_function():
     from orgpu import _lib
     lb = _lib.lib()
     declared = _declared_functions()
-    assert "or_run_batch" in declared and "or_yz_noalloc" in declared
+    assert "or_run_batch" in declared and "or_yz_noalloc" in declared and "or_gKernel_YZ_tracking" in declared
     assert declared == set(_lib.EXPORTS)
     for name in declared:
         getattr(lb, name)

@@ -8,7 +8,9 @@ HasTooManyHits flag, nTracklets, slot counts, every track record):
     5,000 events (events are independent), each chunk compared on the
     device with its rows of the GPU batch;
   - the small configuration at exactly its size: 1,000 one-dimuon events
-    with Poisson(150) noise, seed 906001.
+    with Poisson(150) noise, seed 906001;
+  - 20,000 events of the high-occupancy workload (two muons, Poisson(1000)
+    noise, after-pulses), every one of which the event reducer rejects.
 
 And through properties that do not need the oracle:
 
@@ -111,6 +113,24 @@ def test_small_config_1000_events_bit_exact_with_oracle(geometry):
     total = _assert_oracle_equal(plane, geo, rec, off, 1000)
     assert total["global_tracks"] > 1000
     print("small configuration, 1,000 events:", total)
+
+
+def test_high_occupancy_rejection_equals_oracle(geometry):
+    """The high-occupancy workload (two muons, Poisson(1000) noise, 10 %
+    after-pulses; 20,000 events): every stage's output equals the oracle's
+    bit for bit, and the event reducer's station limits reject every event,
+    in the library as in the oracle."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from orgpu import synth as S
+    plane, wp = geometry
+    geo = S.Geometry(plane, wp)
+    rec, off, _ = S.generate(geo, S.config_high_occupancy(20000, 906004))
+    rec, off = S.cap_records(rec, off)
+    b = _run_device(plane, geo, rec, off)
+    assert bool((b.toomany != 0).all())
+    _assert_oracle_equal(plane, geo, rec, off, 5000)
 
 
 def _valid_tracks(nt, tr):
