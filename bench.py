@@ -484,41 +484,82 @@ def rt_leg(args, rc, b, plane, rec, d_rec, d_off, d_wp, dev):
 
 
 def learned_leg(args, rc, b_plain, rec, off, d_rec, d_off, d_wp, plain_value, dev):
-    """The learned path (scorer + pruned YZ) on the same batch: events/s,
-    and recall against the plain run of the last timed step."""
+    """The learned path on the same batch: the combination scorer (rows =
+    live (u3, v3) outer iterations of the queued YZ tracklets, pruned on the
+    tensor cores' scores, or_run_batch_scored) when its model is present,
+    and the tracklet scorer (or_run_batch_learned) beside it.  Events/s and,
+    against the plain run of the last timed step, the recall of global tracks
+    and of dimuons (tracks bit for bit), learned tracks absent from the plain
+    output, rows kept and uncertain events."""
+    import os as _os
     import torch
     from orgpu import learned, pipeline
     n = b_plain.n
-    sp = learned.ScorerParams.load()
+    stream = torch.cuda.current_stream(dev)
+    bl = pipeline.DeviceBatch(n, dev.index)
     lrn = learned.Learned(rc)
+
+    def timed(step):
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        rc.sync()
+        return e0.elapsed_time(e1) / args.steps
+
+    def agreement(ms, sp, path):
+        n_ref, n_match, n_new = lrn.agreement(b_plain, bl)
+        d_ref, d_rep, d_new, dt_ref, dt_rep = learned.dimuon_agreement(rc, b_plain, bl, dev.index)
+        return {"value": n / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms, "plain_value": plain_value,
+                "ratio_vs_plain": (n / (ms / 1000.0)) / plain_value,
+                "recall": n_match / n_ref if n_ref else 1.0, "plain_global_tracks": n_ref,
+                "reproduced": n_match, "learned_global_tracks": n_new,
+                "learned_tracks_not_in_plain": n_new - n_match,
+                "dimuon_recall": d_rep / d_ref if d_ref else 1.0, "plain_dimuons": d_ref,
+                "dimuons_reproduced": d_rep, "learned_dimuons": d_new,
+                "dimuon_track_recall": dt_rep / dt_ref if dt_ref else 1.0,
+                "model": path, "t_keep": sp.t_keep, "t_unc": sp.t_unc}
+
+    out = None
+    if _os.path.exists(learned.MODEL_COMBO_E906):
+        sp = learned.ScorerParams.load(learned.MODEL_COMBO_E906)
+        cs = learned.ComboScorer(rc)
+        model = learned.DeviceModel(sp, dev.index)
+        orows = learned.OuterRows(n, device=dev.index)
+
+        def step_combo():
+            rc.pack(bl, d_rec, d_off, d_wp)
+            cs.run_batch(bl, orows, model, sp.t_keep, sp.t_unc)
+
+        ms = timed(step_combo)
+        nr = orows.n_rows()
+        out = agreement(ms, sp, "e1039-gpu_gb300/data/combo_scorer_e906.npz")
+        out.update({"scorer": "combination scorer: (u3, v3) outer iterations of queued YZ tracklets",
+                    "rows": nr, "rows_kept": float((orows.scores[:nr] >= sp.t_keep).float().mean().item()) if nr
+                    else 1.0, "uncertain_events": int(orows.uncertain[:n].sum().item())})
+        del orows
+    sp = learned.ScorerParams.load()
     model = learned.DeviceModel(sp, dev.index)
     r = learned.TrackletRows(n, device=dev.index)
-    bl = pipeline.DeviceBatch(n, dev.index)
-    stream = torch.cuda.current_stream(dev)
 
-    def step():
+    def step_tracklet():
         rc.pack(bl, d_rec, d_off, d_wp)
         lrn.run_batch(bl, r, model, sp.t_keep, sp.t_unc)
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
-    n_ref, n_match, n_new = lrn.agreement(b_plain, bl)
+    ms = timed(step_tracklet)
     nr = r.n_rows()
-    rc.sync()
-    return {"value": n / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms, "plain_value": plain_value,
-            "ratio_vs_plain": (n / (ms / 1000.0)) / plain_value,
-            "recall": n_match / n_ref if n_ref else 1.0, "plain_global_tracks": n_ref,
-            "reproduced": n_match, "learned_global_tracks": n_new,
-            "kept_share": float(r.keep[:nr].float().mean().item()) if nr else 1.0,
-            "model": "e1039-gpu_gb300/data/scorer_e906.npz", "t_keep": sp.t_keep, "t_unc": sp.t_unc}
+    tk = agreement(ms, sp, "e1039-gpu_gb300/data/scorer_e906.npz")
+    tk.update({"scorer": "tracklet scorer: XZ tracklets",
+               "kept_share": float(r.keep[:nr].float().mean().item()) if nr else 1.0})
+    if out is None:
+        return tk
+    out["tracklet_scorer"] = tk
+    return out
 
 
 def config4_leg(args, rc, b, plane, wp, dev, with_learned=True, chunks=5, seed=906004):
@@ -545,11 +586,13 @@ def config4_leg(args, rc, b, plane, wp, dev, with_learned=True, chunks=5, seed=9
     d_wp = torch.from_numpy(wp.astype(np.float32).reshape(-1)).to(dev)
     lrn = sp = model = r = bl = None
     if with_learned:
-        sp = learned.ScorerParams.load()
-        lrn = learned.Learned(rc)
+        combo = os.path.exists(learned.MODEL_COMBO_E906)
+        sp = learned.ScorerParams.load(learned.MODEL_COMBO_E906 if combo else learned.MODEL_E906)
+        lrn = learned.ComboScorer(rc) if combo else learned.Learned(rc)
         model = learned.DeviceModel(sp, dev.index)
-        r = learned.TrackletRows(n, device=dev.index)
+        r = learned.OuterRows(n, device=dev.index) if combo else learned.TrackletRows(n, device=dev.index)
         bl = pipeline_batch(n, dev)
+        agree_lrn = learned.Learned(rc)
     ms_plain, ms_learned, rejected, records, tracks = 0.0, 0.0, 0, 0, 0
     agree = [0, 0, 0]
     for rec4, off4 in parts:
@@ -575,7 +618,7 @@ def config4_leg(args, rc, b, plane, wp, dev, with_learned=True, chunks=5, seed=9
         rc.sync()
         rejected += int(b.toomany.sum().item())
         if with_learned:
-            a = lrn.agreement(b, bl)
+            a = agree_lrn.agreement(b, bl)
             agree = [x + y for x, y in zip(agree, a)]
         del d_rec, d_off
     total = n * len(parts)
@@ -591,6 +634,10 @@ def config4_leg(args, rc, b, plane, wp, dev, with_learned=True, chunks=5, seed=9
                           "reproduced": agree[1], "learned_global_tracks": agree[2],
                           "recall": (agree[1] / agree[0]) if agree[0] else None}
     return out
+
+
+def _os_rel(path):
+    return os.path.relpath(path, REPO)
 
 
 def pipeline_batch(n, dev):
@@ -648,11 +695,12 @@ def serving_leg(plane, wp, tuned=None, pool_events=40000, burst_s=4.0, seed=9060
     del srv
     gc.collect()
     torch.cuda.empty_cache()
+    model_path = learned.MODEL_COMBO_E906 if os.path.exists(learned.MODEL_COMBO_E906) else learned.MODEL_E906
     lsrv = serving.Server(plane, wp, slot_events=10000, max_slots=4, rec_per_event=400, launch_config=tuned,
-                          scorer=learned.ScorerParams.load())
+                          scorer=learned.ScorerParams.load(model_path))
     lcal = lsrv.serve([(0.0,) + take(10000) for _ in range(12)])
     learned_res = {"slots": len(lsrv.slots), "capacity_events_per_s": serving.latency_stats(lcal)["events_per_s"],
-                   "loads": run_loads(lsrv)}
+                   "model": _os_rel(model_path), "loads": run_loads(lsrv)}
     del lsrv
     gc.collect()
     torch.cuda.empty_cache()

@@ -34,6 +34,11 @@ cudaError_t launch_pack(const or_hit_record_t *, const int64_t *, int, const flo
                         or_hits_view_t, uint32_t *, cudaStream_t, int);
 cudaError_t launch_wait_selftest(uint32_t *, uint32_t, cudaStream_t);
 cudaError_t yz_read_counts(const void *, long long[3]);
+cudaError_t launch_yz_scored(const or_plane_t *, or_hits_view_t, or_tracks_view_t, const uint8_t *, int, uint32_t *,
+                             void *, int, int, int, cudaStream_t, int, const or_mlp_t *, float, float, float *,
+                             int32_t *, float *, uint32_t *, uint8_t *, long, int, long long, int);
+cudaError_t launch_yz_outer_labels(void *, int, int, int, or_tracks_view_t, const uint8_t *, const int32_t *,
+                                   const uint32_t *, long, uint8_t *, cudaStream_t, int);
 cudaError_t launch_rt_apply(const or_rt_table_t *, or_hits_view_t, int, cudaStream_t, int);
 cudaError_t launch_collect(or_tracks_view_t, const uint8_t *, int, float, float *, long long, unsigned long long *,
                            cudaStream_t);
@@ -298,6 +303,56 @@ int or_yz(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uin
                                            ctx->yz_garena_warps, S(stream), ctx->sm_count, ctx->warps[OR_K_YZ],
                                            ctx->yz_pool_limit, ctx->yz_count_work);
     return e == cudaSuccess ? OR_OK : cuda_fail(e, "YZ launch");
+}
+
+int or_yz_scored(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany, int n_events,
+                 const or_mlp_t *model, float t_keep, float t_unc, float *features, int32_t *outer_index,
+                 float *scores, uint32_t *rows, uint8_t *uncertain, int64_t max_rows, void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany || !features || !outer_index || !scores || !rows || !uncertain || max_rows < 0 ||
+        !aligned16(features))
+        return fail(OR_ERR_ARG, "bad scored-YZ arguments (features must be 16-byte aligned)");
+    if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
+    cudaError_t e = orgpu::launch_yz_scored(ctx->d_plane, hits, tracks, toomany, n_events, ctx->d_errw,
+                                            ctx->yz_scratch, ctx->yz_cap_units, ctx->yz_cap_heavy,
+                                            ctx->yz_garena_warps, S(stream), ctx->sm_count, model, t_keep, t_unc,
+                                            features, outer_index, scores, rows, uncertain, (long)max_rows,
+                                            ctx->warps[OR_K_YZ], ctx->yz_pool_limit, ctx->yz_count_work);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "scored YZ launch");
+}
+
+int or_outer_labels(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, const int32_t *outer_index,
+                    const uint32_t *rows, int64_t max_rows, uint8_t *labels, void *stream) {
+    int rc = check_ctx(ctx, false);
+    if (rc) return rc;
+    if (!toomany || !outer_index || !rows || !labels || max_rows < 0) return fail(OR_ERR_ARG, "bad label arguments");
+    if ((rc = check_tracks(tracks))) return rc;
+    cudaError_t e = cudaMemsetAsync(labels, 0, (size_t)max_rows, S(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "clear labels");
+    e = orgpu::launch_yz_outer_labels(ctx->yz_scratch, ctx->yz_cap_units, ctx->yz_cap_heavy, ctx->yz_garena_warps,
+                                      tracks, toomany, outer_index, rows, (long)max_rows, labels, S(stream),
+                                      ctx->sm_count);
+    return e == cudaSuccess ? OR_OK : cuda_fail(e, "label launch");
+}
+
+int or_run_batch_scored(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, int32_t *ntracklets,
+                        uint8_t *toomany, int n_events, const or_mlp_t *model, float t_keep, float t_unc,
+                        float *features, int32_t *outer_index, float *scores, uint32_t *rows, uint8_t *uncertain,
+                        int64_t max_rows, void *stream) {
+    int rc = check_ctx(ctx, true);
+    if (rc) return rc;
+    if (n_events < 0 || !toomany || !ntracklets) return fail(OR_ERR_ARG, "bad event count or output arrays");
+    if ((rc = check_hits(hits)) || (rc = check_tracks(tracks))) return rc;
+    cudaError_t e = cudaMemsetAsync(ntracklets, 0, sizeof(int32_t) * (size_t)n_events, S(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "clear tracklet counts");
+    if ((rc = or_event_reduce(ctx, hits, toomany, n_events, stream))) return rc;
+    if ((rc = or_xz(ctx, hits, tracks, ntracklets, toomany, n_events, stream))) return rc;
+    if ((rc = or_yz_scored(ctx, hits, tracks, toomany, n_events, model, t_keep, t_unc, features, outer_index, scores,
+                           rows, uncertain, max_rows, stream)))
+        return rc;
+    if ((rc = or_back_clean(ctx, tracks, toomany, n_events, stream))) return rc;
+    return or_global(ctx, hits, tracks, toomany, n_events, stream);
 }
 
 int or_set_yz_work_counting(or_ctx_t *ctx, int enabled) {

@@ -128,6 +128,9 @@ struct YzUnit {
     int g0, g1;
     int pad;
     Stale entry[4];
+    // the unit's live outer iterations as the combination scorer's rows of
+    // its tracklet: ranks [r0, r1)
+    int r0, r1;
 };
 // a heavy tracklet
 struct YzHeavy {
@@ -206,13 +209,14 @@ struct YzPrune {
     // iteration of every queued (heavy) tracklet, written by the planning
     // pass; scores filled before the first cut; an outer iteration scoring
     // below t_keep is skipped, unless its event is uncertain (unc[e])
-    float *ofeat;         // [cap_orows * OR_NFEAT]; nullptr: no outer rows
-    int32_t *og;          // [cap_orows] outer index g of each row
-    const float *oscore;  // [cap_orows]; nullptr: rows written, nothing pruned
-    uint32_t *orows;      // row counter
-    const uint8_t *unc;   // [n_events] uncertain events
+    float *ofeat;          // [cap_orows * OR_NFEAT]; nullptr: no outer rows
+    int32_t *og;           // [cap_orows] outer index g of each row
+    float *oscore;         // [cap_orows]
+    uint32_t *orows;       // row counter
+    uint8_t *unc;          // [n_events] uncertain events
+    const or_mlp_t *model; // nullptr: rows written, nothing scored or pruned
     long cap_orows;
-    float t_keep;
+    float t_keep, t_unc;
 };
 
 
@@ -516,8 +520,25 @@ __device__ __forceinline__ int s3_count(const YzWarp &S, const YzHit *base, int 
 // outer iteration that reaches it.  When `units` is given, the state at the
 // start of every unit (each `gper` outer iterations) is stored there.  `st`
 // goes in as the state before the tracklet and comes out as the state after.
+// live outer iterations (both pairs alive) before outer index g, g <= G:
+// the scorer-row rank of g when g is live
+__device__ __forceinline__ int live_before(const unsigned mu[4], const unsigned mv[4], int nu3, int g) {
+    const int iu = g % nu3, iv = g / nu3;
+    int below_v = 0, below_u = 0, au = 0;
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        au += __popc(mu[w]);
+        if (w < (iv >> 5)) below_v += __popc(mv[w]);
+        else if (w == (iv >> 5)) below_v += __popc(mv[w] & ((1u << (iv & 31)) - 1u));
+        if (w < (iu >> 5)) below_u += __popc(mu[w]);
+        else if (w == (iu >> 5)) below_u += __popc(mu[w] & ((1u << (iu & 31)) - 1u));
+    }
+    const bool v_live = iv < 128 && ((mv[iv >> 5] >> (iv & 31)) & 1u);
+    return below_v * au + (v_live ? below_u : 0);
+}
+
 __device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gper, Stale st[4], YzUnit *units,
-                               int heavy) {
+                               int heavy, const unsigned *alive_u = nullptr, const unsigned *alive_v = nullptr) {
     const int lane = lane_id();
     const int nu2 = S.np[0], nu3 = S.np[2];
     const int C2 = S.np[0] * S.np[1];
@@ -583,6 +604,8 @@ __device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gp
             u.g0 = g;
             u.g1 = min(G, g + gper);
             u.pad = 0;
+            u.r0 = alive_u ? live_before(alive_u, alive_v, nu3, u.g0) : 0;
+            u.r1 = alive_u ? live_before(alive_u, alive_v, nu3, u.g1) : 0;
 #pragma unroll
             for (int k = 0; k < 4; ++k) u.entry[k] = ent[k];
         }
@@ -979,10 +1002,93 @@ __device__ void yz_outer_features(const YzWarp &S, const YzEvent &E, const YzHit
     f[15] = (float)S.nhx;
 }
 
-template <bool FIRST_ONLY>
+// The station-2 load attempts of an outer iteration do not depend on the
+// iteration (only on the inner pair, K:1467-1597): the last inner combination
+// writing scratch offset m (past the station-3 hit count) is the same in
+// every live outer iteration.  Returns those hits as arena offsets, 16 bits
+// per offset m = 0..3, 0xFFFF where no combination writes m.
+__device__ unsigned long long yz_last_writes(const YzWarp &S, const YzHit *base) {
+    const int lane = lane_id();
+    const int nu2 = S.np[0];
+    const int C2 = S.np[0] * S.np[1];
+    unsigned long long lasto = ~0ull;
+#pragma unroll 1
+    for (int b0 = 0; b0 < C2; b0 += 32) {
+        const int c = b0 + lane;
+        int mine[4] = {-1, -1, -1, -1};
+        if (c < C2) {
+            const S2Writes w = s2_writes(S, base, c % nu2, c / nu2);
+#pragma unroll
+            for (int k = 0; k < w.n; ++k) mine[w.off[k]] = (int)(w.hit[k] - base);
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const int l = last_lane(__ballot_sync(0xffffffffu, mine[m] >= 0));
+            if (l >= 0) {
+                const unsigned long long o = (unsigned long long)(unsigned)__shfl_sync(0xffffffffu, mine[m], l);
+                lasto = (lasto & ~(0xFFFFull << (16 * m))) | (o << (16 * m));
+            }
+        }
+    }
+    return lasto;
+}
+
+// Skip the pruned live outer iterations from rank r (the scorer's rows of
+// the tracklet are its live outer iterations in loop order): returns the
+// rank of the next kept one (nrows when none) and, when one follows, sets
+// the scratch entries 4..7 as the skipped iterations' load attempts leave
+// them in the reference -- for each entry, the last skipped iteration whose
+// station-3 hit count puts one of its writes there -- so that the kept
+// combinations read the same stale entries as in the plain run.
+__device__ __noinline__ int yz_skip_pruned(const YzWarp &S, const YzHit *base, const YzAlive &al, int Au, int nrows,
+                                           const float *__restrict__ osc, float t_keep, unsigned long long lasto,
+                                           int r, int r_end, Stale st[4]) {
+    const int lane = lane_id();
+    int rk = nrows;  // no kept iteration before the range's end rank r_end
+#pragma unroll 1
+    for (int b = r; b < r_end; b += 32) {
+        const int j = b + lane;
+        const unsigned m = __ballot_sync(0xffffffffu, j < r_end && osc[j] >= t_keep);
+        if (m) {
+            rk = b + __ffs(m) - 1;
+            break;
+        }
+    }
+    if (rk >= nrows) return rk;
+    unsigned done = 0u;
+#pragma unroll 1
+    for (int b = rk - 1; b >= r && done != 0xFu; b -= 32) {
+        const int j = b - lane;  // lane 0 holds the latest rank of the chunk
+        int n3 = 0;
+        if (j >= r) {
+            bool v;
+            n3 = s3_count(S, base, nth_bit128(al.u, j % Au), nth_bit128(al.v, j / Au), v);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (done & (1u << k)) continue;
+            const int mm = k + 4 - n3;
+            const bool ok = j >= r && mm >= 0 && mm < 4 && ((lasto >> (16 * mm)) & 0xFFFFull) != 0xFFFFull;
+            const unsigned m = __ballot_sync(0xffffffffu, ok);
+            if (m) {
+                const int src = __shfl_sync(0xffffffffu, mm, __ffs(m) - 1);
+                const YzHit &h = base[(int)((lasto >> (16 * src)) & 0xFFFFull)];
+                const Stale v{h.det, h.pos, h.drift};
+                __syncwarp();
+                st[k] = v;
+                done |= 1u << k;
+            }
+        }
+    }
+    __syncwarp();
+    return rk;
+}
+
+template <bool FIRST_ONLY, bool PRUNE = false>
 __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l, long c1l,
                                          Stale st[4], const or_plane_t &P, const YzTab *__restrict__ tab,
-                                         PassEntryStore *Q, int qcap, int *nsurv) {
+                                         PassEntryStore *Q, int qcap, int *nsurv, const float *__restrict__ osc = nullptr,
+                                         float t_keep = 0.f) {
     const int lane = lane_id();
     const int nu2 = S.np[0], nu3 = S.np[2];
     const int C2 = S.np[0] * S.np[1];
@@ -1011,6 +1117,19 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
         s3 = sg / nu3;
     }
     const YzAlive alive = yz_alive(S, base);
+    // the combination scorer (PRUNE): live outer iterations scoring below
+    // t_keep are skipped; `osc` holds the tracklet's scores in loop order
+    int Au = 0, nrows = 0, r_end = 0;
+    unsigned long long lasto = ~0ull;
+    if constexpr (PRUNE) {
+        if (osc) {
+            Au = bits128(alive.u);
+            nrows = Au * bits128(alive.v);
+            r_end = live_before(alive.u, alive.v, nu3, (c1 + C2 - 1) / C2);  // rows of the range's outer iterations
+            lasto = yz_last_writes(S, base);
+        }
+    }
+    bool pruned3 = false;
     // station-3 part of the lane's current outer iteration (iu3, iv3): the
     // fit's right-hand side over its accepted hits in the reference order,
     // their count, the table offset of its plane set, and whether both u3
@@ -1032,6 +1151,26 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
                 basec = gn < 0 ? c1 : min(gn * C2, c1);
                 if (basec < c1) set_digits(basec);
                 need3 = true;
+            }
+        }
+        if constexpr (PRUNE) {
+            // the chunk's first combination in a pruned live outer
+            // iteration: jump to the next kept one, with the scratch entries
+            // the skipped ones write
+            if (osc && basec < c1) {
+                const int iu = __shfl_sync(0xffffffffu, d2, 0), iv = __shfl_sync(0xffffffffu, d3, 0);
+                const int r = bits_below128(alive.v, iv) * Au + bits_below128(alive.u, iu);
+                if (osc[r] < t_keep) {
+                    const int rk = yz_skip_pruned(S, base, alive, Au, nrows, osc, t_keep, lasto, r, r_end, st);
+                    if (rk >= nrows) {
+                        basec = c1;
+                    } else {
+                        const int gk = nth_bit128(alive.u, rk % Au) + nth_bit128(alive.v, rk / Au) * nu3;
+                        basec = min(gk * C2, c1);
+                        if (basec < c1) set_digits(basec);
+                    }
+                    need3 = true;
+                }
             }
         }
         const bool more = basec < c1;
@@ -1086,6 +1225,10 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
                     n3 = nu + nv;
                     alive3 = nu > 0 && nv > 0;
                     tab3 = alive3 ? yz_tab_index(gu, gv, 1, 1) : 0;
+                    if constexpr (PRUNE) {
+                        pruned3 = osc && alive3 &&
+                                  osc[bits_below128(alive.v, d3) * Au + bits_below128(alive.u, d2)] < t_keep;
+                    }
                     need3 = false;
                 }
                 if (alive3) {
@@ -1131,7 +1274,7 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
                         const int off = (int)((offs >> (16 * a)) & 0xFFFFull);
                         if (off != 0xFFFF) attempt(off, a);
                     }
-                    if (nu2hits > n3 && nuv > nu2hits) {  // the v2 group gave a hit: the fit is reached
+                    if (nu2hits > n3 && nuv > nu2hits && !pruned3) {  // the v2 group gave a hit: the fit is reached
                         // Fit2::solve with the plane set's tabulated inverse
                         const YzTab *te = tab + tab3 + (g2 & 3) * 3 - 4 + (g2 >> 2);
                         const float4 ai = __ldg(reinterpret_cast<const float4 *>(te));
@@ -1455,7 +1598,7 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_PLAN_WARPS_SM / W > 0 ? OR_YZ_P
                             hv2.best_g = -1;
                             sc.heavy[hid] = hv2;
                         }
-                        yz_unit_states(S, base, (int)G, (int)gper, st, sc.units + u0, hid);
+                        yz_unit_states(S, base, (int)G, (int)gper, st, sc.units + u0, hid, al.u, al.v);
                     }
                 }
                 if (inline_it) {
@@ -1534,9 +1677,17 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_
 // Split path, first kernel: the first cut of every queued unit (no survivor
 // evaluation, so it needs far fewer registers and no per-lane hit arrays);
 // a unit's survivors go, in order, to one contiguous piece of the pool.
-template <int W>
+// the scores of a queued tracklet's live outer iterations, when the
+// combination scorer prunes it (rows written, event not uncertain)
+__device__ __forceinline__ const float *yz_tracklet_scores(const YzPrune &prune, const YzHeavy &h) {
+    if (!prune.model || h.orow0 < 0 || (prune.unc && prune.unc[h.e])) return nullptr;
+    return prune.oscore + h.orow0;
+}
+
+template <int W, bool PRUNE>
 __global__ void __launch_bounds__(W * 32, (OR_YZ_FIRST_WARPS_SM / W > 0 ? OR_YZ_FIRST_WARPS_SM / W : 1))
-    yz_first_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv, YzScratch sc) {
+    yz_first_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv, YzScratch sc,
+                    YzPrune prune) {
     extern __shared__ __align__(16) unsigned char yz_smem[];
     or_plane_t &P = *reinterpret_cast<or_plane_t *>(yz_smem);
     YzWarp *warps = reinterpret_cast<YzWarp *>(yz_smem + ((sizeof(or_plane_t) + 15) & ~size_t(15)));
@@ -1574,8 +1725,9 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_FIRST_WARPS_SM / W > 0 ? OR_YZ_
         __syncwarp();
         const long C2 = (long)S.np[0] * S.np[1];
         int ns = -1;
-        yz_range_t<true>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, sc.tab + YZ_TAB_SETS * (st3 - 3), Q,
-                         sc.qcap, &ns);
+        const float *osc = PRUNE ? yz_tracklet_scores(prune, hv2) : nullptr;
+        yz_range_t<true, PRUNE>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, sc.tab + YZ_TAB_SETS * (st3 - 3),
+                                Q, sc.qcap, &ns, osc, prune.t_keep);
         __syncwarp();
         long long off = -1;
         if (lane == 0 && ns >= 0) {
@@ -1600,9 +1752,10 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_FIRST_WARPS_SM / W > 0 ? OR_YZ_
 #ifndef OR_YZ_SECOND_WARPS_SM
 #define OR_YZ_SECOND_WARPS_SM 24
 #endif
-template <int W>
+template <int W, bool PRUNE>
 __global__ void __launch_bounds__(W * 32, (OR_YZ_SECOND_WARPS_SM / W > 0 ? OR_YZ_SECOND_WARPS_SM / W : 1))
-    yz_second_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv, YzScratch sc) {
+    yz_second_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv, YzScratch sc,
+                     YzPrune prune) {
     extern __shared__ __align__(16) unsigned char yz_smem[];
     or_plane_t &P = *reinterpret_cast<or_plane_t *>(yz_smem);
     YzWarp *warps = reinterpret_cast<YzWarp *>(yz_smem + ((sizeof(or_plane_t) + 15) & ~size_t(15)));
@@ -1626,6 +1779,10 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_SECOND_WARPS_SM / W > 0 ? OR_YZ
         const YzUnit un = sc.units[u];
         if (un.heavy < 0) continue;
         const int2 seg = sc.useg[u];
+        if (seg.x >= 0 && seg.y == 0) {  // no survivor: nothing to evaluate
+            if (lane == 0) sc.best[u].key = ~0ull;
+            continue;
+        }
         const YzHeavy hv2 = sc.heavy[un.heavy];
         const float *T = trk_rec(tv, hv2.e, hv2.slot, hv2.k);
         const int st3 = 3 + (hv2.slot & 1);
@@ -1644,8 +1801,9 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_SECOND_WARPS_SM / W > 0 ? OR_YZ
 #pragma unroll 1
             for (int k = 0; k < 4; ++k) st[k] = un.entry[k];
             __syncwarp();
-            bk = yz_range(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, sc.tab + YZ_TAB_SETS * (st3 - 3), Q,
-                          sc.qcap);
+            const float *osc = PRUNE ? yz_tracklet_scores(prune, hv2) : nullptr;
+            bk = yz_range_t<false, PRUNE>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P,
+                                          sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap, nullptr, osc, prune.t_keep);
         } else {
             Phase2Carry cs;
 #pragma unroll 1
@@ -1698,6 +1856,7 @@ __global__ void __launch_bounds__(128) yz_apply_kernel(or_tracks_view_t tv, YzSc
                 bu = ou;
             }
         }
+        if (lane == 0) sc.heavy[h].best_g = best == ~0ull ? -1 : (int)((unsigned)best / (unsigned)max(hv2.c2, 1));
         if (best == ~0ull) continue;
         float *T = trk_rec(tv, hv2.e, hv2.slot, hv2.k);
         const int nhx = min((int)T[OR_TRK_NHITS], 4);
@@ -1738,6 +1897,73 @@ __global__ void __launch_bounds__(256) yz_tab_kernel(const or_plane_t *__restric
     e.thr_y0 = Y0_MAX + 2 * e.ey0;
     e.thr_ty = TY_MAX + 2 * e.ety;
     tab[t] = e;
+}
+
+// Events the combination scorer leaves to the plain method: a queued
+// tracklet all of whose live outer iterations score below t_keep, the best
+// of them at or above t_unc -- the scorer would drop the whole tracklet
+// without a clear margin.  Such an event is evaluated without pruning.
+__global__ void __launch_bounds__(128) yz_unc_kernel(YzScratch sc, YzPrune prune) {
+    const int lane = threadIdx.x & 31;
+    const int nheavy = min((int)sc.counters[1], sc.cap_heavy);
+    const long ncap = min((long)*prune.orows, prune.cap_orows);
+#pragma unroll 1
+    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < nheavy; h += (gridDim.x * blockDim.x) >> 5) {
+        const YzHeavy hv2 = sc.heavy[h];
+        if (hv2.nunits <= 0 || hv2.orow0 < 0 || (long)hv2.orow0 + hv2.nrows > ncap) continue;
+        float mx = -1.f;
+#pragma unroll 1
+        for (int r = lane; r < hv2.nrows; r += 32) mx = fmaxf(mx, prune.oscore[hv2.orow0 + r]);
+#pragma unroll 1
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0 && mx < prune.t_keep && mx >= prune.t_unc) prune.unc[hv2.e] = 1;
+    }
+}
+
+// Units of pruned tracklets with no kept row in their rank range are dropped
+// before the first cut (their best key is "none"); everything they would
+// have done is skipped anyway, including the window rebuild.
+__global__ void __launch_bounds__(128) yz_kill_units_kernel(YzScratch sc, YzPrune prune) {
+    const int lane = threadIdx.x & 31;
+    const int nunits = min((int)sc.counters[0], sc.cap_units);
+    const long ncap = min((long)*prune.orows, prune.cap_orows);
+#pragma unroll 1
+    for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nunits; u += (gridDim.x * blockDim.x) >> 5) {
+        const YzUnit un = sc.units[u];
+        if (un.heavy < 0) continue;
+        const YzHeavy hv2 = sc.heavy[un.heavy];
+        if (hv2.orow0 < 0 || (long)hv2.orow0 + hv2.nrows > ncap || prune.unc[hv2.e]) continue;
+        bool kept = false;
+#pragma unroll 1
+        for (int r = un.r0 + lane; r < un.r1 && !kept; r += 32) kept = prune.oscore[hv2.orow0 + r] >= prune.t_keep;
+        if (!__any_sync(0xffffffffu, kept) && lane == 0) {
+            sc.units[u].heavy = -1;
+            sc.best[u].key = ~0ull;
+        }
+    }
+}
+
+// Labels of the scorer's rows after the plain chain: 1 for the row of the
+// outer iteration that holds its tracklet's best combination when the
+// tracklet ended as a global track (stationID 6 after global tracking), else
+// 0.  The scratch still holds the last YZ call's heavy tracklets.
+__global__ void __launch_bounds__(128) yz_outer_labels_kernel(YzScratch sc, or_tracks_view_t tv,
+                                                              const uint8_t *__restrict__ toomany,
+                                                              const int32_t *__restrict__ og, const uint32_t *orows,
+                                                              long cap, uint8_t *__restrict__ labels) {
+    const int lane = threadIdx.x & 31;
+    const int nheavy = min((int)sc.counters[1], sc.cap_heavy);
+    const long ncap = min((long)*orows, cap);
+#pragma unroll 1
+    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < nheavy; h += (gridDim.x * blockDim.x) >> 5) {
+        const YzHeavy hv2 = sc.heavy[h];
+        if (hv2.nunits <= 0 || hv2.orow0 < 0 || (long)hv2.orow0 + hv2.nrows > ncap) continue;
+        const float *T = trk_rec(tv, hv2.e, hv2.slot, hv2.k);
+        const bool global = !toomany[hv2.e] && T[OR_TRK_STID] == 6.f;
+#pragma unroll 1
+        for (int r = lane; r < hv2.nrows; r += 32)
+            labels[hv2.orow0 + r] = (global && og[hv2.orow0 + r] == hv2.best_g) ? 1 : 0;
+    }
 }
 
 size_t yz_smem_bytes(int warps) {
@@ -1784,24 +2010,14 @@ cudaError_t yz_read_counts(const void *scratch, long long out[3]) {
     return cudaSuccess;
 }
 
-template <int W>
-static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
-                                  const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
-                                  int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, YzPrune prune,
-                                  int qcap, long long pool_limit, int count_work) {
-    if (n_events <= 0) return cudaSuccess;
-    const size_t smem = yz_smem_bytes(W);
-    cudaError_t err;
-    if ((err = smem_attr_once((const void *)yz_plan_kernel<W>, (int)smem)))
-        return err;
-    if ((err = smem_attr_once((const void *)yz_work_kernel<W>, (int)smem)))
-        return err;
+// The pointers into a YZ scratch area (the layout yz_scratch_bytes_q sizes).
+static YzScratch yz_scratch_layout(void *scratch, int cap_units, int cap_heavy, int garena_warps, int qcap,
+                                   long long pool_limit) {
     char *p = static_cast<char *>(scratch);
     YzScratch sc;
     sc.counters = reinterpret_cast<unsigned int *>(p);
     p += 256;
-    YzTab *tab = reinterpret_cast<YzTab *>(p);
-    sc.tab = tab;
+    sc.tab = reinterpret_cast<YzTab *>(p);
     p += YZ_TAB_BYTES;
     sc.units = reinterpret_cast<YzUnit *>(p);
     p += sizeof(YzUnit) * (size_t)cap_units;
@@ -1829,6 +2045,33 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
     sc.cap_heavy = cap_heavy;
     sc.garena_warps = garena_warps;
     sc.qcap = qcap;
+    sc.count_work = 0;
+    return sc;
+}
+
+cudaError_t launch_mlp_score(const or_mlp_t *, const float *, long, const int32_t *, float *, uint32_t *, cudaStream_t,
+                             int);
+
+template <int W>
+static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
+                                  const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
+                                  int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, YzPrune prune,
+                                  int qcap, long long pool_limit, int count_work) {
+    if (n_events <= 0) return cudaSuccess;
+    const size_t smem = yz_smem_bytes(W);
+    cudaError_t err;
+    if (prune.ofeat) {
+        if ((err = cudaMemsetAsync(prune.orows, 0, sizeof(uint32_t), stream))) return err;
+        if (prune.unc && (err = cudaMemsetAsync(prune.unc, 0, (size_t)n_events, stream))) return err;
+    } else {
+        prune.model = nullptr;  // no rows: nothing to score or prune
+    }
+    if ((err = smem_attr_once((const void *)yz_plan_kernel<W>, (int)smem)))
+        return err;
+    if ((err = smem_attr_once((const void *)yz_work_kernel<W>, (int)smem)))
+        return err;
+    YzScratch sc = yz_scratch_layout(scratch, cap_units, cap_heavy, garena_warps, qcap, pool_limit);
+    YzTab *tab = const_cast<YzTab *>(sc.tab);
     sc.count_work = count_work;
     if ((err = cudaMemsetAsync(sc.counters, 0, 256, stream))) return err;
     yz_tab_kernel<<<1, 256, 0, stream>>>(d_plane, tab);
@@ -1838,13 +2081,34 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
     yz_plan_kernel<W><<<(unsigned)blocks_plan, W * 32, smem, stream>>>(d_plane, hv, tv, toomany, n_events, sc, errw,
                                                                        prune);
     if ((err = cudaGetLastError())) return err;
-    if (sc.pool_cap > 0) {
-        if ((err = smem_attr_once((const void *)yz_first_kernel<W>, (int)smem))) return err;
-        if ((err = smem_attr_once((const void *)yz_second_kernel<W>, (int)smem))) return err;
-        yz_first_kernel<W><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, sc);
+    if (prune.model) {
+        // score the rows on the tensor cores (the row count stays on the
+        // device), then the uncertain events
+        if ((err = launch_mlp_score(prune.model, prune.ofeat, prune.cap_orows,
+                                    reinterpret_cast<const int32_t *>(prune.orows), prune.oscore, errw, stream,
+                                    sm_count)))
+            return err;
+        yz_unc_kernel<<<(unsigned)(sm_count * 4), 128, 0, stream>>>(sc, prune);
         if ((err = cudaGetLastError())) return err;
+        yz_kill_units_kernel<<<(unsigned)(sm_count * 8), 128, 0, stream>>>(sc, prune);
+        if ((err = cudaGetLastError())) return err;
+    }
+    if (sc.pool_cap > 0) {
         const long res = (long)sm_count * (OR_YZ_SECOND_WARPS_SM / W > 0 ? OR_YZ_SECOND_WARPS_SM / W : 1);
-        yz_second_kernel<W><<<(unsigned)min(blocks, res), W * 32, smem, stream>>>(d_plane, hv, tv, sc);
+        if (prune.model) {
+            if ((err = smem_attr_once((const void *)yz_first_kernel<W, true>, (int)smem))) return err;
+            if ((err = smem_attr_once((const void *)yz_second_kernel<W, true>, (int)smem))) return err;
+            yz_first_kernel<W, true><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, sc, prune);
+            if ((err = cudaGetLastError())) return err;
+            yz_second_kernel<W, true><<<(unsigned)min(blocks, res), W * 32, smem, stream>>>(d_plane, hv, tv, sc, prune);
+        } else {
+            if ((err = smem_attr_once((const void *)yz_first_kernel<W, false>, (int)smem))) return err;
+            if ((err = smem_attr_once((const void *)yz_second_kernel<W, false>, (int)smem))) return err;
+            yz_first_kernel<W, false><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, sc, prune);
+            if ((err = cudaGetLastError())) return err;
+            yz_second_kernel<W, false><<<(unsigned)min(blocks, res), W * 32, smem, stream>>>(d_plane, hv, tv, sc,
+                                                                                          prune);
+        }
     } else {
         yz_work_kernel<W><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, sc);
     }
@@ -1899,6 +2163,37 @@ cudaError_t launch_yz_pruned(const or_plane_t *d_plane, or_hits_view_t hv, or_tr
     pr.max_rows = max_rows;
     return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
                        sm_count, pr, warps, YZ_QCAP_CTX, pool_limit, count_work);
+}
+
+// YZ with the combination scorer: rows of features for every live outer
+// iteration of each queued tracklet, scored by `prune.model` (nullptr: rows
+// only), outer iterations below t_keep skipped
+cudaError_t launch_yz_scored(const or_plane_t *d_plane, or_hits_view_t hv, or_tracks_view_t tv,
+                             const uint8_t *toomany, int n_events, uint32_t *errw, void *scratch, int cap_units,
+                             int cap_heavy, int garena_warps, cudaStream_t stream, int sm_count, const or_mlp_t *model,
+                             float t_keep, float t_unc, float *feat, int32_t *og, float *score, uint32_t *rows,
+                             uint8_t *unc, long max_rows, int warps, long long pool_limit, int count_work) {
+    YzPrune pr{};
+    pr.ofeat = feat;
+    pr.og = og;
+    pr.oscore = score;
+    pr.orows = rows;
+    pr.unc = unc;
+    pr.model = model;
+    pr.cap_orows = max_rows;
+    pr.t_keep = t_keep;
+    pr.t_unc = t_unc;
+    return launch_yz_w(d_plane, hv, tv, toomany, n_events, errw, scratch, cap_units, cap_heavy, garena_warps, stream,
+                       sm_count, pr, warps, YZ_QCAP_CTX, pool_limit, count_work);
+}
+
+// labels of the last scored YZ call's rows (see yz_outer_labels_kernel)
+cudaError_t launch_yz_outer_labels(void *scratch, int cap_units, int cap_heavy, int garena_warps, or_tracks_view_t tv,
+                                   const uint8_t *toomany, const int32_t *og, const uint32_t *rows, long max_rows,
+                                   uint8_t *labels, cudaStream_t stream, int sm_count) {
+    const YzScratch sc = yz_scratch_layout(scratch, cap_units, cap_heavy, garena_warps, YZ_QCAP_CTX, -1);
+    yz_outer_labels_kernel<<<(unsigned)(sm_count * 4), 128, 0, stream>>>(sc, tv, toomany, og, rows, max_rows, labels);
+    return cudaGetLastError();
 }
 
 }  // namespace orgpu

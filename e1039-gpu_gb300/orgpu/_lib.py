@@ -25,7 +25,8 @@ EXPORTS = ("or_version", "or_last_error", "or_status_string", "or_geometry_load"
            "or_run_physics", "or_output_rows", "or_rt_load", "or_rt_set_plane", "or_rt_table_bytes",
            "or_pack_hits_rt", "or_rt_apply", "or_set_yz_pool_limit", "or_selftest_bounded_wait",
            "or_yz_work_counts", "or_set_yz_work_counting", "or_gkernel_eR", "or_gKernel_XZ_tracking", "or_gKernel_YZ_tracking",
-           "or_gKernel_BackTrackCleaning", "or_gKernel_Global_tracking", "or_dropin_sync")
+           "or_gKernel_BackTrackCleaning", "or_gKernel_Global_tracking", "or_dropin_sync", "or_yz_scored",
+           "or_outer_labels", "or_run_batch_scored")
 
 # tunable kernels (or_kernel_id_t)
 KERNELS = {"event_reduce": 0, "xz": 1, "yz": 2, "back_clean": 3, "global": 4, "select": 5, "features": 6}
@@ -95,6 +96,11 @@ def load(path):
     lb.or_gKernel_BackTrackCleaning.argtypes = [vp, vp]
     lb.or_gKernel_Global_tracking.argtypes = [vp, vp, vp, vp]
     lb.or_dropin_sync.argtypes = []
+    lb.or_yz_scored.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, C.c_int, vp, C.c_float, C.c_float, vp, vp, vp,
+                                vp, vp, C.c_int64, vp]
+    lb.or_outer_labels.argtypes = [vp, L.OrTracksView, vp, vp, vp, C.c_int64, vp, vp]
+    lb.or_run_batch_scored.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, vp, C.c_int, vp, C.c_float, C.c_float,
+                                       vp, vp, vp, vp, vp, C.c_int64, vp]
     i64, f32, i32 = C.c_int64, C.c_float, C.c_int
     lb.or_tracklet_rows.argtypes = [vp, L.OrTracksView, vp, i32, vp, vp]
     lb.or_tracklet_features.argtypes = [vp, L.OrHitsView, L.OrTracksView, vp, i32, vp, vp, i64, vp]

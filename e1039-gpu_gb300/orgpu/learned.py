@@ -264,3 +264,110 @@ class Trainer:
     def result(self):
         return ScorerParams(self.param.cpu().numpy(), self.sp.mean, self.sp.inv_std, self.sp.t_keep, self.sp.t_unc,
                             self.sp.meta)
+
+
+# ---------------------------------------------------------------------------
+# The combination scorer: one row per live (u3, v3) outer iteration of every
+# tracklet the YZ stage queues (or_yz_scored)
+# ---------------------------------------------------------------------------
+MODEL_COMBO_E906 = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "data",
+                                "combo_scorer_e906.npz")
+
+
+class OuterRows:
+    """Device buffers of the combination scorer for one batch: features,
+    outer indices, scores, labels, the row counter and the uncertain-event
+    flags.  `max_rows` caps the rows; tracklets past it are not pruned."""
+
+    def __init__(self, n_events, max_rows=None, device=0):
+        torch = _torch()
+        dev = torch.device("cuda", device)
+        self.n = int(n_events)
+        self.max_rows = int(max_rows if max_rows is not None else max(4096, 200 * n_events))
+        self.features = torch.zeros(self.max_rows * NF, dtype=torch.float32, device=dev)
+        self.outer = torch.zeros(self.max_rows, dtype=torch.int32, device=dev)
+        self.scores = torch.zeros(self.max_rows, dtype=torch.float32, device=dev)
+        self.labels = torch.zeros(self.max_rows, dtype=torch.uint8, device=dev)
+        self.rows = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.uncertain = torch.zeros(max(1, self.n), dtype=torch.uint8, device=dev)
+
+    def n_rows(self):
+        return min(int(self.rows.item()), self.max_rows)
+
+    def args(self):
+        return (self.features.data_ptr(), self.outer.data_ptr(), self.scores.data_ptr(), self.rows.data_ptr(),
+                self.uncertain.data_ptr(), self.max_rows)
+
+
+class ComboScorer:
+    """Calls of the combination scorer on a pipeline.Reconstruction context."""
+
+    def __init__(self, rc):
+        self.rc = rc
+        self.lib = rc.lib
+
+    def yz(self, b, orows, model=None, t_keep=0.5, t_unc=0.5, stream=None):
+        """or_yz_scored: model None writes the rows and prunes nothing."""
+        f, o, s, r, u, cap = orows.args()
+        _lib.check(self.lib.or_yz_scored(self.rc.ctx, b.hits_view(), b.tracks_view(), b.toomany.data_ptr(), b.n,
+                                         None if model is None else model.ptr(), float(t_keep), float(t_unc), f, o, s,
+                                         r, u, cap, self.rc._stream(stream)), "or_yz_scored")
+
+    def labels(self, b, orows, stream=None):
+        _lib.check(self.lib.or_outer_labels(self.rc.ctx, b.tracks_view(), b.toomany.data_ptr(),
+                                            orows.outer.data_ptr(), orows.rows.data_ptr(), orows.max_rows,
+                                            orows.labels.data_ptr(), self.rc._stream(stream)), "or_outer_labels")
+
+    def run_batch(self, b, orows, model, t_keep, t_unc, stream=None):
+        """The whole path with the combination scorer (or_run_batch_scored)."""
+        f, o, s, r, u, cap = orows.args()
+        _lib.check(self.lib.or_run_batch_scored(self.rc.ctx, b.hits_view(), b.tracks_view(), b.ntracklets.data_ptr(),
+                                                b.toomany.data_ptr(), b.n, model.ptr(), float(t_keep), float(t_unc),
+                                                f, o, s, r, u, cap, self.rc._stream(stream)), "or_run_batch_scored")
+
+    def plain_with_rows(self, b, orows, stream=None):
+        """The plain chain with the rows of its queued tracklets and their
+        labels: the training data."""
+        rc = self.rc
+        b.ntracklets.zero_()
+        rc.event_reduce(b, stream)
+        rc.xz_tracking(b, stream)
+        self.yz(b, orows, None, stream=stream)
+        rc.back_track_cleaning(b, stream)
+        rc.global_tracking(b, stream)
+        self.labels(b, orows, stream)
+
+
+def dimuon_agreement(rc, b_ref, b_new, device=0):
+    """Dimuons of the plain-method run b_ref reproduced by the run b_new:
+    both batches go through the post-global selection, vertexing and dimuon
+    building (on copies of their tracks), and a plain dimuon counts as
+    reproduced when the same event of b_new holds a dimuon record equal to
+    it bit for bit (which needs both of its tracks reproduced exactly).
+    Returns (plain dimuons, reproduced, new dimuons, tracks of plain dimuons,
+    those reproduced)."""
+    from . import pipeline
+    out = []
+    for b in (b_ref, b_new):
+        d = pipeline.DeviceDimuons(b.n, device)
+        t_n, t_t = b.ntracks.clone(), b.tracks.clone()
+        rc.selection(b)
+        rc.vertexing(b)
+        rc.dimuons(b, d)
+        rc.sync()
+        b.ntracks.copy_(t_n)
+        b.tracks.copy_(t_t)
+        out.append(d.download())
+    ref, new = out
+    n_ref = n_rep = n_new = 0
+    nd_r = ref.ndimuons.astype(np.int64)
+    nd_n = new.ndimuons.astype(np.int64)
+    R = ref.dimuons.reshape(ref.n, -1, L.NDIMUONPARAM).view(np.uint32)
+    N = new.dimuons.reshape(new.n, -1, L.NDIMUONPARAM).view(np.uint32)
+    for e in np.nonzero((nd_r > 0) | (nd_n > 0))[0]:
+        a = {R[e, k].tobytes() for k in range(min(nd_r[e], R.shape[1]))}
+        c = {N[e, k].tobytes() for k in range(min(nd_n[e], N.shape[1]))}
+        n_ref += len(a)
+        n_new += len(c)
+        n_rep += len(a & c)
+    return n_ref, n_rep, n_new, 2 * n_ref, 2 * n_rep

@@ -80,10 +80,18 @@ class Slot:
         self.h_flags = torch.empty(cap, dtype=torch.uint8).pin_memory()
         self.h_out = torch.empty(self.out_cap * L.COLLECT_STRIDE, dtype=torch.float32).pin_memory()
         self.scorer = scorer
+        # a combination-scorer model (its rows are the live (u3, v3) outer
+        # iterations of queued tracklets) runs or_run_batch_scored; a
+        # tracklet-scorer model or_run_batch_learned
+        self.combo = scorer is not None and "candidates" in scorer.meta
         if scorer is not None:
-            self.lrn = learned.Learned(self.rc)
-            self.rows = learned.TrackletRows(cap, device=device)
             self.model = learned.DeviceModel(scorer, device)
+            if self.combo:
+                self.lrn = learned.ComboScorer(self.rc)
+                self.rows = learned.OuterRows(cap, device=device)
+            else:
+                self.lrn = learned.Learned(self.rc)
+                self.rows = learned.TrackletRows(cap, device=device)
         self.graphs = {}
         self.use_graphs = graphs
         self.pieces = None
@@ -99,7 +107,7 @@ class Slot:
         try:
             self.rc.pack(b, self.d_rec, self.d_off, self.d_wp)
             if self.scorer is not None:
-                self.lrn.run_batch(b, self.rows, self.model, self.scorer.t_keep, self.scorer.t_unc)
+                self.lrn.run_batch(b, self.rows, self.model, self.scorer.t_keep, self.scorer.t_unc)  # either scorer
             else:
                 self.rc.run_batch(b)
             self.rc.collect(b, self.d_out, self.d_cnt, 6.0)
@@ -232,7 +240,7 @@ class Server:
         b = _lib.lib().or_hits_view_bytes(cap) + _lib.lib().or_tracks_view_bytes(cap)
         b += cap * rec_per_event * 16 + 4 * cap * L.COLLECT_STRIDE * 4 + (400 << 20)  # records, rows, YZ queue
         if with_scorer:
-            b += 64 * cap * (L.NFEAT * 4 + 4 + 1 + 1)
+            b += 200 * cap * (L.NFEAT * 4 + 4 + 4 + 1)  # rows of either scorer
         return int(b)
 
     def submit(self, records, offsets, arrival=None):

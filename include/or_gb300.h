@@ -106,6 +106,37 @@ int or_set_geometry(or_ctx_t *ctx, const or_plane_t *plane);
  * kernels write past their arrays instead, and its host aborts on CUDA
  * errors (online_reconstruction.cu:50-64). */
 int or_stream_sync(or_ctx_t *ctx, void *stream);
+/* The combination scorer (no counterpart in the reference): or_yz() on the
+ * same buffers, where a learned model prunes the station-3 (u3, v3) outer
+ * iterations of the u3 x v3 x u2 x v2 loop (reconstruction_kernels.cuh
+ * :1320-1461) before their combinations are evaluated.  For every live outer
+ * iteration (both pairs give a hit in the acceptance) of every tracklet the
+ * stage queues (those with more than 32 live combinations), one row of
+ * OR_NFEAT features goes to `features` (16-byte aligned) and the row's
+ * outer index (u3 pair + v3 pair * u3 pairs) to `outer_index`; *rows (device
+ * uint32) gets the row count.  With `model`, the rows are scored on the
+ * tensor cores into `scores` and an outer iteration scoring below t_keep is
+ * skipped -- none of its combinations can win, and the scratch entries its
+ * load attempts would leave are still set, so every kept combination is
+ * evaluated exactly as in or_yz().  An event where some tracklet's rows all
+ * score below t_keep but the best at or above t_unc is uncertain
+ * (uncertain[e] = 1) and runs plain.  model == NULL: the rows are written
+ * and nothing is pruned (the plain result, plus training rows).  Tracklets
+ * whose rows do not fit in max_rows are not pruned. */
+int or_yz_scored(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, const uint8_t *toomany, int n_events,
+                 const or_mlp_t *model, float t_keep, float t_unc, float *features, int32_t *outer_index,
+                 float *scores, uint32_t *rows, uint8_t *uncertain, int64_t max_rows, void *stream);
+/* Labels of the rows of the last or_yz_scored() call on this context, after
+ * back-track cleaning and global tracking of the same batch: 1 for the row
+ * of the outer iteration holding its tracklet's best combination when that
+ * tracklet ended as a global track (stationID 6), else 0. */
+int or_outer_labels(or_ctx_t *ctx, or_tracks_view_t tracks, const uint8_t *toomany, const int32_t *outer_index,
+                    const uint32_t *rows, int64_t max_rows, uint8_t *labels, void *stream);
+/* or_run_batch() with or_yz_scored() as its YZ stage. */
+int or_run_batch_scored(or_ctx_t *ctx, or_hits_view_t hits, or_tracks_view_t tracks, int32_t *ntracklets,
+                        uint8_t *toomany, int n_events, const or_mlp_t *model, float t_keep, float t_unc,
+                        float *features, int32_t *outer_index, float *scores, uint32_t *rows, uint8_t *uncertain,
+                        int64_t max_rows, void *stream);
 /* Work counters of the YZ stage, for throughput accounting.  With counting
  * enabled (or_set_yz_work_counting(ctx, 1); off by default, as it costs
  * about 2 % of the stage), each or_yz() / or_yz_pruned() call on this
