@@ -57,6 +57,7 @@ constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's
 //   OR_YZ_PLAN_WARPS_SM, OR_YZ_FIRST_WARPS_SM, OR_YZ_SECOND_WARPS_SM
 //                        warps per SM (register caps) of the other kernels
 //   OR_YZ_POOL_MI        survivor-pool entries, in Mi
+//   OR_YZ_IMG_MI         window-image pool, in Mi of 16-byte words
 //   OR_YZ_LIGHT          combinations a planning warp evaluates itself
 //   OR_YZ_PLAN_CHUNK     slots per planning unit
 //   OR_YZ_UNIT           live combinations per queued unit
@@ -83,6 +84,13 @@ constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's
 // queues between 64 Mi and 128 Mi survivors; units that do not fit run on
 // the combined path
 constexpr long long YZ_POOL_CAP = (long long)OR_YZ_POOL_MI << 20;
+#ifndef OR_YZ_IMG_MI
+#define OR_YZ_IMG_MI 96
+#endif
+// window images (16-byte words): the 100,000-event uneven batch's queued
+// tracklets take about 1 Gi bytes; tracklets whose image does not fit are
+// windowed again by each of their units
+constexpr long long YZ_IMG_WORDS = (long long)OR_YZ_IMG_MI << 20;
 constexpr int YZ_ARENA_HITS = OR_YZ_ARENA;      // windowed hits kept in shared memory per warp
 #ifndef OR_YZ_LIGHT
 #define OR_YZ_LIGHT 32
@@ -141,6 +149,8 @@ struct YzHeavy {
     // combinations per outer iteration, and the outer index of its best
     // combination (written by yz_apply_kernel; -1: none)
     int orow0, nrows, c2, best_g;
+    // its window image in the image pool (16-byte words), -1: none
+    int img;
 };
 // best combination of one unit
 struct YzBest {
@@ -187,7 +197,8 @@ struct YzScratch {
     YzHeavy *heavy;
     YzBest *best;
     unsigned int *counters;  // [0] units reserved, [1] heavy reserved, [2] queue head, [3] survivor-kernel
-                             // head, [4..5] planning units, [8..9] pool entries, [16..21] work counters
+                             // head, [4..5] planning units, [8..9] pool entries, [10..11] image words,
+                             // [16..21] work counters
     YzHit *garena;           // per-warp overflow arenas
     struct PassEntryStore *qbuf;  // per-warp survivor queues (qcap entries each)
     int cap_units, cap_heavy, garena_warps, qcap;
@@ -196,6 +207,10 @@ struct YzScratch {
     struct PassEntryStore *pool;
     int2 *useg;
     long long pool_cap;  // 0: no pool, the combined kernel runs
+    // window images of the queued tracklets (YzImgHead, arena, pairs),
+    // written by the planning pass; counter [10..11] allocates them
+    uint4 *img;
+    long long img_cap;   // 16-byte words; 0: no images, every unit windows its tracklet
     int count_work;      // nonzero: the kernels add up the work counters
 };
 
@@ -391,6 +406,103 @@ __device__ bool yz_build(YzWarp &S, const YzEvent &E, const float *T, const or_p
     }
     __syncwarp();
     return ok;
+}
+
+// A queued tracklet's windows as yz_build left them: the planning pass
+// stores this image once, and the first-cut and survivor kernels load it
+// for each of the tracklet's units instead of windowing the event's hits
+// again.  Layout in 16-byte words: the head (7 words), the arena (2 words a
+// hit), then the four pair lists back to back (4 pairs a word).
+struct __align__(16) YzImgHead {
+    int np[4];
+    int nw[8], woff[8];
+    float x0, tx, ex0, etx;
+    int total, npair, pad[2];
+};
+static_assert(sizeof(YzImgHead) == 112, "YzImgHead is seven 16-byte words");
+constexpr int YZ_IMG_HEAD_WORDS = sizeof(YzImgHead) / 16;
+
+// Store the windows just built (base: their arena); returns the image's
+// word offset, or -1 when the pool is full.
+__device__ int yz_store_image(const YzWarp &S, const YzHit *base, const YzScratch &sc) {
+    const int lane = lane_id();
+    const int total = S.woff[7] + S.nw[7];
+    const int npair = S.np[0] + S.np[1] + S.np[2] + S.np[3];
+    const long long words = YZ_IMG_HEAD_WORDS + 2LL * total + (npair + 3) / 4;
+    unsigned long long o = 0ull;
+    if (lane == 0) o = atomicAdd(reinterpret_cast<unsigned long long *>(sc.counters + 10), (unsigned long long)words);
+    o = __shfl_sync(0xffffffffu, o, 0);
+    if ((long long)o + words > sc.img_cap) return -1;
+    uint4 *dst = sc.img + o;
+    if (lane == 0) {
+        YzImgHead h;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) h.np[q] = S.np[q];
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+            h.nw[l] = S.nw[l];
+            h.woff[l] = S.woff[l];
+        }
+        h.x0 = S.x0;
+        h.tx = S.tx;
+        h.ex0 = S.ex0;
+        h.etx = S.etx;
+        h.total = total;
+        h.npair = npair;
+        h.pad[0] = h.pad[1] = 0;
+        *reinterpret_cast<YzImgHead *>(dst) = h;
+    }
+    const uint4 *src = reinterpret_cast<const uint4 *>(base);
+    uint4 *da = dst + YZ_IMG_HEAD_WORDS;
+#pragma unroll 1
+    for (int i = lane; i < 2 * total; i += 32) da[i] = src[i];
+    short2 *dp = reinterpret_cast<short2 *>(da + 2 * total);
+    int off = 0;
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll 1
+        for (int i = lane; i < S.np[q]; i += 32) dp[off + i] = S.pair[q][i];
+        off += S.np[q];
+    }
+    return (int)o;
+}
+
+// Load a tracklet's windows from its image into the warp's state; returns
+// the arena (in shared memory when it fits there, else the image itself).
+__device__ const YzHit *yz_load_image(YzWarp &S, const uint4 *__restrict__ img) {
+    const int lane = lane_id();
+    const YzImgHead &h = *reinterpret_cast<const YzImgHead *>(img);
+    const int total = h.total;
+    if (lane < 4) S.np[lane] = h.np[lane];
+    if (lane < 8) {
+        S.nw[lane] = h.nw[lane];
+        S.woff[lane] = h.woff[lane];
+    }
+    if (lane == 0) {
+        S.x0 = h.x0;
+        S.tx = h.tx;
+        S.ex0 = h.ex0;
+        S.etx = h.etx;
+    }
+    const uint4 *ia = img + YZ_IMG_HEAD_WORDS;
+    const YzHit *base = reinterpret_cast<const YzHit *>(ia);
+    if (total <= YZ_ARENA_HITS) {
+        uint4 *da = reinterpret_cast<uint4 *>(S.arena);
+#pragma unroll 1
+        for (int i = lane; i < 2 * total; i += 32) da[i] = ia[i];
+        base = S.arena;
+    }
+    const short2 *ip = reinterpret_cast<const short2 *>(ia + 2 * total);
+    int off = 0;
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        const int n = h.np[q];
+#pragma unroll 1
+        for (int i = lane; i < n; i += 32) S.pair[q][i] = ip[off + i];
+        off += n;
+    }
+    __syncwarp();
+    return base;
 }
 
 // x hits of the tracklet (K:1300-1316)
@@ -1585,8 +1697,10 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_PLAN_WARPS_SM / W > 0 ? OR_YZ_P
                                 }
                             }
                         }
+                        const int img = sc.img_cap > 0 ? yz_store_image(S, base, sc) : -1;
                         if (lane == 0) {
                             YzHeavy hv2;
+                            hv2.img = img;
                             hv2.e = (int)e;
                             hv2.slot = slot;
                             hv2.k = it;
@@ -1717,7 +1831,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_FIRST_WARPS_SM / W > 0 ? OR_YZ_
         if (lane == 0) yz_event_planes(E, hv, hv2.e, st3);
         __syncwarp();
         const YzHit *base;
-        yz_build(S, E, T, P, st3, base, garena);
+        if (hv2.img >= 0) base = yz_load_image(S, sc.img + hv2.img);
+        else yz_build(S, E, T, P, st3, base, garena);
         Stale *st = S.st;
         __syncwarp();
 #pragma unroll 1
@@ -1791,7 +1906,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_SECOND_WARPS_SM / W > 0 ? OR_YZ
         if (lane == 0) yz_event_planes(E, hv, hv2.e, st3);
         __syncwarp();
         const YzHit *base;
-        yz_build(S, E, T, P, st3, base, garena);
+        if (hv2.img >= 0) base = yz_load_image(S, sc.img + hv2.img);
+        else yz_build(S, E, T, P, st3, base, garena);
         yz_xhits(S, T, P);
         const long C2 = (long)S.np[0] * S.np[1];
         unsigned long long bk;
@@ -1973,6 +2089,7 @@ size_t yz_smem_bytes(int warps) {
 // Scratch the YZ stage needs: queue of units, per-unit best records, heavy
 // tracklets, per-warp overflow arenas.
 static long long yz_pool_cap(int qcap) { return (OR_YZ_SPLIT && qcap == YZ_QCAP_CTX) ? YZ_POOL_CAP : 0; }
+static long long yz_img_cap(int qcap) { return (OR_YZ_SPLIT && qcap == YZ_QCAP_CTX) ? YZ_IMG_WORDS : 0; }
 
 size_t yz_scratch_bytes_q(int cap_units, int cap_heavy, int garena_warps, int qcap) {
     size_t b = 256 + YZ_TAB_BYTES + (sizeof(YzUnit) + sizeof(YzBest)) * (size_t)cap_units +
@@ -1985,6 +2102,10 @@ size_t yz_scratch_bytes_q(int cap_units, int cap_heavy, int garena_warps, int qc
         b += sizeof(int2) * (size_t)cap_units;
         b = (b + 255) & ~size_t(255);
         b += sizeof(PassEntryStore) * (size_t)yz_pool_cap(qcap);
+    }
+    if (yz_img_cap(qcap) > 0) {
+        b = (b + 255) & ~size_t(255);
+        b += 16 * (size_t)yz_img_cap(qcap);
     }
     return b;
 }
@@ -2041,6 +2162,11 @@ static YzScratch yz_scratch_layout(void *scratch, int cap_units, int cap_heavy, 
         p = reinterpret_cast<char *>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
         sc.pool = reinterpret_cast<PassEntryStore *>(p);
     }
+    // the images follow the whole pool (pool_limit only narrows its use)
+    p = reinterpret_cast<char *>(scratch) + yz_scratch_bytes_q(cap_units, cap_heavy, garena_warps, qcap) -
+        16 * (size_t)yz_img_cap(qcap);
+    sc.img = yz_img_cap(qcap) > 0 ? reinterpret_cast<uint4 *>(p) : nullptr;
+    sc.img_cap = yz_img_cap(qcap);
     sc.cap_units = cap_units;
     sc.cap_heavy = cap_heavy;
     sc.garena_warps = garena_warps;
