@@ -1196,6 +1196,175 @@ __device__ __noinline__ int yz_skip_pruned(const YzWarp &S, const YzHit *base, c
     return rk;
 }
 
+// Station-3 part of the outer iteration (iu3, iv3) (K:1326-1390): the first
+// y fit's right-hand side over its accepted hits in the reference order,
+// their count and the table offset of the plane set.  False when the u3 or
+// the v3 pair gives no accepted hit (the iteration ends before station 2).
+struct Yz3 {
+    float b0, b1;
+    int n3, tab3;
+};
+
+__device__ __forceinline__ bool yz_station3(const YzWarp &S, const YzHit *base, int iu3, int iv3, Yz3 &o) {
+    const short2 pu = S.pair[2][iu3], pv = S.pair[3][iv3];
+    const unsigned long long offs = (unsigned long long)(pu.x >= 0 ? S.woff[4] + pu.x : 0xFFFF) |
+                                    ((unsigned long long)(pu.y >= 0 ? S.woff[5] + pu.y : 0xFFFF) << 16) |
+                                    ((unsigned long long)(pv.x >= 0 ? S.woff[6] + pv.x : 0xFFFF) << 32) |
+                                    ((unsigned long long)(pv.y >= 0 ? S.woff[7] + pv.y : 0xFFFF) << 48);
+    // B0 += w*y, B1 += w*y*z per accepted hit, as Fit2::add
+    float b0 = 0.f, b1 = 0.f;
+    int nu = 0, nv = 0, gu = 0, gv = 0;
+#pragma unroll 1
+    for (int a = 0; a < 4; ++a) {
+        if (a == 2 && nu == 0) break;  // no u3 hit: v3 is not loaded
+        const int off = (int)((offs >> (16 * a)) & 0xFFFFull);
+        if (off == 0xFFFF) continue;
+        const YzHit &r = base[off];
+        if (!r.acc) continue;
+        const float t = r.eY * r.Y;
+        b0 += t;
+        b1 += t * r.z;
+        if (a < 2) {
+            ++nu;
+            gu |= 1 << a;
+        } else {
+            ++nv;
+            gv |= 1 << (a - 2);
+        }
+    }
+    const bool alive3 = nu > 0 && nv > 0;
+    o.b0 = b0;
+    o.b1 = b1;
+    o.n3 = nu + nv;
+    o.tab3 = alive3 ? yz_tab_index(gu, gv, 1, 1) : 0;
+    return alive3;
+}
+
+// Station-2 load attempts of the inner pair (iu2, iv2) in the reference order
+// (K:1467-1597) after the station-3 part s3: every attempted hit writes the
+// scratch entry at the running count (4..7 at most: n3 <= 4, four attempts;
+// `own` holds those writes as arena offsets, 16 bits per entry, `wmask` which
+// entries), accepted ones enter the fit.  When the v2 group gives a hit and
+// `fit` is set, the first y fit with the plane set's tabulated inverse and
+// its 2-sigma cut (K:1602-1611).  Returns the accepted hit count.
+__device__ __forceinline__ int yz_station2_fit(const YzWarp &S, const YzHit *base, int iu2, int iv2, const Yz3 &s3,
+                                               bool fit, const YzTab *__restrict__ tab, unsigned long long &own,
+                                               unsigned &wmask, bool &pass1, float &y0, float &ty, float &ey0,
+                                               float &ety) {
+    float b0 = s3.b0, b1 = s3.b1;
+    int g2 = 0;  // plane bits u2 u2' v2 v2' of the accepted hits
+    int nuv = s3.n3;
+    const short2 pu = S.pair[0][iu2];
+    auto attempt = [&](int off, int a) {
+        const YzHit &r = base[off];
+        const int k = nuv - 4;
+        if (k >= 0) {
+            const int sh = k << 4;
+            own = (own & ~(0xFFFFull << sh)) | ((unsigned long long)off << sh);
+            wmask |= 1u << k;
+        }
+        if (r.acc) {
+            const float t = r.eY * r.Y;
+            b0 += t;
+            b1 += t * r.z;
+            g2 |= 1 << a;
+            ++nuv;
+        }
+    };
+    // the four attempts as one loop body: arena offsets (0xFFFF = no hit) of
+    // u2, u2', v2, v2' packed in 64 bits
+    const short2 pv = S.pair[1][iv2];
+    const unsigned long long offs = (unsigned long long)(pu.x >= 0 ? S.woff[0] + pu.x : 0xFFFF) |
+                                    ((unsigned long long)(pu.y >= 0 ? S.woff[1] + pu.y : 0xFFFF) << 16) |
+                                    ((unsigned long long)(pv.x >= 0 ? S.woff[2] + pv.x : 0xFFFF) << 32) |
+                                    ((unsigned long long)(pv.y >= 0 ? S.woff[3] + pv.y : 0xFFFF) << 48);
+    int nu2hits = s3.n3;
+#pragma unroll 1
+    for (int a = 0; a < 4; ++a) {
+        if (a == 2) {
+            nu2hits = nuv;
+            if (nu2hits == s3.n3) break;  // the u2 group gave no hit
+        }
+        const int off = (int)((offs >> (16 * a)) & 0xFFFFull);
+        if (off != 0xFFFF) attempt(off, a);
+    }
+    if (nu2hits > s3.n3 && nuv > nu2hits && fit) {  // the v2 group gave a hit: the fit is reached
+        // Fit2::solve with the plane set's tabulated inverse
+        const YzTab *te = tab + s3.tab3 + (g2 & 3) * 3 - 4 + (g2 >> 2);
+        const float4 ai = __ldg(reinterpret_cast<const float4 *>(te));
+        const float2 thr = __ldg(reinterpret_cast<const float2 *>(&te->thr_y0));
+        y0 = 0.0f;
+        y0 += ai.x * b0;
+        y0 += ai.y * b1;
+        ty = 0.0f;
+        ty += ai.z * b0;
+        ty += ai.w * b1;
+        pass1 = !(fabsf(y0) > thr.x || fabsf(ty) > thr.y);
+        if (pass1) {
+            const float2 er = __ldg(reinterpret_cast<const float2 *>(&te->ey0));
+            ey0 = er.x;
+            ety = er.y;
+        }
+    }
+    return nuv;
+}
+
+// One chunk's scratch entries and survivors.  Entry k+4 as the lane's
+// combination c reads it: its own write, else the last earlier lane's write
+// in this chunk, else the state st[] before the chunk; the chunk's last
+// write becomes the new state.  The survivors (pass1) go to Q[qn..] in lane
+// order with the entry past their hit count; returns the new queue length.
+__device__ __forceinline__ int yz_scan_queue(const YzHit *base, Stale st[4], unsigned long long own, unsigned wmask,
+                                             int nuv, bool pass1, int c, float y0, float ty, float ey0, float ety,
+                                             PassEntryStore *Q, int qn) {
+    Stale stj{DET_SENTINEL, 0.f, 0.f};
+    int stj_off = -1;
+    {
+        const int j = nuv;
+        const unsigned lt = lanemask_lt();
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) {
+            const bool mine = (wmask >> k) & 1u;
+            const int ok = (int)((own >> (16 * k)) & 0xFFFFull);
+            const unsigned m = __ballot_sync(0xffffffffu, mine);
+            const int src = last_lane(m & lt);
+            const int so = __shfl_sync(0xffffffffu, ok, src < 0 ? 0 : src);
+            if (j == k + 4) {
+                if (mine) stj_off = ok;
+                else if (src >= 0) stj_off = so;
+                else stj = st[k];
+            }
+            const int lw = last_lane(m);
+            if (lw >= 0) {
+                const YzHit &r = base[__shfl_sync(0xffffffffu, ok, lw)];
+                __syncwarp();  // every lane has read entry k
+                st[k] = Stale{r.det, r.pos, r.drift};
+            }
+        }
+    }
+    if (pass1 && stj_off >= 0) {
+        const YzHit &r = base[stj_off];
+        stj = Stale{r.det, r.pos, r.drift};
+    }
+    // --- queue the survivors in order ----------------------------------
+    const unsigned pm = __ballot_sync(0xffffffffu, pass1);
+    if (pass1) {
+        PassEntryStore e;
+        e.c = c;
+        e.y0 = y0;
+        e.ty = ty;
+        e.ey0 = ey0;
+        e.ety = ety;
+        e.stdet = stj.det;
+        e.stpos = stj.pos;
+        e.stdrift = stj.drift;
+        Q[qn + __popc(pm & lanemask_lt())] = e;
+    }
+    qn += __popc(pm);
+    __syncwarp();
+    return qn;
+}
+
 template <bool FIRST_ONLY, bool PRUNE = false>
 __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l, long c1l,
                                          Stale st[4], const or_plane_t &P, const YzTab *__restrict__ tab,
@@ -1305,157 +1474,23 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
             bool pass1 = false;
             if (valid) {
                 if (need3) {
-                    const short2 pu = S.pair[2][d2], pv = S.pair[3][d3];
-                    const unsigned long long offs =
-                        (unsigned long long)(pu.x >= 0 ? S.woff[4] + pu.x : 0xFFFF) |
-                        ((unsigned long long)(pu.y >= 0 ? S.woff[5] + pu.y : 0xFFFF) << 16) |
-                        ((unsigned long long)(pv.x >= 0 ? S.woff[6] + pv.x : 0xFFFF) << 32) |
-                        ((unsigned long long)(pv.y >= 0 ? S.woff[7] + pv.y : 0xFFFF) << 48);
-                    // B0 += w*y, B1 += w*y*z per accepted hit, as Fit2::add
-                    float b0 = 0.f, b1 = 0.f;
-                    int nu = 0, nv = 0, gu = 0, gv = 0;
-#pragma unroll 1
-                    for (int a = 0; a < 4; ++a) {
-                        if (a == 2 && nu == 0) break;  // no u3 hit: v3 is not loaded
-                        const int off = (int)((offs >> (16 * a)) & 0xFFFFull);
-                        if (off == 0xFFFF) continue;
-                        const YzHit &r = base[off];
-                        if (!r.acc) continue;
-                        const float t = r.eY * r.Y;
-                        b0 += t;
-                        b1 += t * r.z;
-                        if (a < 2) {
-                            ++nu;
-                            gu |= 1 << a;
-                        } else {
-                            ++nv;
-                            gv |= 1 << (a - 2);
-                        }
-                    }
-                    b0_3 = b0;
-                    b1_3 = b1;
-                    n3 = nu + nv;
-                    alive3 = nu > 0 && nv > 0;
-                    tab3 = alive3 ? yz_tab_index(gu, gv, 1, 1) : 0;
+                    Yz3 t3;
+                    alive3 = yz_station3(S, base, d2, d3, t3);
+                    b0_3 = t3.b0;
+                    b1_3 = t3.b1;
+                    n3 = t3.n3;
+                    tab3 = t3.tab3;
                     if constexpr (PRUNE) {
                         pruned3 = osc && alive3 &&
                                   osc[bits_below128(alive.v, d3) * Au + bits_below128(alive.u, d2)] < t_keep;
                     }
                     need3 = false;
                 }
-                if (alive3) {
-                    // station-2 attempts in the reference order (K:1467-1597):
-                    // every attempted hit writes the scratch entry at the
-                    // running count (4..7 at most: n3 <= 4, four attempts),
-                    // accepted ones enter the fit
-                    float b0 = b0_3, b1 = b1_3;
-                    int g2 = 0;  // plane bits u2 u2' v2 v2' of the accepted hits
-                    nuv = n3;
-                    const short2 pu = S.pair[0][d0];
-                    auto attempt = [&](int off, int a) {
-                        const YzHit &r = base[off];
-                        const int k = nuv - 4;
-                        if (k >= 0) {
-                            const int sh = k << 4;
-                            own = (own & ~(0xFFFFull << sh)) | ((unsigned long long)off << sh);
-                            wmask |= 1u << k;
-                        }
-                        if (r.acc) {
-                            const float t = r.eY * r.Y;
-                            b0 += t;
-                            b1 += t * r.z;
-                            g2 |= 1 << a;
-                            ++nuv;
-                        }
-                    };
-                    // the four attempts as one loop body: arena offsets
-                    // (0xFFFF = no hit) of u2, u2', v2, v2' packed in 64 bits
-                    const short2 pv = S.pair[1][d1];
-                    const unsigned long long offs =
-                        (unsigned long long)(pu.x >= 0 ? S.woff[0] + pu.x : 0xFFFF) |
-                        ((unsigned long long)(pu.y >= 0 ? S.woff[1] + pu.y : 0xFFFF) << 16) |
-                        ((unsigned long long)(pv.x >= 0 ? S.woff[2] + pv.x : 0xFFFF) << 32) |
-                        ((unsigned long long)(pv.y >= 0 ? S.woff[3] + pv.y : 0xFFFF) << 48);
-                    int nu2hits = n3;
-#pragma unroll 1
-                    for (int a = 0; a < 4; ++a) {
-                        if (a == 2) {
-                            nu2hits = nuv;
-                            if (nu2hits == n3) break;  // the u2 group gave no hit
-                        }
-                        const int off = (int)((offs >> (16 * a)) & 0xFFFFull);
-                        if (off != 0xFFFF) attempt(off, a);
-                    }
-                    if (nu2hits > n3 && nuv > nu2hits && !pruned3) {  // the v2 group gave a hit: the fit is reached
-                        // Fit2::solve with the plane set's tabulated inverse
-                        const YzTab *te = tab + tab3 + (g2 & 3) * 3 - 4 + (g2 >> 2);
-                        const float4 ai = __ldg(reinterpret_cast<const float4 *>(te));
-                        const float2 thr = __ldg(reinterpret_cast<const float2 *>(&te->thr_y0));
-                        y0 = 0.0f;
-                        y0 += ai.x * b0;
-                        y0 += ai.y * b1;
-                        ty = 0.0f;
-                        ty += ai.z * b0;
-                        ty += ai.w * b1;
-                        pass1 = !(fabsf(y0) > thr.x || fabsf(ty) > thr.y);
-                        if (pass1) {
-                            const float2 er = __ldg(reinterpret_cast<const float2 *>(&te->ey0));
-                            ey0 = er.x;
-                            ety = er.y;
-                        }
-                    }
-
-                }
+                if (alive3)
+                    nuv = yz_station2_fit(S, base, d0, d1, Yz3{b0_3, b1_3, n3, tab3}, !pruned3, tab, own, wmask, pass1,
+                                          y0, ty, ey0, ety);
             }
-            // --- scratch entry past the hit count ------------------------------
-            // entry k+4 as combination c reads it: its own write, else the
-            // last earlier lane's write in this chunk, else the state before
-            // the chunk; the chunk's last write becomes the new state
-            Stale stj{DET_SENTINEL, 0.f, 0.f};
-            int stj_off = -1;
-            {
-                const int j = nuv;
-                const unsigned lt = lanemask_lt();
-#pragma unroll 1
-                for (int k = 0; k < 4; ++k) {
-                    const bool mine = (wmask >> k) & 1u;
-                    const int ok = (int)((own >> (16 * k)) & 0xFFFFull);
-                    const unsigned m = __ballot_sync(0xffffffffu, mine);
-                    const int src = last_lane(m & lt);
-                    const int so = __shfl_sync(0xffffffffu, ok, src < 0 ? 0 : src);
-                    if (j == k + 4) {
-                        if (mine) stj_off = ok;
-                        else if (src >= 0) stj_off = so;
-                        else stj = st[k];
-                    }
-                    const int lw = last_lane(m);
-                    if (lw >= 0) {
-                        const YzHit &r = base[__shfl_sync(0xffffffffu, ok, lw)];
-                        __syncwarp();  // every lane has read entry k
-                        st[k] = Stale{r.det, r.pos, r.drift};
-                    }
-                }
-            }
-            if (pass1 && stj_off >= 0) {
-                const YzHit &r = base[stj_off];
-                stj = Stale{r.det, r.pos, r.drift};
-            }
-            // --- queue the survivors in order ----------------------------------
-            const unsigned pm = __ballot_sync(0xffffffffu, pass1);
-            if (pass1) {
-                PassEntry e;
-                e.c = c;
-                e.y0 = y0;
-                e.ty = ty;
-                e.ey0 = ey0;
-                e.ety = ety;
-                e.stdet = stj.det;
-                e.stpos = stj.pos;
-                e.stdrift = stj.drift;
-                Q[qn + __popc(pm & lanemask_lt())] = e;
-            }
-            qn += __popc(pm);
-            __syncwarp();
+            qn = yz_scan_queue(base, st, own, wmask, nuv, pass1, c, y0, ty, ey0, ety, Q, qn);
             // --- next chunk: digits + 32 -----------------------------------------
             basec += 32;
             d0 += s0;
@@ -1490,6 +1525,153 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
         }
     }
     return cs.best;
+}
+
+// The pruned first cut of one unit over its kept outer iterations only
+// (the combination scorer; first kernel).  The unit's live outer iterations
+// -- the scorer's rows [r0, r1) of its tracklet, in loop order -- are
+// classified 32 at a time; the kept ones go, up to YZ_KEPT_BATCH at a time,
+// into a list in the warp's shared memory, each with the scratch writes of
+// the pruned iterations right before it (its gap: for every entry 4..7 the
+// arena offset of the last pruned iteration's write there, from the load
+// pattern alone, as yz_skip_pruned finds it).  The list's combinations are
+// then walked densely, 32 a chunk, as yz_range_t walks a range; the first
+// combination of a kept iteration counts its gap's writes as its own, made
+// before its own loads, so every survivor reads the scratch entry of the
+// plain run.  Survivors go to Q in order; *nsurv = their count, or -1 when
+// the queue could overflow (the unit then runs on the combined path).
+constexpr int YZ_KEPT_BATCH = 128;
+struct YzKept {
+    unsigned short uv[YZ_KEPT_BATCH];       // iu3 | iv3 << 8
+    unsigned long long gap[YZ_KEPT_BATCH];  // 4 x 16-bit arena offsets, 0xFFFF: no write
+};
+static_assert(sizeof(YzKept) <= sizeof(((YzWarp *)nullptr)->widx), "the kept list reuses the window indices");
+static_assert(offsetof(YzWarp, widx) % 8 == 0, "the kept list's gaps are 8-byte words");
+
+__device__ void yz_first_kept(YzWarp &S, const YzHit *base, int r0, int r1, Stale st[4],
+                              const YzTab *__restrict__ tab, PassEntryStore *Q, int qcap, int *nsurv,
+                              const float *__restrict__ osc, float t_keep) {
+    const int lane = lane_id();
+    const unsigned lt = lanemask_lt();
+    const int nu2 = S.np[0], nv2 = S.np[1], nu3 = S.np[2];
+    const int C2 = nu2 * nv2;
+    const YzAlive alive = yz_alive(S, base);
+    const int Au = bits128(alive.u);
+    const unsigned long long lasto = yz_last_writes(S, base);
+    // the window indices are not read after the windows are built
+    YzKept &K = *reinterpret_cast<YzKept *>(&S.widx[0][0]);
+    const int sg = 32 / C2, sr = 32 - sg * C2;
+    const int s0 = sr % nu2, s1 = sr / nu2;  // a chunk's step in the inner digits ...
+    int qn = 0;
+    unsigned long long gapc = ~0ull;  // writes of the pruned iterations since the last kept one
+    int r = r0;
+    while (r < r1) {
+        // --- the next kept iterations and their gaps ---------------------
+        int nk = 0;
+        __syncwarp();  // every lane is done with the previous list
+        while (r < r1 && nk <= YZ_KEPT_BATCH - 32) {
+            const int j = r + lane;
+            const bool in = j < r1;
+            bool kept = false;
+            int iu = 0, iv = 0;
+            unsigned long long w = ~0ull;  // this pruned iteration's writes
+            if (in) {
+                kept = osc[j] >= t_keep;
+                iu = nth_bit128(alive.u, j % Au);
+                iv = nth_bit128(alive.v, j / Au);
+                if (!kept) {
+                    bool v;
+                    const int n3 = s3_count(S, base, iu, iv, v);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int mm = k + 4 - n3;
+                        if (mm >= 0 && mm < 4)
+                            w = (w & ~(0xFFFFull << (16 * k))) | (((lasto >> (16 * mm)) & 0xFFFFull) << (16 * k));
+                    }
+                }
+            }
+            const unsigned km = __ballot_sync(0xffffffffu, kept);
+            const int lk = last_lane(km & lt);  // the last kept lane before this one
+            const unsigned after = lk >= 0 ? ~((2u << lk) - 1u) : 0xffffffffu;
+            const int lka = last_lane(km);  // ... and of the chunk
+            const unsigned aftera = lka >= 0 ? ~((2u << lka) - 1u) : 0xffffffffu;
+            unsigned long long gap = 0ull, carry = 0ull;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const unsigned wk = (unsigned)((w >> (16 * k)) & 0xFFFFull);
+                const unsigned ck = (unsigned)((gapc >> (16 * k)) & 0xFFFFull);
+                const unsigned pm = __ballot_sync(0xffffffffu, wk != 0xFFFFu);
+                const int src = last_lane(pm & lt & after);
+                const unsigned v = __shfl_sync(0xffffffffu, wk, src < 0 ? 0 : src);
+                const unsigned g = src >= 0 ? v : (lk >= 0 ? 0xFFFFu : ck);
+                gap |= (unsigned long long)g << (16 * k);
+                const int srca = last_lane(pm & aftera);
+                const unsigned va = __shfl_sync(0xffffffffu, wk, srca < 0 ? 0 : srca);
+                const unsigned ga = srca >= 0 ? va : (lka >= 0 ? 0xFFFFu : ck);
+                carry |= (unsigned long long)ga << (16 * k);
+            }
+            gapc = carry;
+            if (kept) {
+                const int pos = nk + __popc(km & lt);
+                K.uv[pos] = (unsigned short)(iu | (iv << 8));
+                K.gap[pos] = gap;
+            }
+            nk += __popc(km);
+            r += 32;
+        }
+        __syncwarp();  // the list is written
+        // --- their combinations, 32 a chunk ------------------------------
+        const int ctot = nk * C2;
+        int k = lane / C2, d0, d1;
+        {
+            const int rr = lane - k * C2;
+            d0 = rr % nu2;
+            d1 = rr / nu2;
+        }
+        int kl = -1;  // list index whose station-3 part the lane holds
+        Yz3 t3{0.f, 0.f, 0, 0};
+        bool alive3 = false;
+#pragma unroll 1
+        for (int cb = 0; cb < ctot; cb += 32) {
+            const bool valid = cb + lane < ctot;
+            int nuv = 0, c = 0;
+            unsigned long long own = 0ull;
+            unsigned wmask = 0u;
+            float y0 = 0.f, ty = 0.f, ey0 = 0.f, ety = 0.f;
+            bool pass1 = false;
+            if (valid) {
+                const unsigned uv = K.uv[k];
+                const int iu3 = (int)(uv & 0xFFu), iv3 = (int)(uv >> 8);
+                if (k != kl) {
+                    alive3 = yz_station3(S, base, iu3, iv3, t3);
+                    kl = k;
+                }
+                c = (iu3 + iv3 * nu3) * C2 + d1 * nu2 + d0;
+                if (d0 == 0 && d1 == 0) {
+                    // the gap's writes come before the iteration's own
+                    own = K.gap[k];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        if (((own >> (16 * e)) & 0xFFFFull) != 0xFFFFull) wmask |= 1u << e;
+                }
+                if (alive3)
+                    nuv = yz_station2_fit(S, base, d0, d1, t3, true, tab, own, wmask, pass1, y0, ty, ey0, ety);
+            }
+            qn = yz_scan_queue(base, st, own, wmask, nuv, pass1, c, y0, ty, ey0, ety, Q, qn);
+            if (qn > qcap - 32) {
+                *nsurv = -1;
+                return;
+            }
+            d0 += s0;
+            int cy = d0 >= nu2;
+            d0 -= cy ? nu2 : 0;
+            d1 += s1 + cy;
+            cy = d1 >= nv2;
+            d1 -= cy ? nv2 : 0;
+            k += sg + cy;
+        }
+    }
+    *nsurv = qn;
 }
 
 __device__ __forceinline__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l,
@@ -1730,10 +1912,18 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_PLAN_WARPS_SM / W > 0 ? OR_YZ_P
     if (lane == 0 && sc.count_work) yz_flush_counts(sc, n_fitted, n_hitsum, S.nsurv);
 }
 
+// the scores of a queued tracklet's live outer iterations, when the
+// combination scorer prunes it (rows written, event not uncertain)
+__device__ __forceinline__ const float *yz_tracklet_scores(const YzPrune &prune, const YzHeavy &h) {
+    if (!prune.model || h.orow0 < 0 || (prune.unc && prune.unc[h.e])) return nullptr;
+    return prune.oscore + h.orow0;
+}
+
 // persistent warps drain the unit queue
-template <int W>
+template <int W, bool PRUNE>
 __global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_SM / W : 1))
-    yz_work_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv, YzScratch sc) {
+    yz_work_kernel(const or_plane_t *__restrict__ gplane, or_hits_view_t hv, or_tracks_view_t tv, YzScratch sc,
+                   YzPrune prune) {
     extern __shared__ __align__(16) unsigned char yz_smem[];
     or_plane_t &P = *reinterpret_cast<or_plane_t *>(yz_smem);
     YzWarp *warps = reinterpret_cast<YzWarp *>(yz_smem + ((sizeof(or_plane_t) + 15) & ~size_t(15)));
@@ -1762,7 +1952,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_
         if (lane == 0) yz_event_planes(E, hv, hv2.e, st3);
         __syncwarp();
         const YzHit *base;
-        yz_build(S, E, T, P, st3, base, garena);
+        if (hv2.img >= 0) base = yz_load_image(S, sc.img + hv2.img);
+        else yz_build(S, E, T, P, st3, base, garena);
         yz_xhits(S, T, P);
         Stale *st = S.st;
         __syncwarp();  // every lane is done with the previous unit's states
@@ -1770,8 +1961,10 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_
         for (int k = 0; k < 4; ++k) st[k] = un.entry[k];
         __syncwarp();
         const long C2 = (long)S.np[0] * S.np[1];
-        const unsigned long long bk = yz_range(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P,
-                                               sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap);
+        const float *osc = PRUNE ? yz_tracklet_scores(prune, hv2) : nullptr;
+        const unsigned long long bk =
+            yz_range_t<false, PRUNE>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P,
+                                     sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap, nullptr, osc, prune.t_keep);
         __syncwarp();
         YzBest *dst = sc.best + u;
         if (bk == ~0ull) {
@@ -1791,12 +1984,6 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_
 // Split path, first kernel: the first cut of every queued unit (no survivor
 // evaluation, so it needs far fewer registers and no per-lane hit arrays);
 // a unit's survivors go, in order, to one contiguous piece of the pool.
-// the scores of a queued tracklet's live outer iterations, when the
-// combination scorer prunes it (rows written, event not uncertain)
-__device__ __forceinline__ const float *yz_tracklet_scores(const YzPrune &prune, const YzHeavy &h) {
-    if (!prune.model || h.orow0 < 0 || (prune.unc && prune.unc[h.e])) return nullptr;
-    return prune.oscore + h.orow0;
-}
 
 template <int W, bool PRUNE>
 __global__ void __launch_bounds__(W * 32, (OR_YZ_FIRST_WARPS_SM / W > 0 ? OR_YZ_FIRST_WARPS_SM / W : 1))
@@ -1841,8 +2028,12 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_FIRST_WARPS_SM / W > 0 ? OR_YZ_
         const long C2 = (long)S.np[0] * S.np[1];
         int ns = -1;
         const float *osc = PRUNE ? yz_tracklet_scores(prune, hv2) : nullptr;
-        yz_range_t<true, PRUNE>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P, sc.tab + YZ_TAB_SETS * (st3 - 3),
-                                Q, sc.qcap, &ns, osc, prune.t_keep);
+        if (osc)
+            yz_first_kept(S, base, un.r0, un.r1, st, sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap, &ns, osc,
+                          prune.t_keep);
+        else
+            yz_range_t<true, false>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P,
+                                    sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap, &ns);
         __syncwarp();
         long long off = -1;
         if (lane == 0 && ns >= 0) {
@@ -2194,8 +2385,6 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
     }
     if ((err = smem_attr_once((const void *)yz_plan_kernel<W>, (int)smem)))
         return err;
-    if ((err = smem_attr_once((const void *)yz_work_kernel<W>, (int)smem)))
-        return err;
     YzScratch sc = yz_scratch_layout(scratch, cap_units, cap_heavy, garena_warps, qcap, pool_limit);
     YzTab *tab = const_cast<YzTab *>(sc.tab);
     sc.count_work = count_work;
@@ -2235,8 +2424,12 @@ static cudaError_t launch_yz_impl(const or_plane_t *d_plane, or_hits_view_t hv, 
             yz_second_kernel<W, false><<<(unsigned)min(blocks, res), W * 32, smem, stream>>>(d_plane, hv, tv, sc,
                                                                                           prune);
         }
+    } else if (prune.model) {
+        if ((err = smem_attr_once((const void *)yz_work_kernel<W, true>, (int)smem))) return err;
+        yz_work_kernel<W, true><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, sc, prune);
     } else {
-        yz_work_kernel<W><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, sc);
+        if ((err = smem_attr_once((const void *)yz_work_kernel<W, false>, (int)smem))) return err;
+        yz_work_kernel<W, false><<<(unsigned)blocks, W * 32, smem, stream>>>(d_plane, hv, tv, sc, prune);
     }
     if ((err = cudaGetLastError())) return err;
     yz_apply_kernel<<<(unsigned)(sm_count * 4), 128, 0, stream>>>(tv, sc);

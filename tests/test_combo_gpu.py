@@ -145,3 +145,26 @@ def test_everything_pruned_drops_queued_tracklets_only(runs):
     # the tracklets still extended (the ones evaluated in the planning pass)
     # carry the plain record bit for bit
     assert torch.equal(ta[ext_g].view(torch.int32), tb[ext_g].view(torch.int32))
+
+
+def test_kept_list_equals_range_walk(runs):
+    """The first-cut kernel walks the kept iterations as a list with the
+    pruned ones' scratch writes folded in; with no survivor pool every unit
+    runs on the combined kernel, and with a pool of one entry on the survivor
+    kernel's combined fallback, both of which walk the unit's whole range and
+    jump over the pruned iterations.  All give the same records bit for bit
+    at any cut."""
+    import torch
+    rc, cs, b, orows, model, plain, scored, hits = runs
+    scored(model, 0.0, 0.0)
+    nr = orows.n_rows()
+    for q in (0.3, 0.6, 0.9):
+        t = float(torch.quantile(orows.scores[:nr].float(), q).item())
+        listed = scored(model, t, t)
+        for limit in (0, 1):  # no pool: the combined kernel; one entry: the survivor kernel's fallback
+            rc.set_yz_pool_limit(limit)
+            try:
+                walked = scored(model, t, t)
+            finally:
+                rc.set_yz_pool_limit(-1)
+            assert _equal(listed, walked, hits.n, b.toomany)
