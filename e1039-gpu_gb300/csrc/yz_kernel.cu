@@ -265,23 +265,28 @@ struct YzWarp {
     YzBest b;
 };
 
+// The event's plane views for a tracklet of station half st3, one plane per
+// lane (every lane calls): u2 u2' v2 v2' u3 u3' v3 v3' (K:910-984), the
+// prop-tube y planes and the x hodoscopes of stations 2-4.
 __device__ __forceinline__ void yz_event_planes(YzEvent &E, const or_hits_view_t &hv, long e, int st3) {
-    // u2 u2' v2 v2' u3 u3' v3 v3' (K:910-984)
-    const short dl[8] = {DET_U2, DET_UP2, DET_V2, DET_VP2, (short)det_u3(st3), (short)(det_u3(st3) - 1),
-                         (short)det_v3(st3), (short)(det_v3(st3) - 1)};
-#pragma unroll 1
-    for (int k = 0; k < 8; ++k) {
-        E.dl[k] = dl[k];
-        E.hc[k] = hits_of(hv, e, dl[k]);
+    const int lane = lane_id();
+    int det = 0;
+    HitPlane *dst = nullptr;
+    if (lane < 8) {
+        const int u3 = det_u3(st3), v3 = det_v3(st3);
+        det = lane == 0 ? DET_U2 : lane == 1 ? DET_UP2 : lane == 2 ? DET_V2 : lane == 3 ? DET_VP2
+            : lane == 4 ? u3 : lane == 5 ? u3 - 1 : lane == 6 ? v3 : v3 - 1;
+        E.dl[lane] = (short)det;
+        dst = &E.hc[lane];
+    } else if (lane < 12) {
+        det = lane == 8 ? DET_P1Y1 : lane == 9 ? DET_P1Y2 : lane == 10 ? DET_P2Y1 : DET_P2Y2;
+        dst = lane == 8 ? &E.p1y1 : lane == 9 ? &E.p1y2 : lane == 10 ? &E.p2y1 : &E.p2y2;
+    } else if (lane < 18) {
+        const int q = (lane - 12) >> 1, c = (lane - 12) & 1;
+        det = c_hodoplanesx[q + 1][c];
+        dst = &E.hod[q][c];
     }
-    E.p1y1 = hits_of(hv, e, DET_P1Y1);
-    E.p1y2 = hits_of(hv, e, DET_P1Y2);
-    E.p2y1 = hits_of(hv, e, DET_P2Y1);
-    E.p2y2 = hits_of(hv, e, DET_P2Y2);
-#pragma unroll 1
-    for (int q = 0; q < 3; ++q)
-#pragma unroll 1
-        for (int c = 0; c < 2; ++c) E.hod[q][c] = hits_of(hv, e, c_hodoplanesx[q + 1][c]);
+    if (dst) *dst = hits_of(hv, e, det);
 }
 
 // Build the tracklet's windows (make_hitpairs_in_station, H:464-549) with the
@@ -1792,7 +1797,7 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_PLAN_WARPS_SM / W > 0 ? OR_YZ_P
             const int st3 = 3 + (slot & 1);  // K:884
             YzEvent &E = S.ev;
             __syncwarp();  // every lane is done with the previous slot's views
-            if (lane == 0) yz_event_planes(E, hv, e, st3);
+            yz_event_planes(E, hv, e, st3);
             __syncwarp();
             Stale *st = S.st;
             __syncwarp();  // every lane is done with the previous slot's states
@@ -1949,7 +1954,7 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_
         const int st3 = 3 + (hv2.slot & 1);
         YzEvent &E = S.ev;
         __syncwarp();  // every lane is done with the previous unit's views
-        if (lane == 0) yz_event_planes(E, hv, hv2.e, st3);
+        yz_event_planes(E, hv, hv2.e, st3);
         __syncwarp();
         const YzHit *base;
         if (hv2.img >= 0) base = yz_load_image(S, sc.img + hv2.img);
@@ -2015,7 +2020,7 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_FIRST_WARPS_SM / W > 0 ? OR_YZ_
         const int st3 = 3 + (hv2.slot & 1);
         YzEvent &E = S.ev;
         __syncwarp();
-        if (lane == 0) yz_event_planes(E, hv, hv2.e, st3);
+        yz_event_planes(E, hv, hv2.e, st3);
         __syncwarp();
         const YzHit *base;
         if (hv2.img >= 0) base = yz_load_image(S, sc.img + hv2.img);
@@ -2094,7 +2099,7 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_SECOND_WARPS_SM / W > 0 ? OR_YZ
         const int st3 = 3 + (hv2.slot & 1);
         YzEvent &E = S.ev;
         __syncwarp();
-        if (lane == 0) yz_event_planes(E, hv, hv2.e, st3);
+        yz_event_planes(E, hv, hv2.e, st3);
         __syncwarp();
         const YzHit *base;
         if (hv2.img >= 0) base = yz_load_image(S, sc.img + hv2.img);
