@@ -531,58 +531,84 @@ __device__ __forceinline__ void yz_xhits(YzWarp &S, const float *T, const or_pla
     __syncwarp();
 }
 
-struct UvHit {
-    short det, el, sign;
-    float pos, drift, tdc, Y, eY, Z;
+// A survivor's accepted u/v hits in the reference order (K:1326-1597), kept
+// in registers: arena offsets, 16 bits each (hits 0-3 in lo, 4-7 in hi), and
+// the left/right signs, 2 bits each in two's complement (0, 1 or -1).  The
+// hits' fields are read from the arena where they are needed.
+struct UvSet {
+    unsigned long long lo, hi;
+    unsigned sign;
 };
 
-// resolve_leftright_newhits walk over h[0..n) with the scratch entry past the
-// end given by `st` (H:714-780), then the singles (H:785-804).
-__device__ __forceinline__ void walk_newhits(int n, UvHit *h, const Stale &st, float x0, float tx, float y0, float ty,
-                                             float ex0, float etx, float ey0, float ety, const or_plane_t &P) {
+__device__ __forceinline__ int uv_off(const UvSet &U, int k) {
+    return (int)(((k < 4 ? U.lo : U.hi) >> (16 * (k & 3))) & 0xFFFFull);
+}
+__device__ __forceinline__ short uv_sign(const UvSet &U, int k) {
+    return (short)((int)(U.sign << (30 - 2 * k)) >> 30);
+}
+__device__ __forceinline__ void uv_set_sign(UvSet &U, int k, int s) {
+    U.sign = (U.sign & ~(3u << (2 * k))) | (((unsigned)s & 3u) << (2 * k));
+}
+
+// resolve_leftright_newhits walk over the n hits of U with the scratch entry
+// past the end given by `st` (H:714-780), then the singles (H:785-804).
+__device__ __forceinline__ void walk_newhits(int n, UvSet &U, const YzHit *base, const Stale &st, float x0, float tx,
+                                             float y0, float ty, float ex0, float etx, float ey0, float ety,
+                                             const or_plane_t &P) {
 #pragma unroll 1
     for (int i = 0; i < n;) {
         const int j = i + 1;
-        const short di = h[i].det;
-        const short dj = j < n ? h[j].det : st.det;
+        const YzHit &hi = base[uv_off(U, i)];
+        const short di = hi.det;
+        short dj = st.det, sj = 0;
+        float pj = st.pos, drj = st.drift;
+        if (j < n) {
+            const YzHit &hj = base[uv_off(U, j)];
+            dj = hj.det;
+            sj = uv_sign(U, j);
+            pj = hj.pos;
+            drj = hj.drift;
+        }
         if (abs(di - dj) != 1) {
             i += 1;
             continue;
         }
-        const short sj = j < n ? h[j].sign : (short)0;
-        if (h[i].sign * sj == 0) {
-            const float pj = j < n ? h[j].pos : st.pos;
-            const float drj = j < n ? h[j].drift : st.drift;
-            const int k = lr_pair_newhits(x0, tx, y0, ty, ex0, etx, ey0, ety, di, dj, h[i].pos, h[i].drift, pj, drj, P,
+        if (uv_sign(U, i) * sj == 0) {
+            const int k = lr_pair_newhits(x0, tx, y0, ty, ex0, etx, ey0, ety, di, dj, hi.pos, hi.drift, pj, drj, P,
                                           150.f);
             if (k >= 0) {
-                h[i].sign = c_lrpossibility[k][0];
-                if (j < n) h[j].sign = c_lrpossibility[k][1];
+                uv_set_sign(U, i, c_lrpossibility[k][0]);
+                if (j < n) uv_set_sign(U, j, c_lrpossibility[k][1]);
             }
         }
         i += 2;
     }
 #pragma unroll 1
-    for (int k = 0; k < n; ++k)
-        if (!h[k].sign) h[k].sign = single_sign_newhits(x0, tx, y0, ty, h[k].det, h[k].pos, P);
+    for (int k = 0; k < n; ++k) {
+        if (uv_sign(U, k)) continue;
+        const YzHit &h = base[uv_off(U, k)];
+        uv_set_sign(U, k, single_sign_newhits(x0, tx, y0, ty, h.det, h.pos, P));
+    }
 }
 
 // The per-survivor work below runs once per 32 queued survivors, between long
 // stretches of the first-cut loop; it is kept out of line (one copy each) so
-// that the loop's instructions stay resident in the instruction cache.
-__device__ __noinline__ void walk_uv(int n, UvHit *h, const Stale &st, float x0, float tx, float y0, float ty,
-                                     float ex0, float etx, float ey0, float ety, const or_plane_t &P) {
-    walk_newhits(n, h, st, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
+// that the loop's instructions stay resident in the instruction cache.  The
+// walk takes and returns the hit set by value (registers, not a stack frame).
+__device__ __noinline__ unsigned walk_uv(int n, UvSet U, const YzHit *base, Stale st, float x0, float tx, float y0,
+                                         float ty, float ex0, float etx, float ey0, float ety, const or_plane_t &P) {
+    walk_newhits(n, U, base, st, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
+    return U.sign;
 }
 
 // Index of the last station-3 hit when the walk pairs it with the first
 // station-2 hit, else -1.  The walk's pairs depend only on plane ids.
-__device__ __forceinline__ int cross_pair_index(int n3, const UvHit *h, int nuv) {
+__device__ __forceinline__ int cross_pair_index(int n3, const UvSet &U, const YzHit *base, int nuv) {
 #pragma unroll 1
     for (int i = 0; i < n3;) {
         const int j = i + 1;
         if (j >= nuv) return -1;
-        if (abs(h[i].det - h[j].det) != 1) {
+        if (abs(base[uv_off(U, i)].det - base[uv_off(U, j)].det) != 1) {
             i += 1;
             continue;
         }
@@ -738,32 +764,27 @@ __device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gp
 using PassEntry = PassEntryStore;
 
 // Gather the accepted hits of combination c in the reference order
-// (K:1326-1597); returns nuv, sets n3.
-__device__ __forceinline__ int yz_gather(const YzWarp &S, const YzHit *base, int c, int C2, UvHit *h, int &n3,
-                                         const or_plane_t &P) {
+// (K:1326-1597), station 3 first; returns nuv, sets n3.
+__device__ __forceinline__ int yz_gather(const YzWarp &S, const YzHit *base, int c, int C2, UvSet &U, int &n3) {
     const int iuv3 = c / C2, iuv2 = c - iuv3 * C2;
     const int nu2 = S.np[0], nu3 = S.np[2];
-    const short2 pq[4] = {S.pair[2][iuv3 % nu3], S.pair[3][iuv3 / nu3], S.pair[0][iuv2 % nu2], S.pair[1][iuv2 / nu2]};
-    const int lists[8] = {4, 5, 6, 7, 0, 1, 2, 3};
+    const short2 p3u = S.pair[2][iuv3 % nu3], p3v = S.pair[3][iuv3 / nu3];
+    const short2 p2u = S.pair[0][iuv2 % nu2], p2v = S.pair[1][iuv2 / nu2];
+    U.lo = U.hi = 0ull;
+    U.sign = 0u;
     int nuv = 0;
-#pragma unroll 1
+#pragma unroll
     for (int a = 0; a < 8; ++a) {
-        if (a == 4) n3 = nuv;  // station-3 hits come first
-        const short2 p = pq[a >> 1];
+        if (a == 4) n3 = nuv;
+        const short2 p = a < 2 ? p3u : a < 4 ? p3v : a < 6 ? p2u : p2v;
         const int wi = (a & 1) ? p.y : p.x;
         if (wi < 0) continue;
-        const YzHit &r = yz_list(S, base, lists[a])[wi];
-        if (!r.acc) continue;
-        UvHit &u = h[nuv];
-        u.det = r.det;
-        u.el = r.el;
-        u.tdc = r.tdc;
-        u.sign = 0;
-        u.drift = r.drift;
-        u.pos = r.pos;
-        u.Z = r.z;
-        u.Y = r.Y;
-        u.eY = r.eY;
+        const int l = (a + 4) & 7;  // lists u3 u3' v3 v3' u2 u2' v2 v2'
+        const int off = S.woff[l] + wi;
+        if (!base[off].acc) continue;
+        const unsigned long long f = (unsigned long long)off << (16 * (nuv & 3));
+        if (nuv < 4) U.lo |= f;
+        else U.hi |= f;
         ++nuv;
     }
     return nuv;
@@ -789,23 +810,32 @@ __device__ __noinline__ bool yz_gates(const YzEvent &E, const or_plane_t &P, flo
     return true;
 }
 
-// chi2_track over the x hits and the uv hits (H:1182-1204), residuals into resid
-__device__ __noinline__ float yz_chi2(const YzWarp &S, const UvHit *h, int nuv, int nhx, const or_plane_t &P, float x0,
-                                      float y0, float tx, float ty, float *resid) {
+// One residual of chi2_track (H:1149-1165): x hit m < nhx, else u/v hit
+// m - nhx of U.
+__device__ __forceinline__ float yz_residual(const YzWarp &S, const UvSet &U, const YzHit *base, int m, int nhx,
+                                             const or_plane_t &P, float x0, float y0, float tx, float ty, float &res) {
+    if (m < nhx) {
+        res = S.xres[m];
+        return residual_line(S.xp1x[m], S.xp1y[m], S.xp1z[m], S.xdpx[m], S.xdpy[m], S.xdpz[m], S.xdd[m], S.xhs[m], x0,
+                             y0, tx, ty);
+    }
+    const int k = m - nhx;
+    const YzHit &h = base[uv_off(U, k)];
+    const short d = h.det;
+    res = P.resolution[d];
+    return residual_line(x_bep(d, h.el, P), y_bep(d, h.el, P), z_bep(d, h.el, P), P.deltapx[d], P.deltapy[d],
+                         P.deltapz[d], h.drift, uv_sign(U, k), x0, y0, tx, ty);
+}
+
+// chi2_track over the x hits and the uv hits (H:1182-1204)
+__device__ __noinline__ float yz_chi2(const YzWarp &S, UvSet U, const YzHit *base, int nuv, int nhx,
+                                      const or_plane_t &P, float x0, float y0, float tx, float ty) {
     float chi2 = 0.f;
 #pragma unroll 1
-    for (int m = 0; m < nhx; ++m) {
-        resid[m] = residual_line(S.xp1x[m], S.xp1y[m], S.xp1z[m], S.xdpx[m], S.xdpy[m], S.xdpz[m], S.xdd[m], S.xhs[m],
-                                 x0, y0, tx, ty);
-        chi2 += resid[m] * resid[m] / S.xres[m] / S.xres[m];
-    }
-#pragma unroll 1
-    for (int k = 0; k < nuv; ++k) {
-        const short d = h[k].det;
-        const float r = residual_line(x_bep(d, h[k].el, P), y_bep(d, h[k].el, P), z_bep(d, h[k].el, P), P.deltapx[d],
-                                      P.deltapy[d], P.deltapz[d], h[k].drift, h[k].sign, x0, y0, tx, ty);
-        resid[nhx + k] = r;
-        chi2 += r * r / P.resolution[d] / P.resolution[d];
+    for (int m = 0; m < nhx + nuv; ++m) {
+        float res;
+        const float r = yz_residual(S, U, base, m, nhx, P, x0, y0, tx, ty, res);
+        chi2 += r * r / res / res;
     }
     return chi2;
 }
@@ -837,9 +867,9 @@ __device__ __noinline__ void yz_phase2(YzWarp &S, const YzEvent &E, const YzHit 
     if (valid) q = Qc[lane];
     const int c = valid ? q.c : 0;
     const int g = valid ? c / C2 : -1 - lane;
-    UvHit h[8];
+    UvSet U{0ull, 0ull, 0u};
     int n3 = 0, nuv = 0;
-    if (valid) nuv = yz_gather(S, base, c, C2, h, n3, P);
+    if (valid) nuv = yz_gather(S, base, c, C2, U, n3);
     const Stale stj{(short)(valid ? q.stdet : DET_SENTINEL), valid ? q.stpos : 0.f, valid ? q.stdrift : 0.f};
     const float y0 = valid ? q.y0 : 0.f, ty = valid ? q.ty : 0.f;
     const float ey0 = valid ? q.ey0 : 0.f, ety = valid ? q.ety : 0.f;
@@ -848,21 +878,22 @@ __device__ __noinline__ void yz_phase2(YzWarp &S, const YzEvent &E, const YzHit 
     const bool carried_f = (g == cs.g) && cs.hasf;
     const int fl = __ffs(vm & seg) - 1;
     const bool is_first = valid && !carried_f && fl == lane;
-    if (is_first) walk_uv(nuv, h, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
+    if (is_first) U.sign = walk_uv(nuv, U, base, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
     short sig[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const short mine = (k < n3) ? h[k].sign : (short)0;
+        const short mine = (k < n3) ? uv_sign(U, k) : (short)0;
         const short v = (short)__shfl_sync(0xffffffffu, (int)mine, fl < 0 ? 0 : fl);
         sig[k] = carried_f ? cs.sig[k] : v;
     }
     bool xok = false;
     short xval = 0;
     if (valid && !is_first) {
-        const int xi = cross_pair_index(n3, h, nuv);
+        const int xi = cross_pair_index(n3, U, base, nuv);
         if (xi >= 0) {
-            const int k = lr_pair_newhits_ool(x0, tx, y0, ty, ex0, etx, ey0, ety, h[xi].det, h[xi + 1].det, h[xi].pos,
-                                          h[xi].drift, h[xi + 1].pos, h[xi + 1].drift, P, 150.f);
+            const YzHit &ha = base[uv_off(U, xi)], &hb = base[uv_off(U, xi + 1)];
+            const int k = lr_pair_newhits_ool(x0, tx, y0, ty, ex0, etx, ey0, ety, ha.det, hb.det, ha.pos, ha.drift,
+                                              hb.pos, hb.drift, P, 150.f);
             if (k >= 0) {
                 xok = true;
                 xval = c_lrpossibility[k][0];
@@ -874,19 +905,19 @@ __device__ __noinline__ void yz_phase2(YzWarp &S, const YzEvent &E, const YzHit 
     const short xprev = (short)__shfl_sync(0xffffffffu, (int)xval, xs < 0 ? 0 : xs);
     bool pass = false;
     float chi2 = 0.f;
-    float resid[12];
     if (valid && !is_first) {
-#pragma unroll 1
-        for (int k = 0; k < n3 && k < 4; ++k) h[k].sign = sig[k];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < n3) uv_set_sign(U, k, sig[k]);
         if (n3 > 0) {
-            if (xs >= 0) h[n3 - 1].sign = xprev;
-            else if (g == cs.g && cs.hascross) h[n3 - 1].sign = cs.cross;
+            if (xs >= 0) uv_set_sign(U, n3 - 1, xprev);
+            else if (g == cs.g && cs.hascross) uv_set_sign(U, n3 - 1, cs.cross);
         }
-        walk_uv(nuv, h, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
+        U.sign = walk_uv(nuv, U, base, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
     }
     if (valid) {
         pass = yz_gates(E, P, x0, y0, tx, ty, ex0, ey0, etx, ety);
-        if (pass) chi2 = yz_chi2(S, h, nuv, nhx, P, x0, y0, tx, ty, resid);
+        if (pass) chi2 = yz_chi2(S, U, base, nuv, nhx, P, x0, y0, tx, ty);
     }
     // carry of the sign state to the next survivor chunk
     {
@@ -935,15 +966,20 @@ __device__ __noinline__ void yz_phase2(YzWarp &S, const YzEvent &E, const YzHit 
                 S.b.ey0 = ey0;
 #pragma unroll 1
                 for (int n = 0; n < nuv; ++n) {
-                    S.b.det[n] = h[n].det;
-                    S.b.el[n] = h[n].el;
-                    S.b.pos[n] = h[n].pos;
-                    S.b.drift[n] = h[n].drift;
-                    S.b.sign[n] = h[n].sign;
-                    S.b.tdc[n] = h[n].tdc;
+                    const YzHit &h = base[uv_off(U, n)];
+                    S.b.det[n] = h.det;
+                    S.b.el[n] = h.el;
+                    S.b.pos[n] = h.pos;
+                    S.b.drift[n] = h.drift;
+                    S.b.sign[n] = uv_sign(U, n);
+                    S.b.tdc[n] = h.tdc;
                 }
+                // the winner's residuals, recomputed as chi2 formed them
 #pragma unroll 1
-                for (int n = 0; n < nhx + nuv; ++n) S.b.res[n] = resid[n];
+                for (int n = 0; n < nhx + nuv; ++n) {
+                    float res;
+                    S.b.res[n] = yz_residual(S, U, base, n, nhx, P, x0, y0, tx, ty, res);
+                }
             }
         }
     }
@@ -2061,7 +2097,7 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_FIRST_WARPS_SM / W > 0 ? OR_YZ_
 // survivors replayed in order with the sign carry (or the whole unit on the
 // combined path when its survivors did not fit); writes the unit's best.
 #ifndef OR_YZ_SECOND_WARPS_SM
-#define OR_YZ_SECOND_WARPS_SM 24
+#define OR_YZ_SECOND_WARPS_SM 28
 #endif
 template <int W, bool PRUNE>
 __global__ void __launch_bounds__(W * 32, (OR_YZ_SECOND_WARPS_SM / W > 0 ? OR_YZ_SECOND_WARPS_SM / W : 1))
