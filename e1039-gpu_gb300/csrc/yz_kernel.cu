@@ -1715,10 +1715,16 @@ __device__ void yz_first_kept(YzWarp &S, const YzHit *base, int r0, int r1, Stal
     *nsurv = qn;
 }
 
-__device__ __forceinline__ unsigned long long yz_range(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l,
-                                                      long c1l, Stale st[4], const or_plane_t &P,
-                                                      const YzTab *tab, PassEntryStore *Q, int qcap) {
-    return yz_range_t<false>(S, E, base, c0l, c1l, st, P, tab, Q, qcap, nullptr);
+
+// The combined evaluation of a range, out of line: the survivor kernel runs
+// it only for units whose survivors did not fit the pool, the planning
+// kernel for light tracklets, and inlined its registers would weigh on the
+// rest of those kernels.
+template <bool PRUNE>
+__device__ __noinline__ unsigned long long yz_range_ool(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l,
+                                                        long c1l, Stale *st, const or_plane_t &P, const YzTab *tab,
+                                                        PassEntryStore *Q, int qcap, const float *osc, float t_keep) {
+    return yz_range_t<false, PRUNE>(S, E, base, c0l, c1l, st, P, tab, Q, qcap, nullptr, osc, t_keep);
 }
 
 // write the best combination into the track record (K:1804-1825)
@@ -1941,7 +1947,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_PLAN_WARPS_SM / W > 0 ? OR_YZ_P
                 if (inline_it) {
                     budget -= Cl;
                     const unsigned long long bk =
-                        yz_range(S, E, base, 0, C, st, P, sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap);
+                        yz_range_ool<false>(S, E, base, 0, C, st, P, sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap,
+                                            nullptr, 0.f);
                     __syncwarp();
                     if (bk != ~0ull) yz_store(T, S.b, S.nhx);
                 }
@@ -2150,8 +2157,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_SECOND_WARPS_SM / W > 0 ? OR_YZ
             for (int k = 0; k < 4; ++k) st[k] = un.entry[k];
             __syncwarp();
             const float *osc = PRUNE ? yz_tracklet_scores(prune, hv2) : nullptr;
-            bk = yz_range_t<false, PRUNE>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P,
-                                          sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap, nullptr, osc, prune.t_keep);
+            bk = yz_range_ool<PRUNE>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P,
+                                     sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap, osc, prune.t_keep);
         } else {
             Phase2Carry cs;
 #pragma unroll 1
