@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-rt", action="store_true", help="skip the R-T calibration packer leg")
     ap.add_argument("--no-config4", action="store_true", help="skip the high-occupancy leg")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="reference arm: skip the reference's own GPU kernels")
+    ap.add_argument("--reference-gpu-sample", type=int, default=20000,
+                    help="reference arm: events given to the reference's GPU kernels")
     return ap.parse_args()
 
 
@@ -131,6 +135,74 @@ def run_cpu(plane, wp, rec, off, n, threads):
     return dt, (threads if threads > 0 else O.hardware_threads())
 
 
+def reference_gpu_leg(plane, wp, rec, off, n_sample):
+    """The reference's own GPU kernels (oracle/_ref/ref_kernels_fmad1.cubin:
+    reconstruction_kernels.cuh compiled unchanged for sm_103a with the flags
+    of its Makefile) on the first n_sample events of the workload, chained as
+    online_reconstruction.cu:776-933 launches them -- one block per event,
+    8 threads for the event reducer, 32 for the others, in chunks of its
+    EstnEvtMax = 10,000 events -- each launch timed with CUDA events.  The
+    reference XZ kernel is not run (it calls __syncthreads in thread-dependent
+    branches, K:684-807): the oracle's XZ, bit-exact with the reference's own
+    XZ helpers, fills the tracklets between the reducer and YZ.  Only events
+    inside the reference's fixed arrays are given to it (raw chamber hits per
+    plane <= 120, windowed hits and pairs <= 100, from the oracle's counted
+    run); the rest would write past them."""
+    from oracle import pyoracle as O
+    from oracle.ref import build_ref, refrun
+    from orgpu import layout as L, synth as S
+    if not os.path.exists(build_ref.image_path("fmad1")):
+        return {"unavailable": "reference images not built (oracle/ref/build_ref.py needs the reference sources)"}
+    geo = S.Geometry(plane, wp)
+    n = min(n_sample, len(off) - 1)
+    hits = S.pack(rec[:off[n]], off[:n + 1], geo.wire_pos_f32())
+    h2, t2, st2 = hits.copy(), L.HostTracks(n), O.OracleState(n)
+    O.run_all(plane, h2, t2, st2, counted=True)
+    counts = st2.counts.reshape(n, O.NCOUNTS)
+    raw = hits.nhits_cham.reshape(n, L.NCHAM).max(axis=1)
+    idx = np.nonzero((raw <= 120) & (counts[:, 6] <= 100) & (counts[:, 7] <= 100))[0]
+    per = (L.NCHAM, L.EVT_CHAM_FLOATS, L.NHODO, L.EVT_HODO_FLOATS, L.NPROP, L.EVT_PROP_FLOATS)
+    rk = refrun.RefKernels("fmad1")
+    rk.set_plane(plane)
+    rk.timing = {}
+    tracks_out = 0
+    try:
+        for a in range(0, len(idx), L.REF_EVTMAX):
+            sel = idx[a:a + L.REF_EVTMAX]
+            m = len(sel)
+            h = L.HostHits(m)
+            for dst, src, k in zip(h.arrays(), hits.arrays(), per):
+                dst[:] = src.reshape(n, k)[sel].reshape(-1)
+            rk.put_hits(h)
+            rk.put_flags(np.zeros(m, np.uint8))
+            rk.event_reduce(m)
+            h_er = rk.get_hits(m)
+            st = O.OracleState(m)
+            st.toomany[:] = rk.get_flags(m)
+            t = L.HostTracks(m)
+            O.xz(plane, h_er, t, st)
+            rk.put_tracks(t)
+            rk.put_flags(st.toomany)
+            rk.yz(m)
+            rk.back_clean(m)
+            rk.global_tracking(m)
+            rk.selection(m)
+            tracks_out += int(rk.get_tracks(m).ntracks.astype(np.int64).sum())
+    finally:
+        rk.close()
+    tm = dict(rk.timing)
+    stage = {"event_reduce": tm.get("er", 0.0), "yz": tm.get("yz", 0.0),
+             "back_clean": tm.get("clean", 0.0) + tm.get("clean_x", 0.0), "global": tm.get("global", 0.0),
+             "select": tm.get("prop", 0.0) + tm.get("gclean", 0.0) + tm.get("gclean_x", 0.0)}
+    chain = sum(stage.values())
+    return {"image": "fmad1 (the reference's Makefile flags), device code compiled here from its sources",
+            "events_sample": int(n), "events_in_reference_bounds": int(len(idx)),
+            "stage_ms": stage, "chain_ms_without_xz": chain,
+            "events_per_s_without_xz": len(idx) / (chain / 1000.0) if chain > 0 else None,
+            "xz": "oracle (the reference XZ kernel is not runnable)",
+            "timing": "CUDA events around each launch, summed over chunks of 10,000 events"}
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup(args)
@@ -174,6 +246,11 @@ def main():
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                  "sample": "first %d events of the workload per step" % ns},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        if not args.no_reference_gpu:
+            try:
+                line["reference_gpu_kernels"] = reference_gpu_leg(plane, wp, rec, off, args.reference_gpu_sample)
+            except Exception as ex:  # the CPU arm's line stands without it
+                line["reference_gpu_kernels"] = {"unavailable": "%s: %s" % (type(ex).__name__, ex)}
         print(json.dumps(line))
         return
 
@@ -329,12 +406,7 @@ def main():
         return
 
     # ---- roofline of the dominant stage (YZ) and of the event reducer --------
-    peaks = {}
-    try:
-        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except OSError:
-        pass
+    peaks = measured_peaks()
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     prof = profile_figures()
@@ -391,6 +463,15 @@ def opcounts():
     import re
     with open(os.path.join(REPO, "include", "or_opcount.h")) as f:
         return {m.group(1): int(m.group(2)) for m in re.finditer(r"#define (OR_OPS_[A-Z0-9_]+) (\d+)", f.read())}
+
+
+def measured_peaks():
+    """MEASURED_PEAKS.json (HBM copy GB/s, cuBLAS bf16 TFLOP/s), or {}."""
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 def profile_figures():
@@ -541,7 +622,8 @@ def learned_leg(args, rc, b_plain, rec, off, d_rec, d_off, d_wp, plain_value, de
         out = agreement(ms, sp, "e1039-gpu_gb300/data/combo_scorer_e906.npz")
         out.update({"scorer": "combination scorer: (u3, v3) outer iterations of queued YZ tracklets",
                     "rows": nr, "rows_kept": float((orows.scores[:nr] >= sp.t_keep).float().mean().item()) if nr
-                    else 1.0, "uncertain_events": int(orows.uncertain[:n].sum().item())})
+                    else 1.0, "uncertain_events": int(orows.uncertain[:n].sum().item()),
+                    "mlp": mlp_figures(lrn, model, orows.features, nr, orows.scores, stream)})
         del orows
     sp = learned.ScorerParams.load()
     model = learned.DeviceModel(sp, dev.index)
@@ -560,6 +642,41 @@ def learned_leg(args, rc, b_plain, rec, off, d_rec, d_off, d_wp, plain_value, de
         return tk
     out["tracklet_scorer"] = tk
     return out
+
+
+def mlp_figures(lrn, model, features, nr, scores, stream, reps=10):
+    """The scoring MLP (mlp_score_kernel, 16-64-64-1 in BF16 on the tensor
+    cores) over the step's nr combination rows, timed alone with CUDA events:
+    achieved BF16 FLOP/s against the measured cuBLAS bf16 peak, and the rows'
+    bytes (16 f32 features in, one f32 score out) against the HBM peak -- at
+    10,368 FLOP per 68 bytes the kernel is bound by memory, not by the
+    tensor pipe; the ncu tensor-pipe activity is given beside it."""
+    import torch
+    if nr <= 0:
+        return None
+    for _ in range(3):
+        lrn.score(model, features, nr, scores)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        lrn.score(model, features, nr, scores)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    flops_row = 2 * (16 * 64 + 64 * 64 + 64 * 1)
+    bytes_row = 16 * 4 + 4
+    peaks = measured_peaks()
+    bf16 = float(peaks.get("bf16_tflops", 1900.0))
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    tflops = nr * flops_row / (ms / 1000.0) / 1e12
+    gbs = nr * bytes_row / (ms / 1000.0) / 1e9
+    prof = profile_figures().get("kernels", {}).get("mlp_score_kernel", {})
+    return {"kernel": "mlp_score_kernel", "rows": nr, "ms": ms, "flops_per_row": flops_row, "bytes_per_row": bytes_row,
+            "achieved_tflops": tflops, "bf16_peak_tflops": bf16, "frac_of_bf16_peak": tflops / bf16,
+            "achieved_gbs": gbs, "hbm_peak_gbs": hbm, "frac_of_hbm_peak": gbs / hbm, "bound": "hbm",
+            "peak_source": "measured (MEASURED_PEAKS.json)" if peaks else "fallback",
+            "tensor_pipe_active_ncu": prof.get("tensor_pipe_active")}
 
 
 def config4_leg(args, rc, b, plane, wp, dev, with_learned=True, chunks=5, seed=906004):
