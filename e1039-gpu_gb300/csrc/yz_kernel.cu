@@ -23,15 +23,18 @@
 //                    order; builds each tracklet's hit windows once (y, error
 //                    and acceptance of every windowed hit for this tracklet);
 //                    evaluates light tracklets itself, and cuts heavy ones
-//                    into units of whole (u3,v3) iterations on a device queue;
-//   yz_first_kernel  persistent warps (28 per SM, 80 registers) drain the
+//                    into units of whole (u3,v3) iterations on a device queue,
+//                    storing each one's windows as an image;
+//   yz_first_kernel  persistent warps (28 per SM, 72 registers) drain the
 //                    queue with the first cut only: fit of the station-3 and
 //                    station-2 y hits, 2-sigma cut, scratch-entry scan; each
 //                    unit's survivors (about 6 %) go in order to a device pool;
+//                    with the combination scorer it walks only the listed
+//                    kept (u3,v3) iterations;
 //   yz_second_kernel per unit, the survivors replayed in order with the sign
 //                    carry: left/right walk, prop and hodoscope gates, chi2
-//                    (24 warps per SM, registers capped at 85: its spills
-//                    cost less than the extra warps gain); a unit whose survivors
+//                    (28 warps per SM, 72 registers; a survivor's hits are
+//                    register offsets into the arena); a unit whose survivors
 //                    did not fit runs whole, first cut and survivors together
 //                    (yz_work_kernel's path, which also serves contexts
 //                    without a pool, such as the no-allocation entry);
