@@ -1,5 +1,6 @@
 // capi.cu -- the C ABI of the library (include/or_gb300.h): context,
 // argument checks, stage launches, error reporting.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -137,8 +138,48 @@ const char *or_status_string(int s) {
     }
 }
 
-int or_create(int device, or_ctx_t **out) {
+#ifndef OR_YZ_WARPS_SM
+#define OR_YZ_WARPS_SM 16
+#endif
+#ifndef OR_YZ_SPLIT
+#define OR_YZ_SPLIT 1
+#endif
+#ifndef OR_YZ_FIRST_WARPS_SM
+#define OR_YZ_FIRST_WARPS_SM 28
+#endif
+
+// Room for every heavy tracklet of a 100,000-event batch of the uneven
+// workload (about 0.7 M heavy tracklets, 0.75 M units), and in proportion
+// for a context sized to a smaller largest batch (42 units and 21 heavy
+// tracklets per event, at least 64 Ki and 32 Ki); a batch beyond it
+// evaluates the excess in the planning pass, correct but without the queue's
+// balance.  The survivor pool and the window images scale with the units.
+static void yz_caps(int max_events, int &units, int &heavy) {
+    if (max_events <= 0 || max_events >= 100000) {
+        units = 1 << 22;
+        heavy = 1 << 21;
+    } else {
+        units = std::max(1 << 16, 42 * max_events);
+        heavy = std::max(1 << 15, 21 * max_events);
+    }
+}
+
+// per-warp arenas and queues for the most warps a YZ kernel launches
+static int yz_arena_warps(int sm_count) { return sm_count * (OR_YZ_SPLIT ? OR_YZ_FIRST_WARPS_SM : OR_YZ_WARPS_SM); }
+
+size_t or_context_bytes(int max_events, int sm_count) {
+    if (max_events < 0 || sm_count <= 0) return 0;
+    int units, heavy;
+    yz_caps(max_events, units, heavy);
+    return sizeof(or_plane_t) + sizeof(uint32_t) + 256 +
+           orgpu::yz_scratch_bytes_ctx(units, heavy, yz_arena_warps(sm_count));
+}
+
+int or_create(int device, or_ctx_t **out) { return or_create_sized(device, 0, out); }
+
+int or_create_sized(int device, int max_events, or_ctx_t **out) {
     if (!out) return fail(OR_ERR_ARG, "null output pointer");
+    if (max_events < 0) return fail(OR_ERR_ARG, "max_events must be >= 0 (0: the 100,000-event default)");
     *out = nullptr;
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -169,22 +210,8 @@ int or_create(int device, or_ctx_t **out) {
         delete c;
         return fail(OR_ERR_NOMEM, "cudaMalloc work counters");
     }
-    // room for every heavy tracklet of a 100,000-event batch of the uneven
-    // workload (about 1.5 M tracklets); a batch beyond it evaluates the
-    // excess in the planning pass, correct but without the queue's balance
-    c->yz_cap_units = 1 << 22;
-    c->yz_cap_heavy = 1 << 21;
-#ifndef OR_YZ_WARPS_SM
-#define OR_YZ_WARPS_SM 16
-#endif
-#ifndef OR_YZ_SPLIT
-#define OR_YZ_SPLIT 1
-#endif
-#ifndef OR_YZ_FIRST_WARPS_SM
-#define OR_YZ_FIRST_WARPS_SM 28
-#endif
-    // per-warp arenas and queues for the most warps a YZ kernel launches
-    c->yz_garena_warps = c->sm_count * (OR_YZ_SPLIT ? OR_YZ_FIRST_WARPS_SM : OR_YZ_WARPS_SM);
+    yz_caps(max_events, c->yz_cap_units, c->yz_cap_heavy);
+    c->yz_garena_warps = yz_arena_warps(c->sm_count);
     c->yz_pool_limit = -1;
     if ((e = cudaMalloc(&c->yz_scratch,
                         orgpu::yz_scratch_bytes_ctx(c->yz_cap_units, c->yz_cap_heavy, c->yz_garena_warps))) !=

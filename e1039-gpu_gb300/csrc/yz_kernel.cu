@@ -59,8 +59,8 @@ constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's
 //   OR_YZ_SPLIT          first-cut / survivor kernels (1) or the combined one (0)
 //   OR_YZ_PLAN_WARPS_SM, OR_YZ_FIRST_WARPS_SM, OR_YZ_SECOND_WARPS_SM
 //                        warps per SM (register caps) of the other kernels
-//   OR_YZ_POOL_MI        survivor-pool entries, in Mi
-//   OR_YZ_IMG_MI         window-image pool, in Mi of 16-byte words
+//   OR_YZ_POOL_PER_UNIT  survivor-pool entries per unit of queue capacity
+//   OR_YZ_IMG_PER_UNIT   window-image 16-byte words per unit of queue capacity
 //   OR_YZ_LIGHT          combinations a planning warp evaluates itself
 //   OR_YZ_PLAN_CHUNK     slots per planning unit
 //   OR_YZ_UNIT           live combinations per queued unit
@@ -80,20 +80,22 @@ constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's
 #ifndef OR_YZ_FIRST_WARPS_SM
 #define OR_YZ_FIRST_WARPS_SM 28
 #endif
-#ifndef OR_YZ_POOL_MI
-#define OR_YZ_POOL_MI 192
+#ifndef OR_YZ_POOL_PER_UNIT
+#define OR_YZ_POOL_PER_UNIT 48
 #endif
-// survivor entries in the pool (32 B each): the 100,000-event uneven batch
-// queues between 64 Mi and 128 Mi survivors; units that do not fit run on
-// the combined path
-constexpr long long YZ_POOL_CAP = (long long)OR_YZ_POOL_MI << 20;
-#ifndef OR_YZ_IMG_MI
-#define OR_YZ_IMG_MI 96
+// survivor entries in the pool (32 B each), per unit of queue capacity: a
+// context sized for the 100,000-event uneven batch (4 Mi units) holds
+// 192 Mi, and that batch queues between 64 Mi and 128 Mi survivors; units
+// that do not fit run on the combined path
+constexpr long long YZ_POOL_PER_UNIT = OR_YZ_POOL_PER_UNIT;
+#ifndef OR_YZ_IMG_PER_UNIT
+#define OR_YZ_IMG_PER_UNIT 24
 #endif
-// window images (16-byte words): the 100,000-event uneven batch's queued
-// tracklets take about 1 Gi bytes; tracklets whose image does not fit are
+// window images (16-byte words) per unit of queue capacity: 96 Mi words
+// (1.5 GiB) for 4 Mi units, and the 100,000-event uneven batch's queued
+// tracklets take about 1 GiB; tracklets whose image does not fit are
 // windowed again by each of their units
-constexpr long long YZ_IMG_WORDS = (long long)OR_YZ_IMG_MI << 20;
+constexpr long long YZ_IMG_PER_UNIT = OR_YZ_IMG_PER_UNIT;
 constexpr int YZ_ARENA_HITS = OR_YZ_ARENA;      // windowed hits kept in shared memory per warp
 #ifndef OR_YZ_LIGHT
 #define OR_YZ_LIGHT 32
@@ -2330,8 +2332,12 @@ size_t yz_smem_bytes(int warps) {
 
 // Scratch the YZ stage needs: queue of units, per-unit best records, heavy
 // tracklets, per-warp overflow arenas.
-static long long yz_pool_cap(int qcap) { return (OR_YZ_SPLIT && qcap == YZ_QCAP_CTX) ? YZ_POOL_CAP : 0; }
-static long long yz_img_cap(int qcap) { return (OR_YZ_SPLIT && qcap == YZ_QCAP_CTX) ? YZ_IMG_WORDS : 0; }
+static long long yz_pool_cap(int qcap, int cap_units) {
+    return (OR_YZ_SPLIT && qcap == YZ_QCAP_CTX) ? YZ_POOL_PER_UNIT * cap_units : 0;
+}
+static long long yz_img_cap(int qcap, int cap_units) {
+    return (OR_YZ_SPLIT && qcap == YZ_QCAP_CTX) ? YZ_IMG_PER_UNIT * cap_units : 0;
+}
 
 size_t yz_scratch_bytes_q(int cap_units, int cap_heavy, int garena_warps, int qcap) {
     size_t b = 256 + YZ_TAB_BYTES + (sizeof(YzUnit) + sizeof(YzBest)) * (size_t)cap_units +
@@ -2339,15 +2345,15 @@ size_t yz_scratch_bytes_q(int cap_units, int cap_heavy, int garena_warps, int qc
     b = (b + 255) & ~size_t(255);
     b += sizeof(YzHit) * YZ_GARENA_HITS * (size_t)garena_warps;
     b += sizeof(PassEntryStore) * (size_t)qcap * (size_t)garena_warps;
-    if (yz_pool_cap(qcap) > 0) {
+    if (yz_pool_cap(qcap, cap_units) > 0) {
         b = (b + 255) & ~size_t(255);
         b += sizeof(int2) * (size_t)cap_units;
         b = (b + 255) & ~size_t(255);
-        b += sizeof(PassEntryStore) * (size_t)yz_pool_cap(qcap);
+        b += sizeof(PassEntryStore) * (size_t)yz_pool_cap(qcap, cap_units);
     }
-    if (yz_img_cap(qcap) > 0) {
+    if (yz_img_cap(qcap, cap_units) > 0) {
         b = (b + 255) & ~size_t(255);
-        b += 16 * (size_t)yz_img_cap(qcap);
+        b += 16 * (size_t)yz_img_cap(qcap, cap_units);
     }
     return b;
 }
@@ -2393,7 +2399,7 @@ static YzScratch yz_scratch_layout(void *scratch, int cap_units, int cap_heavy, 
     p += sizeof(YzHit) * YZ_GARENA_HITS * (size_t)garena_warps;
     sc.qbuf = reinterpret_cast<PassEntryStore *>(p);
     p += sizeof(PassEntryStore) * (size_t)qcap * (size_t)garena_warps;
-    sc.pool_cap = yz_pool_cap(qcap);
+    sc.pool_cap = yz_pool_cap(qcap, cap_units);
     if (pool_limit >= 0 && pool_limit < sc.pool_cap) sc.pool_cap = pool_limit;  // the rest of the pool goes unused
     sc.useg = nullptr;
     sc.pool = nullptr;
@@ -2406,9 +2412,9 @@ static YzScratch yz_scratch_layout(void *scratch, int cap_units, int cap_heavy, 
     }
     // the images follow the whole pool (pool_limit only narrows its use)
     p = reinterpret_cast<char *>(scratch) + yz_scratch_bytes_q(cap_units, cap_heavy, garena_warps, qcap) -
-        16 * (size_t)yz_img_cap(qcap);
-    sc.img = yz_img_cap(qcap) > 0 ? reinterpret_cast<uint4 *>(p) : nullptr;
-    sc.img_cap = yz_img_cap(qcap);
+        16 * (size_t)yz_img_cap(qcap, cap_units);
+    sc.img = yz_img_cap(qcap, cap_units) > 0 ? reinterpret_cast<uint4 *>(p) : nullptr;
+    sc.img_cap = yz_img_cap(qcap, cap_units);
     sc.cap_units = cap_units;
     sc.cap_heavy = cap_heavy;
     sc.garena_warps = garena_warps;

@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(PKG, "liborgpu.so")
 OR_OK, OR_ERR_ARG, OR_ERR_CUDA, OR_ERR_IO, OR_ERR_NOMEM, OR_ERR_CAPACITY, OR_ERR_TIMEOUT, OR_ERR_NOGEOM = range(8)
 
 # every symbol include/or_gb300.h declares
-EXPORTS = ("or_version", "or_last_error", "or_status_string", "or_geometry_load", "or_create", "or_destroy",
+EXPORTS = ("or_version", "or_last_error", "or_status_string", "or_geometry_load", "or_create", "or_create_sized", "or_context_bytes", "or_destroy",
            "or_set_geometry", "or_stream_sync", "or_event_reduce", "or_xz", "or_yz", "or_back_clean", "or_global",
            "or_run_batch", "or_hits_view_from_collection", "or_tracks_view_from_collection", "or_hits_view_bytes",
            "or_tracks_view_bytes", "or_pack_hits", "or_collect_tracks", "or_yz_noalloc", "or_tracklet_rows",
@@ -66,6 +66,9 @@ def load(path):
     lb.or_status_string.argtypes = [C.c_int]
     lb.or_geometry_load.argtypes = [C.c_char_p, P(L.OrPlane), vp]
     lb.or_create.argtypes = [C.c_int, P(vp)]
+    lb.or_create_sized.argtypes = [C.c_int, C.c_int, P(vp)]
+    lb.or_context_bytes.argtypes = [C.c_int, C.c_int]
+    lb.or_context_bytes.restype = C.c_size_t
     lb.or_destroy.argtypes = [vp]
     lb.or_set_geometry.argtypes = [vp, P(L.OrPlane)]
     lb.or_stream_sync.argtypes = [vp, vp]

@@ -156,14 +156,19 @@ class DeviceHists:
 class Reconstruction:
     """One library context (one device) with its geometry."""
 
-    def __init__(self, plane, device=0, lib=None):
+    def __init__(self, plane, device=0, lib=None, max_events=None):
         """lib: a library handle from _lib.load() (default: the product
-        build, _lib.lib())."""
+        build, _lib.lib()).  max_events: size the YZ scratch for batches of at
+        most that many events (or_create_sized; larger batches stay correct,
+        only slower); None: or_create's 100,000-event sizes."""
         torch = _torch()
         self.device = device
         self.lib = lib if lib is not None else _lib.lib()
         self.ctx = C.c_void_p()
-        _lib.check(self.lib.or_create(device, C.byref(self.ctx)), "or_create")
+        if max_events is None:
+            _lib.check(self.lib.or_create(device, C.byref(self.ctx)), "or_create")
+        else:
+            _lib.check(self.lib.or_create_sized(device, int(max_events), C.byref(self.ctx)), "or_create_sized")
         self.plane = plane
         _lib.check(self.lib.or_set_geometry(self.ctx, C.byref(plane)), "or_set_geometry")
         self._torch = torch

@@ -65,7 +65,7 @@ class Slot:
         self.dev = torch.device("cuda", device)
         self.cap = cap
         self.rec_cap = rec_cap
-        self.rc = pipeline.Reconstruction(plane, device)
+        self.rc = pipeline.Reconstruction(plane, device, max_events=cap)
         self.stream = torch.cuda.Stream(device=self.dev)
         self.b = pipeline.DeviceBatch(cap, device)
         self.d_rec = torch.zeros(rec_cap * L.HIT_RECORD_DTYPE.itemsize, dtype=torch.uint8, device=self.dev)
@@ -217,7 +217,8 @@ class Server:
         self.device = device
         wp = torch.from_numpy(np.asarray(wire_pos, np.float32).reshape(-1)).cuda(device)
         self.slots = []
-        per_slot = self.slot_bytes(slot_events, rec_per_event, scorer is not None)
+        sms = torch.cuda.get_device_properties(device).multi_processor_count
+        per_slot = self.slot_bytes(slot_events, rec_per_event, scorer is not None, sms)
         for _ in range(max_slots):
             free, _total = torch.cuda.mem_get_info(device)
             if free - per_slot < reserve_bytes:
@@ -236,9 +237,11 @@ class Server:
         self._open = collections.deque()  # submitted, not finished
 
     @staticmethod
-    def slot_bytes(cap, rec_per_event, with_scorer):
-        b = _lib.lib().or_hits_view_bytes(cap) + _lib.lib().or_tracks_view_bytes(cap)
-        b += cap * rec_per_event * 16 + 4 * cap * L.COLLECT_STRIDE * 4 + (400 << 20)  # records, rows, YZ queue
+    def slot_bytes(cap, rec_per_event, with_scorer, sm_count=152):
+        lb = _lib.lib()
+        b = lb.or_hits_view_bytes(cap) + lb.or_tracks_view_bytes(cap)
+        b += cap * rec_per_event * 16 + 4 * cap * L.COLLECT_STRIDE * 4  # records, output rows
+        b += lb.or_context_bytes(cap, sm_count)  # the slot's context, sized for its batch
         if with_scorer:
             b += 200 * cap * (L.NFEAT * 4 + 4 + 4 + 1)  # rows of either scorer
         return int(b)

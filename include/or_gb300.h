@@ -79,9 +79,20 @@ int or_geometry_load(const char *path, or_plane_t *plane, double *wire_pos);
 
 /* Context: one per device.  or_create() selects `device` and allocates the
  * context's device state: the geometry, error words, and the YZ scratch
- * (work queue, per-warp arenas and survivor queues, and the 6 GB survivor
- * pool of the split YZ path: about 7.9 GB in all). */
+ * (work queue, per-warp arenas and survivor queues, the 6 GB survivor pool of
+ * the split YZ path and the 1.5 GiB of window images: about 10.0 GB in all,
+ * sized for 100,000-event batches of the uneven workload). */
 int or_create(int device, or_ctx_t **out);
+/* or_create() with the YZ queue, survivor pool and window images sized for
+ * batches of at most `max_events` events (0, or 100,000 and above: the
+ * or_create() sizes): about 1.4 GB at 10,000 events.  Larger batches stay
+ * correct -- work that does not fit the queue is evaluated in the planning
+ * pass, survivors that do not fit the pool on the combined path -- and only
+ * lose speed.  OR_ERR_ARG for max_events < 0. */
+int or_create_sized(int device, int max_events, or_ctx_t **out);
+/* Device bytes or_create_sized(max_events) allocates on a GPU with
+ * `sm_count` SMs (0 for max_events < 0 or sm_count <= 0).  Host only. */
+size_t or_context_bytes(int max_events, int sm_count);
 int or_destroy(or_ctx_t *ctx);
 /* Events per CTA of `kernel` (1, 2, 4, 8 or 16; default 4), e.g. as chosen by
  * the autotuner (orgpu/autotune.py); or_get_launch returns the current one. */
@@ -340,7 +351,7 @@ int or_mlp_adam(or_ctx_t *ctx, float *param, float *m1, float *m2, const float *
  *
  * It is for callers that cannot allocate device memory when they call: a
  * trigger or serving process that gives all free HBM to its own pool at
- * start-up (or_create() would need about 7.9 GB for its YZ scratch), or
+ * start-up (or_create() would need about 10.0 GB for its YZ scratch), or
  * a latency-critical loop that must not call cudaMalloc/cudaFree because they
  * synchronise the device.  Results are those of or_yz() on the same buffers.
  *

@@ -18,6 +18,11 @@ And through properties that do not need the oracle:
   - event independence: the batch run as four chunks gives, event by event,
     the same tracks and flags as the batch run whole (the work queue, the
     planning units and the overflow arenas differ between the two);
+  - sized contexts: 20,000 events of the batch give the same buffers on a
+    context sized for them (or_create_sized) and on one sized for 1,000
+    events, whose YZ queue, survivor pool and window images overflow (the
+    excess evaluated in the planning pass, on the combined path, or windowed
+    again), as on the default context;
   - well-formed output: every global track has 5-18 hits with detector ids
     in the chamber range, charge +-1, a finite chi2 and 1/p in the window
     the global stage enforces;
@@ -50,11 +55,11 @@ def full(geometry):
     return plane, geo, rec, off
 
 
-def _run(plane, geo, rec, off):
+def _run(plane, geo, rec, off, max_events=None):
     import torch
     from orgpu import pipeline
     n = len(off) - 1
-    rc = pipeline.Reconstruction(plane, 0)
+    rc = pipeline.Reconstruction(plane, 0, max_events=max_events)
     b = pipeline.DeviceBatch(n)
     rc.pack(b, torch.from_numpy(rec.view(np.uint8)).cuda(), torch.from_numpy(off).cuda(),
             torch.from_numpy(geo.wire_pos_f32().reshape(-1)).cuda())
@@ -226,3 +231,17 @@ def test_full_batch_rt_fused_equals_apply(full):
         assert torch.equal(flat_f[head].view(torch.int32), flat_p[head].view(torch.int32)), name
         changed = (flat_f.view(torch.int32) != flat_p.view(torch.int32)).any(dim=1)
         assert bool(changed.any()), name
+
+
+def test_sized_contexts_equal_default(full):
+    plane, geo, rec, off = full
+    n = 20000
+    r, o = rec[:off[n]], off[:n + 1]
+    nt0, tr0, f0 = _run(plane, geo, r, o)
+    T0, m0 = _valid_tracks(nt0, tr0)
+    for cap in (n, 1000):
+        nt, tr, f = _run(plane, geo, r, o, max_events=cap)
+        np.testing.assert_array_equal(nt, nt0)
+        np.testing.assert_array_equal(f, f0)
+        T, _ = _valid_tracks(nt, tr)
+        assert np.array_equal(T[m0].view(np.uint32), T0[m0].view(np.uint32))

@@ -74,9 +74,10 @@ def test_yz(setup):
 
 @pytest.mark.parametrize("limit", [0, 300, 5000])
 def test_yz_survivor_pool_fallback(setup, limit):
-    """The split YZ path with the survivor pool limited: units whose
-    survivors do not fit run whole in the second kernel (limit 0: every unit;
-    300: some), and the tracks stay bit-exact with the oracle."""
+    """The YZ path with the survivor pool limited, bit-exact with the oracle:
+    limit 0 leaves no pool (the combined kernel runs every unit); 300 and
+    5,000: units whose survivors do not fit run whole in the survivor kernel's
+    combined fallback."""
     import torch
     from orgpu import pipeline
     plane, geo, rec, off, hits0, snap, rc = setup
