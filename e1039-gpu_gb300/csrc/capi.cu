@@ -832,7 +832,8 @@ int dropin_ctx(or_ctx_t **out) {
     if (dev < 0 || dev >= DROPIN_MAX_DEVICES) return fail(OR_ERR_ARG, "device index above the drop-in table (64)");
     std::lock_guard<std::mutex> lock(g_dropin_mutex);
     if (!g_dropin[dev]) {
-        int rc = or_create(dev, &g_dropin[dev]);
+        // the reference's structs hold OR_REF_EVTMAX events: a context sized for them
+        int rc = or_create_sized(dev, OR_REF_EVTMAX, &g_dropin[dev]);
         if (rc) return rc;
     }
     *out = g_dropin[dev];

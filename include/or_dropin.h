@@ -16,7 +16,8 @@
  * ignores launch results; its error checks read cudaGetLastError()).
  *
  * The calls run on a library context per device, created at the first call
- * on that device (about 10.0 GB of scratch, or_create()) and kept until the
+ * on that device (sized for OR_REF_EVTMAX events: about 1.4 GB of scratch,
+ * or_create_sized()) and kept until the
  * process exits; make that first call outside any stream capture.  The
  * geometry is the caller's device gPlane, read in place.  Device-side
  * error words (bounded-wait timeout, window capacity) of these calls are
