@@ -89,12 +89,12 @@ constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's
 // that do not fit run on the combined path
 constexpr long long YZ_POOL_PER_UNIT = OR_YZ_POOL_PER_UNIT;
 #ifndef OR_YZ_IMG_PER_UNIT
-#define OR_YZ_IMG_PER_UNIT 24
+#define OR_YZ_IMG_PER_UNIT 36
 #endif
-// window images (16-byte words) per unit of queue capacity: 96 Mi words
-// (1.5 GiB) for 4 Mi units, and the 100,000-event uneven batch's queued
-// tracklets take about 1 GiB; tracklets whose image does not fit are
-// windowed again by each of their units
+// window images (16-byte words) per unit of queue capacity: 144 Mi words
+// (2.25 GiB) for 4 Mi units, and the 100,000-event uneven batch's queued
+// tracklets take 128 Mi words (1.9 GiB); tracklets whose image does not fit
+// are windowed again by each of their units
 constexpr long long YZ_IMG_PER_UNIT = OR_YZ_IMG_PER_UNIT;
 constexpr int YZ_ARENA_HITS = OR_YZ_ARENA;      // windowed hits kept in shared memory per warp
 #ifndef OR_YZ_LIGHT
@@ -253,13 +253,29 @@ struct YzEvent {
     short dl[8];
 };
 
+// the first cut's listed iterations at a time (yz_first_kept)
+constexpr int YZ_KEPT_BATCH = 32;
+// inner-pair records (yz_s2_record) the first cut keeps in shared memory
+constexpr int YZ_REC_SMEM = (8 * YZ_MAXWIN * 2 + 2 * YZ_MAXWIN) / 8;
+
 struct YzWarp {
-    YzEvent ev;  // the event's plane views, the same for every lane
+    union {
+        YzEvent ev;  // the event's plane views, the same for every lane
+        // first cut (the event's views are not read there): the scratch
+        // writes of the pruned iterations before each listed one
+        unsigned long long kgap[YZ_KEPT_BATCH];
+    };
     Stale st[4];  // scratch entries 4..7 as the next combination finds them, the same for every lane
     YzHit arena[YZ_ARENA_HITS];
     short2 pair[4][YZ_MAXPAIR];  // windowed indices (or -1) in sides 0, 1 of list q
-    short widx[8][YZ_MAXWIN];    // plane hit index of each windowed hit
-    uint8_t wfl[2][YZ_MAXWIN];
+    union {
+        struct {
+            short widx[8][YZ_MAXWIN];  // plane hit index of each windowed hit
+            uint8_t wfl[2][YZ_MAXWIN];
+        } w;                           // while the windows are built
+        unsigned long long rec[YZ_REC_SMEM];  // first cut: the inner pairs' records
+    };
+    unsigned short kuv[YZ_KEPT_BATCH];  // first cut: the listed iterations, iu3 | iv3 << 8
     int np[4], nw[8], woff[8];
     float x0, tx, ex0, etx;
     int nhx;
@@ -324,7 +340,7 @@ __device__ bool yz_build(YzWarp &S, const YzEvent &E, const float *T, const or_p
                 const unsigned m = __ballot_sync(0xffffffffu, in);
                 if (in) {
                     const int k = c + __popc(m & lanemask_lt());
-                    if (k < YZ_MAXWIN) S.widx[a + side][k] = (short)i;
+                    if (k < YZ_MAXWIN) S.w.widx[a + side][k] = (short)i;
                 }
                 c += __popc(m);
             }
@@ -346,7 +362,7 @@ __device__ bool yz_build(YzWarp &S, const YzEvent &E, const float *T, const or_p
         const int det = E.dl[l];
 #pragma unroll 1
         for (int i = lane; i < S.nw[l]; i += 32) {
-            const int hi = S.widx[l][i];
+            const int hi = S.w.widx[l][i];
             YzHit r;
             r.det = (short)det;
             r.el = (short)h.chan(hi);
@@ -368,9 +384,9 @@ __device__ bool yz_build(YzWarp &S, const YzEvent &E, const float *T, const or_p
         const int a = 2 * q;
         const int c1 = S.nw[a], c2 = S.nw[a + 1];
 #pragma unroll 1
-        for (int i = lane; i < c1; i += 32) S.wfl[0][i] = 0;
+        for (int i = lane; i < c1; i += 32) S.w.wfl[0][i] = 0;
 #pragma unroll 1
-        for (int i = lane; i < c2; i += 32) S.wfl[1][i] = 0;
+        for (int i = lane; i < c2; i += 32) S.w.wfl[1][i] = 0;
         __syncwarp();
         const float spacing = c_spacingplane[c_detsuperid[stid_of[q]][proj_of[q]]];
         int np = 0;
@@ -384,8 +400,8 @@ __device__ bool yz_build(YzWarp &S, const YzEvent &E, const float *T, const or_p
                 if (!(fabsf(dst[S.woff[a] + ia].pos - dst[S.woff[a + 1] + ib].pos) > spacing)) {
                     take = true;
                     v = make_short2((short)ia, (short)ib);
-                    S.wfl[0][ia] = 1;
-                    S.wfl[1][ib] = 1;
+                    S.w.wfl[0][ia] = 1;
+                    S.w.wfl[1][ib] = 1;
                 }
             }
             wp_append(take, v, S.pair[q], YZ_MAXPAIR, np);
@@ -394,13 +410,13 @@ __device__ bool yz_build(YzWarp &S, const YzEvent &E, const float *T, const or_p
 #pragma unroll 1
         for (int b0 = 0; b0 < c1; b0 += 32) {
             const int ia = b0 + lane;
-            const bool take = ia < c1 && !S.wfl[0][ia];
+            const bool take = ia < c1 && !S.w.wfl[0][ia];
             wp_append(take, make_short2((short)ia, -1), S.pair[q], YZ_MAXPAIR, np);
         }
 #pragma unroll 1
         for (int b0 = 0; b0 < c2; b0 += 32) {
             const int ib = b0 + lane;
-            const bool take = ib < c2 && !S.wfl[1][ib];
+            const bool take = ib < c2 && !S.w.wfl[1][ib];
             wp_append(take, make_short2(-1, (short)ib), S.pair[q], YZ_MAXPAIR, np);
         }
         if (np > YZ_MAXPAIR) ok = false;
@@ -1358,7 +1374,9 @@ __device__ __forceinline__ int yz_station2_fit(const YzWarp &S, const YzHit *bas
 // One chunk's scratch entries and survivors.  Entry k+4 as the lane's
 // combination c reads it: its own write, else the last earlier lane's write
 // in this chunk, else the state st[] before the chunk; the chunk's last
-// write becomes the new state.  The survivors (pass1) go to Q[qn..] in lane
+// write becomes the new state.  `own` holds the lane's writes as arena
+// offsets in the low 10 bits of 16-bit fields (entry k in field k; bits above
+// them are ignored), `wmask` which entries it writes.  The survivors (pass1) go to Q[qn..] in lane
 // order with the entry past their hit count; returns the new queue length.
 __device__ __forceinline__ int yz_scan_queue(const YzHit *base, Stale st[4], unsigned long long own, unsigned wmask,
                                              int nuv, bool pass1, int c, float y0, float ty, float ey0, float ety,
@@ -1371,7 +1389,7 @@ __device__ __forceinline__ int yz_scan_queue(const YzHit *base, Stale st[4], uns
 #pragma unroll 1
         for (int k = 0; k < 4; ++k) {
             const bool mine = (wmask >> k) & 1u;
-            const int ok = (int)((own >> (16 * k)) & 0xFFFFull);
+            const int ok = (int)((own >> (16 * k)) & 0x3FFull);  // arena offsets are below 1,024
             const unsigned m = __ballot_sync(0xffffffffu, mine);
             const int src = last_lane(m & lt);
             const int so = __shfl_sync(0xffffffffu, ok, src < 0 ? 0 : src);
@@ -1573,39 +1591,76 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
     return cs.best;
 }
 
-// The pruned first cut of one unit over its kept outer iterations only
-// (the combination scorer; first kernel).  The unit's live outer iterations
+static_assert(8 * YZ_MAXWIN <= 1024, "arena offsets fit 10 bits");
+
+// The station-2 record of the inner pair (iu2, iv2): its load attempts in
+// the reference order (K:1467-1597) reduced to what the first cut needs, the
+// same in every outer iteration.  16-bit field e (0..3) holds in bits 0-9 the
+// arena offset of the last hit attempted when e of the pair's hits had been
+// accepted -- for e below the accepted count, accepted hit e, in order -- so
+// that after n3 station-3 hits the attempts write scratch entries e + n3 - 4;
+// bits 10-13 which fields were written, bits 26-28 the accepted count, bits
+// 42-45 the planes of the accepted hits (u2 u2' v2 v2'), bit 58 whether both
+// the u2 and the v2 group gave a hit (the first fit is reached).
+__device__ __forceinline__ unsigned long long yz_s2_record(const YzWarp &S, const YzHit *base, int iu2, int iv2) {
+    const short2 pu = S.pair[0][iu2], pv = S.pair[1][iv2];
+    const int offs[4] = {pu.x >= 0 ? S.woff[0] + pu.x : -1, pu.y >= 0 ? S.woff[1] + pu.y : -1,
+                         pv.x >= 0 ? S.woff[2] + pv.x : -1, pv.y >= 0 ? S.woff[3] + pv.y : -1};
+    unsigned long long rec = 0ull;
+    unsigned pm = 0u, g2 = 0u;
+    int nacc = 0, nu = 0;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        if (a == 2) {
+            nu = nacc;
+            if (nu == 0) break;  // no u2 hit: v2 is not loaded
+        }
+        const int off = offs[a];
+        if (off < 0) continue;
+        const int sh = 16 * nacc;
+        rec = (rec & ~(0x3FFull << sh)) | ((unsigned long long)off << sh);
+        pm |= 1u << nacc;
+        if (base[off].acc) {
+            g2 |= 1u << a;
+            ++nacc;
+        }
+    }
+    const unsigned fit = (nu > 0 && nacc > nu) ? 1u : 0u;
+    return rec | ((unsigned long long)pm << 10) | ((unsigned long long)nacc << 26) | ((unsigned long long)g2 << 42) |
+           ((unsigned long long)fit << 58);
+}
+
+// The first cut of one unit over its live outer iterations, or with the
+// combination scorer (`osc`) over the kept ones only (first kernel).  The unit's live outer iterations
 // -- the scorer's rows [r0, r1) of its tracklet, in loop order -- are
-// classified 32 at a time; the kept ones go, up to YZ_KEPT_BATCH at a time,
-// into a list in the warp's shared memory, each with the scratch writes of
+// classified 32 at a time; the kept ones go, 32 at a time, into a list in
+// the warp's shared memory, each with the scratch writes of
 // the pruned iterations right before it (its gap: for every entry 4..7 the
 // arena offset of the last pruned iteration's write there, from the load
 // pattern alone, as yz_skip_pruned finds it).  The list's combinations are
 // then walked densely, 32 a chunk, as yz_range_t walks a range; the first
 // combination of a kept iteration counts its gap's writes as its own, made
 // before its own loads, so every survivor reads the scratch entry of the
-// plain run.  Survivors go to Q in order; *nsurv = their count, or -1 when
-// the queue could overflow (the unit then runs on the combined path).
-constexpr int YZ_KEPT_BATCH = 128;
-struct YzKept {
-    unsigned short uv[YZ_KEPT_BATCH];       // iu3 | iv3 << 8
-    unsigned long long gap[YZ_KEPT_BATCH];  // 4 x 16-bit arena offsets, 0xFFFF: no write
-};
-static_assert(sizeof(YzKept) <= sizeof(((YzWarp *)nullptr)->widx), "the kept list reuses the window indices");
-static_assert(offsetof(YzWarp, widx) % 8 == 0, "the kept list's gaps are 8-byte words");
+// plain run.  A combination's station-2 part comes from the record of its
+// inner pair (R, yz_s2_record); its station-3 part is computed once per
+// listed iteration.  Survivors go to Q in order; *nsurv = their count, or -1
+// when the queue could overflow (the unit then runs on the combined path).
+
+// inner-pair records (8 B) that fit the per-warp overflow arena, where the
+// first cut keeps them when the shared ones do not suffice
+constexpr int YZ_RECORDS_MAX = (int)(YZ_GARENA_HITS * sizeof(YzHit) / 8);
+static_assert(sizeof(YzEvent) >= sizeof(unsigned long long) * YZ_KEPT_BATCH, "the listed gaps fit the event's views");
 
 __device__ void yz_first_kept(YzWarp &S, const YzHit *base, int r0, int r1, Stale st[4],
                               const YzTab *__restrict__ tab, PassEntryStore *Q, int qcap, int *nsurv,
-                              const float *__restrict__ osc, float t_keep) {
+                              const float *__restrict__ osc, float t_keep, const unsigned long long *R) {
     const int lane = lane_id();
     const unsigned lt = lanemask_lt();
     const int nu2 = S.np[0], nv2 = S.np[1], nu3 = S.np[2];
     const int C2 = nu2 * nv2;
     const YzAlive alive = yz_alive(S, base);
     const int Au = bits128(alive.u);
-    const unsigned long long lasto = yz_last_writes(S, base);
-    // the window indices are not read after the windows are built
-    YzKept &K = *reinterpret_cast<YzKept *>(&S.widx[0][0]);
+    const unsigned long long lasto = osc ? yz_last_writes(S, base) : ~0ull;
     const int sg = 32 / C2, sr = 32 - sg * C2;
     const int s0 = sr % nu2, s1 = sr / nu2;  // a chunk's step in the inner digits ...
     int qn = 0;
@@ -1622,7 +1677,7 @@ __device__ void yz_first_kept(YzWarp &S, const YzHit *base, int r0, int r1, Stal
             int iu = 0, iv = 0;
             unsigned long long w = ~0ull;  // this pruned iteration's writes
             if (in) {
-                kept = osc[j] >= t_keep;
+                kept = !osc || osc[j] >= t_keep;
                 iu = nth_bit128(alive.u, j % Au);
                 iv = nth_bit128(alive.v, j / Au);
                 if (!kept) {
@@ -1659,8 +1714,8 @@ __device__ void yz_first_kept(YzWarp &S, const YzHit *base, int r0, int r1, Stal
             gapc = carry;
             if (kept) {
                 const int pos = nk + __popc(km & lt);
-                K.uv[pos] = (unsigned short)(iu | (iv << 8));
-                K.gap[pos] = gap;
+                S.kuv[pos] = (unsigned short)(iu | (iv << 8));
+                S.kgap[pos] = gap;
             }
             nk += __popc(km);
             r += 32;
@@ -1686,22 +1741,62 @@ __device__ void yz_first_kept(YzWarp &S, const YzHit *base, int r0, int r1, Stal
             float y0 = 0.f, ty = 0.f, ey0 = 0.f, ety = 0.f;
             bool pass1 = false;
             if (valid) {
-                const unsigned uv = K.uv[k];
+                const unsigned uv = S.kuv[k];
                 const int iu3 = (int)(uv & 0xFFu), iv3 = (int)(uv >> 8);
                 if (k != kl) {
                     alive3 = yz_station3(S, base, iu3, iv3, t3);
                     kl = k;
                 }
-                c = (iu3 + iv3 * nu3) * C2 + d1 * nu2 + d0;
-                if (d0 == 0 && d1 == 0) {
+                const int r2 = d1 * nu2 + d0;
+                c = (iu3 + iv3 * nu3) * C2 + r2;
+                if (r2 == 0) {
                     // the gap's writes come before the iteration's own
-                    own = K.gap[k];
+                    own = S.kgap[k];
 #pragma unroll
                     for (int e = 0; e < 4; ++e)
                         if (((own >> (16 * e)) & 0xFFFFull) != 0xFFFFull) wmask |= 1u << e;
                 }
-                if (alive3)
-                    nuv = yz_station2_fit(S, base, d0, d1, t3, true, tab, own, wmask, pass1, y0, ty, ey0, ety);
+                if (alive3) {
+                    // the inner pair's attempts: scratch writes shifted by the
+                    // station-3 count (n3 = 2..4), accepted hits in order
+                    const unsigned long long rec = R[r2];
+                    const int sh = 4 - t3.n3;
+                    const int nacc = (int)((rec >> 26) & 7u);
+                    const unsigned wr = ((unsigned)(rec >> 10) & 0xFu) >> sh;
+                    const unsigned long long mine = rec >> (16 * sh);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        if ((wr >> e) & 1u) own = (own & ~(0xFFFFull << (16 * e))) | (mine & (0xFFFFull << (16 * e)));
+                    wmask |= wr;
+                    nuv = t3.n3 + nacc;
+                    if ((rec >> 58) & 1u) {
+                        // Fit2::solve with the plane set's tabulated inverse
+                        float b0 = t3.b0, b1 = t3.b1;
+#pragma unroll 1
+                        for (int e = 0; e < nacc; ++e) {
+                            const YzHit &h = base[(int)((rec >> (16 * e)) & 0x3FFull)];
+                            const float t = h.eY * h.Y;
+                            b0 += t;
+                            b1 += t * h.z;
+                        }
+                        const unsigned g2 = (unsigned)(rec >> 42) & 0xFu;
+                        const YzTab *te = tab + t3.tab3 + (g2 & 3u) * 3 - 4 + (g2 >> 2);
+                        const float4 ai = __ldg(reinterpret_cast<const float4 *>(te));
+                        const float2 thr = __ldg(reinterpret_cast<const float2 *>(&te->thr_y0));
+                        y0 = 0.0f;
+                        y0 += ai.x * b0;
+                        y0 += ai.y * b1;
+                        ty = 0.0f;
+                        ty += ai.z * b0;
+                        ty += ai.w * b1;
+                        pass1 = !(fabsf(y0) > thr.x || fabsf(ty) > thr.y);
+                        if (pass1) {
+                            const float2 er = __ldg(reinterpret_cast<const float2 *>(&te->ey0));
+                            ey0 = er.x;
+                            ety = er.y;
+                        }
+                    }
+                }
             }
             qn = yz_scan_queue(base, st, own, wmask, nuv, pass1, c, y0, ty, ey0, ety, Q, qn);
             if (qn > qcap - 32) {
@@ -2067,26 +2162,35 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_FIRST_WARPS_SM / W > 0 ? OR_YZ_
         const float *T = trk_rec(tv, hv2.e, hv2.slot, hv2.k);
         const int st3 = 3 + (hv2.slot & 1);
         YzEvent &E = S.ev;
-        __syncwarp();
-        yz_event_planes(E, hv, hv2.e, st3);
-        __syncwarp();
         const YzHit *base;
-        if (hv2.img >= 0) base = yz_load_image(S, sc.img + hv2.img);
-        else yz_build(S, E, T, P, st3, base, garena);
+        __syncwarp();  // every lane is done with the previous unit's state
+        if (hv2.img >= 0) {
+            base = yz_load_image(S, sc.img + hv2.img);
+        } else {
+            yz_event_planes(E, hv, hv2.e, st3);
+            __syncwarp();
+            yz_build(S, E, T, P, st3, base, garena);
+        }
         Stale *st = S.st;
         __syncwarp();
 #pragma unroll 1
         for (int k = 0; k < 4; ++k) st[k] = un.entry[k];
         __syncwarp();
-        const long C2 = (long)S.np[0] * S.np[1];
-        int ns = -1;
-        const float *osc = PRUNE ? yz_tracklet_scores(prune, hv2) : nullptr;
-        if (osc)
+        const int C2 = S.np[0] * S.np[1];
+        int ns = -1;  // -1: the unit runs on the combined path (survivor kernel)
+        if (C2 <= YZ_REC_SMEM || (hv2.img >= 0 && C2 <= YZ_RECORDS_MAX)) {
+            // the inner pairs' records: in shared memory (the window indices
+            // are not needed once the windows exist), else in the per-warp
+            // overflow arena, free when the windows came from an image
+            unsigned long long *R = C2 <= YZ_REC_SMEM ? S.rec : reinterpret_cast<unsigned long long *>(garena);
+            const int nu2 = S.np[0];
+#pragma unroll 1
+            for (int r = lane; r < C2; r += 32) R[r] = yz_s2_record(S, base, r % nu2, r / nu2);
+            __syncwarp();
+            const float *osc = PRUNE ? yz_tracklet_scores(prune, hv2) : nullptr;
             yz_first_kept(S, base, un.r0, un.r1, st, sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap, &ns, osc,
-                          prune.t_keep);
-        else
-            yz_range_t<true, false>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P,
-                                    sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap, &ns);
+                          prune.t_keep, R);
+        }
         __syncwarp();
         long long off = -1;
         if (lane == 0 && ns >= 0) {

@@ -1,6 +1,6 @@
 // yz_noalloc.cu -- the YZ tracklet stage on a statically reserved scratch area.
 //
-// or_yz() runs on the scratch that or_create() allocates (about 10.0 GB: the
+// or_yz() runs on the scratch that or_create() allocates (about 10.8 GB: the
 // work queue, per-warp arenas, the survivor pool and the window images).  Some callers cannot
 // allocate device memory when they call: a trigger or serving process that
 // hands all free HBM to its own pool at start-up, or a latency-critical loop

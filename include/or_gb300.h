@@ -80,7 +80,7 @@ int or_geometry_load(const char *path, or_plane_t *plane, double *wire_pos);
 /* Context: one per device.  or_create() selects `device` and allocates the
  * context's device state: the geometry, error words, and the YZ scratch
  * (work queue, per-warp arenas and survivor queues, the 6 GB survivor pool of
- * the split YZ path and the 1.5 GiB of window images: about 10.0 GB in all,
+ * the split YZ path and the 2.25 GiB of window images: about 10.8 GB in all,
  * sized for 100,000-event batches of the uneven workload). */
 int or_create(int device, or_ctx_t **out);
 /* or_create() with the YZ queue, survivor pool and window images sized for
@@ -351,7 +351,7 @@ int or_mlp_adam(or_ctx_t *ctx, float *param, float *m1, float *m2, const float *
  *
  * It is for callers that cannot allocate device memory when they call: a
  * trigger or serving process that gives all free HBM to its own pool at
- * start-up (or_create() would need about 10.0 GB for its YZ scratch), or
+ * start-up (or_create() would need about 10.8 GB for its YZ scratch), or
  * a latency-critical loop that must not call cudaMalloc/cudaFree because they
  * synchronise the device.  Results are those of or_yz() on the same buffers.
  *
