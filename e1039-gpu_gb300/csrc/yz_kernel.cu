@@ -1429,6 +1429,72 @@ __device__ __forceinline__ int yz_scan_queue(const YzHit *base, Stale st[4], uns
     return qn;
 }
 
+// yz_scan_queue for the first-cut kernel, with the scratch state in a
+// register: field k (16 bits) of `stp` is the arena offset of the last write
+// of entry k before this chunk, 0xFFFF while entry k still holds st[k] (the
+// unit's starting state, which stays in shared memory unchanged).  Hits are
+// read only for the survivors' entries, and a chunk without survivors only
+// advances the state.
+__device__ __forceinline__ int yz_scan_queue_off(const YzHit *base, const Stale *st, unsigned long long &stp,
+                                                 unsigned long long own, unsigned wmask, int nuv, bool pass1, int c,
+                                                 float y0, float ty, float ey0, float ety, PassEntryStore *Q, int qn) {
+    const unsigned pm = __ballot_sync(0xffffffffu, pass1);
+    if (pm == 0u) {
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) {
+            const unsigned m = __ballot_sync(0xffffffffu, (wmask >> k) & 1u);
+            if (m) {
+                const int ok = (int)((own >> (16 * k)) & 0x3FFull);
+                const unsigned long long v = (unsigned)__shfl_sync(0xffffffffu, ok, last_lane(m));
+                stp = (stp & ~(0xFFFFull << (16 * k))) | (v << (16 * k));
+            }
+        }
+        return qn;
+    }
+    const unsigned lt = lanemask_lt();
+    int stj = -2;  // the entry past the hit count: -2 none, -1 st[kk], else an arena offset
+    int kk = 0;
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+        const bool mine = (wmask >> k) & 1u;
+        const int ok = (int)((own >> (16 * k)) & 0x3FFull);
+        const unsigned m = __ballot_sync(0xffffffffu, mine);
+        const int src = last_lane(m & lt);
+        const int so = __shfl_sync(0xffffffffu, ok, src < 0 ? 0 : src);
+        if (nuv == k + 4) {
+            const int cur = (int)((stp >> (16 * k)) & 0xFFFFull);
+            stj = mine ? ok : (src >= 0 ? so : (cur == 0xFFFF ? -1 : cur));
+            kk = k;
+        }
+        if (m) {
+            const unsigned long long v = (unsigned)__shfl_sync(0xffffffffu, ok, last_lane(m));
+            stp = (stp & ~(0xFFFFull << (16 * k))) | (v << (16 * k));
+        }
+    }
+    if (pass1) {
+        Stale e3{DET_SENTINEL, 0.f, 0.f};
+        if (stj >= 0) {
+            const YzHit &r = base[stj];
+            e3 = Stale{r.det, r.pos, r.drift};
+        } else if (stj == -1) {
+            e3 = st[kk];
+        }
+        PassEntryStore e;
+        e.c = c;
+        e.y0 = y0;
+        e.ty = ty;
+        e.ey0 = ey0;
+        e.ety = ety;
+        e.stdet = e3.det;
+        e.stpos = e3.pos;
+        e.stdrift = e3.drift;
+        Q[qn + __popc(pm & lt)] = e;
+    }
+    qn += __popc(pm);
+    __syncwarp();
+    return qn;
+}
+
 template <bool FIRST_ONLY, bool PRUNE = false>
 __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l, long c1l,
                                          Stale st[4], const or_plane_t &P, const YzTab *__restrict__ tab,
@@ -1664,6 +1730,7 @@ __device__ void yz_first_kept(YzWarp &S, const YzHit *base, int r0, int r1, Stal
     const int sg = 32 / C2, sr = 32 - sg * C2;
     const int s0 = sr % nu2, s1 = sr / nu2;  // a chunk's step in the inner digits ...
     int qn = 0;
+    unsigned long long stp = ~0ull;  // scratch entries' last writes (yz_scan_queue_off)
     unsigned long long gapc = ~0ull;  // writes of the pruned iterations since the last kept one
     int r = r0;
     while (r < r1) {
@@ -1798,7 +1865,7 @@ __device__ void yz_first_kept(YzWarp &S, const YzHit *base, int r0, int r1, Stal
                     }
                 }
             }
-            qn = yz_scan_queue(base, st, own, wmask, nuv, pass1, c, y0, ty, ey0, ety, Q, qn);
+            qn = yz_scan_queue_off(base, st, stp, own, wmask, nuv, pass1, c, y0, ty, ey0, ety, Q, qn);
             if (qn > qcap - 32) {
                 *nsurv = -1;
                 return;
