@@ -641,29 +641,6 @@ __device__ __forceinline__ int cross_pair_index(int n3, const UvSet &U, const Yz
 
 __device__ __forceinline__ const YzHit *yz_list(const YzWarp &S, const YzHit *base, int l) { return base + S.woff[l]; }
 
-// Station-2 load attempts of the inner combination (iu2, iv2) in the
-// reference order (K:1467-1597): the scratch offsets they write (relative to
-// the station-3 count).
-struct S2Writes {
-    int n;
-    int off[4];
-    const YzHit *hit[4];
-};
-
-__device__ __forceinline__ S2Writes s2_writes(const YzWarp &S, const YzHit *base, int iu2, int iv2) {
-    S2Writes w;
-    w.n = 0;
-    const short2 pu = S.pair[0][iu2], pv = S.pair[1][iv2];
-    int acc = 0;
-    if (pu.x >= 0) { const YzHit *r = yz_list(S, base, 0) + pu.x; w.off[w.n] = acc; w.hit[w.n++] = r; acc += r->acc; }
-    if (pu.y >= 0) { const YzHit *r = yz_list(S, base, 1) + pu.y; w.off[w.n] = acc; w.hit[w.n++] = r; acc += r->acc; }
-    if (acc > 0) {
-        if (pv.x >= 0) { const YzHit *r = yz_list(S, base, 2) + pv.x; w.off[w.n] = acc; w.hit[w.n++] = r; acc += r->acc; }
-        if (pv.y >= 0) { const YzHit *r = yz_list(S, base, 3) + pv.y; w.off[w.n] = acc; w.hit[w.n++] = r; }
-    }
-    return w;
-}
-
 // accepted station-3 hits of the outer iteration (iu3, iv3)
 __device__ __forceinline__ int s3_count(const YzWarp &S, const YzHit *base, int iu3, int iv3, bool &valid) {
     const short2 pu = S.pair[2][iu3], pv = S.pair[3][iv3];
@@ -701,68 +678,119 @@ __device__ __forceinline__ int live_before(const unsigned mu[4], const unsigned 
     return below_v * au + (v_live ? below_u : 0);
 }
 
-__device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gper, Stale st[4], YzUnit *units,
-                               int heavy, const unsigned *alive_u = nullptr, const unsigned *alive_v = nullptr) {
-    const int lane = lane_id();
-    const int nu2 = S.np[0], nu3 = S.np[2];
-    const int C2 = S.np[0] * S.np[1];
-    // last inner combination writing each offset m, and its hit
-    int lastc[4] = {-1, -1, -1, -1};
-    unsigned long long lasth[4] = {0, 0, 0, 0};
+static_assert(8 * YZ_MAXWIN <= 1024, "arena offsets fit 10 bits");
+
+// The station-2 record of the inner pair (iu2, iv2): its load attempts in
+// the reference order (K:1467-1597) reduced to what the first cut needs, the
+// same in every outer iteration.  16-bit field e (0..3) holds in bits 0-9 the
+// arena offset of the last hit attempted when e of the pair's hits had been
+// accepted -- for e below the accepted count, accepted hit e, in order -- so
+// that after n3 station-3 hits the attempts write scratch entries e + n3 - 4;
+// bits 10-13 which fields were written, bits 26-28 the accepted count, bits
+// 42-45 the planes of the accepted hits (u2 u2' v2 v2'), bit 58 whether both
+// the u2 and the v2 group gave a hit (the first fit is reached).
+__device__ __forceinline__ unsigned long long yz_s2_record(const YzWarp &S, const YzHit *base, int iu2, int iv2) {
+    const short2 pu = S.pair[0][iu2], pv = S.pair[1][iv2];
+    const int offs[4] = {pu.x >= 0 ? S.woff[0] + pu.x : -1, pu.y >= 0 ? S.woff[1] + pu.y : -1,
+                         pv.x >= 0 ? S.woff[2] + pv.x : -1, pv.y >= 0 ? S.woff[3] + pv.y : -1};
+    unsigned long long rec = 0ull;
+    unsigned pm = 0u, g2 = 0u;
+    int nacc = 0, nu = 0;
 #pragma unroll
-    for (int b0 = 0; b0 < C2; b0 += 32) {
-        const int c = b0 + lane;
-        int mine[4] = {-1, -1, -1, -1};
-        unsigned long long mh[4] = {0, 0, 0, 0};
-        if (c < C2) {
-            const S2Writes w = s2_writes(S, base, c % nu2, c / nu2);
-#pragma unroll
-            for (int k = 0; k < w.n; ++k) {
-                mine[w.off[k]] = c;
-                mh[w.off[k]] = (unsigned long long)w.hit[k];
-            }
+    for (int a = 0; a < 4; ++a) {
+        if (a == 2) {
+            nu = nacc;
+            if (nu == 0) break;  // no u2 hit: v2 is not loaded
         }
+        const int off = offs[a];
+        if (off < 0) continue;
+        const int sh = 16 * nacc;
+        rec = (rec & ~(0x3FFull << sh)) | ((unsigned long long)off << sh);
+        pm |= 1u << nacc;
+        if (base[off].acc) {
+            g2 |= 1u << a;
+            ++nacc;
+        }
+    }
+    const unsigned fit = (nu > 0 && nacc > nu) ? 1u : 0u;
+    return rec | ((unsigned long long)pm << 10) | ((unsigned long long)nacc << 26) | ((unsigned long long)g2 << 42) |
+           ((unsigned long long)fit << 58);
+}
+
+// The station-2 load attempts of an outer iteration do not depend on the
+// iteration (only on the inner pair, K:1467-1597): the last inner combination
+// writing scratch offset m (past the station-3 hit count) is the same in
+// every live outer iteration.  Returns those hits as arena offsets, 16 bits
+// per offset m = 0..3, 0xFFFF where no combination writes m.
+__device__ unsigned long long yz_last_writes(const YzWarp &S, const YzHit *base) {
+    const int nu2 = S.np[0];
+    const int C2 = S.np[0] * S.np[1];
+    unsigned long long lasto = ~0ull;
+#pragma unroll 1
+    for (int b0 = 0; b0 < C2; b0 += 32) {
+        const int c = b0 + lane_id();
+        const unsigned long long rec = c < C2 ? yz_s2_record(S, base, c % nu2, c / nu2) : 0ull;
+        const unsigned pm = (unsigned)(rec >> 10) & 0xFu;
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-            const int l = last_lane(__ballot_sync(0xffffffffu, mine[m] >= 0));
+            const int l = last_lane(__ballot_sync(0xffffffffu, (pm >> m) & 1u));
             if (l >= 0) {
-                lastc[m] = __shfl_sync(0xffffffffu, mine[m], l);
-                lasth[m] = __shfl_sync(0xffffffffu, mh[m], l);
+                const unsigned long long o =
+                    (unsigned)__shfl_sync(0xffffffffu, (unsigned)((rec >> (16 * m)) & 0x3FFull), l);
+                lasto = (lasto & ~(0xFFFFull << (16 * m))) | (o << (16 * m));
             }
         }
     }
+    return lasto;
+}
+
+__device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gper, Stale st[4], YzUnit *units,
+                               int heavy, const unsigned *alive_u = nullptr, const unsigned *alive_v = nullptr) {
+    const int lane = lane_id();
+    const unsigned lt = lanemask_lt();
+    const int nu3 = S.np[2];
+    // the last inner combination's write of each offset m, as arena offsets
+    const unsigned long long lasto = yz_last_writes(S, base);
     const Stale st_in[4] = {st[0], st[1], st[2], st[3]};
-    int carry[4] = {-1, -1, -1, -1};  // offset m last mapped onto entry k, -1 = unchanged
-    auto resolve = [&](int k, int m) -> Stale {
-        if (m < 0) return st_in[k];
-        const YzHit *r = (const YzHit *)lasth[m];
-        return Stale{r->det, r->pos, r->drift};
+    // per entry k the arena offset of its last write so far (0xFFFF: st_in[k])
+    unsigned long long carry = ~0ull;
+    auto resolve = [&](int k, unsigned o) -> Stale {
+        if (o == 0xFFFFu) return st_in[k];
+        const YzHit &r = base[o];
+        return Stale{r.det, r.pos, r.drift};
     };
-#pragma unroll
+#pragma unroll 1
     for (int b0 = 0; b0 < G; b0 += 32) {
         const int g = b0 + lane;
-        int mk[4] = {-1, -1, -1, -1};
+        unsigned long long mk = ~0ull;  // this outer iteration's writes of entries 4..7
         if (g < G) {
             bool valid;
             const int n3 = s3_count(S, base, g % nu3, g / nu3, valid);
+            if (valid) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int mm = k + 4 - n3;
-                if (valid && mm >= 0 && mm < 4 && lastc[mm] >= 0) mk[k] = mm;
+                for (int k = 0; k < 4; ++k) {
+                    const int mm = k + 4 - n3;
+                    if (mm >= 0 && mm < 4)
+                        mk = (mk & ~(0xFFFFull << (16 * k))) | (((lasto >> (16 * mm)) & 0xFFFFull) << (16 * k));
+                }
             }
         }
-        const bool ustart = units && g < G && (g % gper) == 0;
-        Stale ent[4];
+        unsigned long long ent = 0ull;  // the entries as this outer iteration finds them
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const unsigned wm = __ballot_sync(0xffffffffu, mk[k] >= 0);
-            const int src = last_lane(wm & lanemask_lt());
-            const int msrc = __shfl_sync(0xffffffffu, mk[k], src < 0 ? 0 : src);
-            ent[k] = resolve(k, src >= 0 ? msrc : carry[k]);
+            const unsigned wk = (unsigned)((mk >> (16 * k)) & 0xFFFFull);
+            const unsigned wm = __ballot_sync(0xffffffffu, wk != 0xFFFFu);
+            const int src = last_lane(wm & lt);
+            const unsigned v = __shfl_sync(0xffffffffu, wk, src < 0 ? 0 : src);
+            const unsigned e = src >= 0 ? v : (unsigned)((carry >> (16 * k)) & 0xFFFFull);
+            ent |= (unsigned long long)e << (16 * k);
             const int l = last_lane(wm);
-            if (l >= 0) carry[k] = __shfl_sync(0xffffffffu, mk[k], l);
+            if (l >= 0) {
+                const unsigned long long c = __shfl_sync(0xffffffffu, wk, l);
+                carry = (carry & ~(0xFFFFull << (16 * k))) | (c << (16 * k));
+            }
         }
-        if (ustart) {
+        if (units && g < G && (g % gper) == 0) {
             YzUnit &u = units[g / gper];
             u.heavy = heavy;
             u.g0 = g;
@@ -771,12 +799,15 @@ __device__ void yz_unit_states(const YzWarp &S, const YzHit *base, int G, int gp
             u.r0 = alive_u ? live_before(alive_u, alive_v, nu3, u.g0) : 0;
             u.r1 = alive_u ? live_before(alive_u, alive_v, nu3, u.g1) : 0;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) u.entry[k] = ent[k];
+            for (int k = 0; k < 4; ++k) u.entry[k] = resolve(k, (unsigned)((ent >> (16 * k)) & 0xFFFFull));
         }
     }
     __syncwarp();  // every lane has read the entry states
 #pragma unroll
-    for (int k = 0; k < 4; ++k) st[k] = resolve(k, carry[k]);
+    for (int k = 0; k < 4; ++k) {
+        const Stale v = resolve(k, (unsigned)((carry >> (16 * k)) & 0xFFFFull));
+        if (lane == 0) st[k] = v;
+    }
     __syncwarp();
 }
 
@@ -1176,36 +1207,6 @@ __device__ void yz_outer_features(const YzWarp &S, const YzEvent &E, const YzHit
     f[15] = (float)S.nhx;
 }
 
-// The station-2 load attempts of an outer iteration do not depend on the
-// iteration (only on the inner pair, K:1467-1597): the last inner combination
-// writing scratch offset m (past the station-3 hit count) is the same in
-// every live outer iteration.  Returns those hits as arena offsets, 16 bits
-// per offset m = 0..3, 0xFFFF where no combination writes m.
-__device__ unsigned long long yz_last_writes(const YzWarp &S, const YzHit *base) {
-    const int lane = lane_id();
-    const int nu2 = S.np[0];
-    const int C2 = S.np[0] * S.np[1];
-    unsigned long long lasto = ~0ull;
-#pragma unroll 1
-    for (int b0 = 0; b0 < C2; b0 += 32) {
-        const int c = b0 + lane;
-        int mine[4] = {-1, -1, -1, -1};
-        if (c < C2) {
-            const S2Writes w = s2_writes(S, base, c % nu2, c / nu2);
-#pragma unroll
-            for (int k = 0; k < w.n; ++k) mine[w.off[k]] = (int)(w.hit[k] - base);
-        }
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            const int l = last_lane(__ballot_sync(0xffffffffu, mine[m] >= 0));
-            if (l >= 0) {
-                const unsigned long long o = (unsigned long long)(unsigned)__shfl_sync(0xffffffffu, mine[m], l);
-                lasto = (lasto & ~(0xFFFFull << (16 * m))) | (o << (16 * m));
-            }
-        }
-    }
-    return lasto;
-}
 
 // Skip the pruned live outer iterations from rank r (the scorer's rows of
 // the tracklet are its live outer iterations in loop order): returns the
@@ -1657,44 +1658,6 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
     return cs.best;
 }
 
-static_assert(8 * YZ_MAXWIN <= 1024, "arena offsets fit 10 bits");
-
-// The station-2 record of the inner pair (iu2, iv2): its load attempts in
-// the reference order (K:1467-1597) reduced to what the first cut needs, the
-// same in every outer iteration.  16-bit field e (0..3) holds in bits 0-9 the
-// arena offset of the last hit attempted when e of the pair's hits had been
-// accepted -- for e below the accepted count, accepted hit e, in order -- so
-// that after n3 station-3 hits the attempts write scratch entries e + n3 - 4;
-// bits 10-13 which fields were written, bits 26-28 the accepted count, bits
-// 42-45 the planes of the accepted hits (u2 u2' v2 v2'), bit 58 whether both
-// the u2 and the v2 group gave a hit (the first fit is reached).
-__device__ __forceinline__ unsigned long long yz_s2_record(const YzWarp &S, const YzHit *base, int iu2, int iv2) {
-    const short2 pu = S.pair[0][iu2], pv = S.pair[1][iv2];
-    const int offs[4] = {pu.x >= 0 ? S.woff[0] + pu.x : -1, pu.y >= 0 ? S.woff[1] + pu.y : -1,
-                         pv.x >= 0 ? S.woff[2] + pv.x : -1, pv.y >= 0 ? S.woff[3] + pv.y : -1};
-    unsigned long long rec = 0ull;
-    unsigned pm = 0u, g2 = 0u;
-    int nacc = 0, nu = 0;
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-        if (a == 2) {
-            nu = nacc;
-            if (nu == 0) break;  // no u2 hit: v2 is not loaded
-        }
-        const int off = offs[a];
-        if (off < 0) continue;
-        const int sh = 16 * nacc;
-        rec = (rec & ~(0x3FFull << sh)) | ((unsigned long long)off << sh);
-        pm |= 1u << nacc;
-        if (base[off].acc) {
-            g2 |= 1u << a;
-            ++nacc;
-        }
-    }
-    const unsigned fit = (nu > 0 && nacc > nu) ? 1u : 0u;
-    return rec | ((unsigned long long)pm << 10) | ((unsigned long long)nacc << 26) | ((unsigned long long)g2 << 42) |
-           ((unsigned long long)fit << 58);
-}
 
 // The first cut of one unit over its live outer iterations, or with the
 // combination scorer (`osc`) over the kept ones only (first kernel).  The unit's live outer iterations
