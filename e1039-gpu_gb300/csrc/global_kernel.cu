@@ -33,11 +33,48 @@ struct GlWarp {
     short s_det[12], s_chan[12], s_sign[12];
     float s_drift[12], s_res[12];
     float Y[12], eY[12], Zy[12];
+    // the current track's (u1, v1) y fit by plane set (gl_tab_entry)
+    float tab[9][8];
     // best
     float b_chi2, b_ty, b_y0, b_invp, b_ety, b_ey0, b_einvp, b_charge;
     int b_n;
     float b_det[6], b_el[6], b_pos[6], b_drift[6], b_sign[6], b_tdc[6], b_res[18];
 };
+
+// The y fit of a (u1, v1) combination (K:2368-2379) adds the track's
+// station-2/3 y hits and then the accepted u1 u1' v1 v1' hits, each with its
+// plane's weight (calculate_y_uvhit's error, a plane constant) and z: its
+// normal matrix, inverse and errors depend only on which station-1 planes
+// gave a hit.  Entry (gu - 1) * 3 + gv - 1 (plane bits of the u1 and v1
+// groups, 1..3) holds Fit2::solve's inverse A^-1 (4), the 2-sigma bounds of
+// the first cut Y0_MAX + 2 err_y0, TY_MAX + 2 err_ty, and err_y0, err_ty --
+// computed as Fit2 accumulates (the station-2/3 hits first, the station-1
+// planes in attempt order), so a combination needs only its right-hand side.
+__device__ __forceinline__ void gl_tab_entry(const float *eY, const float *Zy, int nyh, int gu, int gv,
+                                             const short *dl, const or_plane_t &P, float *out) {
+    Fit2 f;
+#pragma unroll 1
+    for (int k = 0; k < nyh; ++k) f.add(0.f, Zy[k], eY[k]);
+    const int lists[4] = {2, 3, 4, 5};
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+        if (!((a < 2 ? gu >> a : gv >> (a - 2)) & 1)) continue;
+        const int d = dl[lists[a]];
+        f.add(0.f, P.z[d], P.resolution[d] * fabsf(P.deltapy[d] / P.deltapx[d]));
+    }
+    const float A[4] = {f.A0, f.A1, f.A2, f.A3};
+    float Ai[4];
+    matinv_2x2(A, Ai);
+    const float e0 = sqrtf(fabsf(Ai[0])), e1 = sqrtf(fabsf(Ai[3]));
+    out[0] = Ai[0];
+    out[1] = Ai[1];
+    out[2] = Ai[2];
+    out[3] = Ai[3];
+    out[4] = Y0_MAX + 2 * e0;
+    out[5] = TY_MAX + 2 * e1;
+    out[6] = e0;
+    out[7] = e1;
+}
 
 struct GHit {
     short det, el, sign;
@@ -257,6 +294,16 @@ __global__ void __launch_bounds__(W * 32)
                     }
                 }
                 __syncwarp();
+                // the y fit's station-1 plane sets, one per lane, and the
+                // right-hand side of the station-2/3 hits (Fit2::add order)
+                if (lane < 9) gl_tab_entry(S.eY, S.Zy, nyh, lane / 3 + 1, lane % 3 + 1, dl, P, S.tab[lane]);
+                float bs0 = 0.f, bs1 = 0.f;
+#pragma unroll 1
+                for (int k = 0; k < nyh; ++k) {
+                    bs0 += S.eY[k] * S.Y[k];
+                    bs1 += S.eY[k] * S.Y[k] * S.Zy[k];
+                }
+                __syncwarp();
                 float chi2min = 10000.1f;
                 bool update = false;
                 const int C = nu1 * nv1;
@@ -344,8 +391,8 @@ __global__ void __launch_bounds__(W * 32)
                         GHit h[6];
 #pragma unroll 1
                         for (int k = 0; k < nhx; ++k) h[k] = xh[k];
-                        float Yu[4], eYu[4], Zu[4];
-                        int nuv = 0, nhu = 0;
+                        float b0 = bs0, b1 = bs1;  // the y fit's right-hand side
+                        int nuv = 0, nhu = 0, gb = 0;  // gb: plane bits u1 u1' v1 v1' of the accepted hits
                         // scratch entries this combination writes: (list << 12 | hit index)
                         // codes, 16 bits each, entries 0-3 and 4-6
                         unsigned long long own_lo = 0ull, own_hi = 0ull;
@@ -372,9 +419,9 @@ __global__ void __launch_bounds__(W * 32)
                                 }
                                 float yy, ey;
                                 if (calculate_y_uvhit(u.det, u.el, u.drift, 0, xs0, xst, P, yy, ey)) {
-                                    Yu[nuv] = yy;
-                                    eYu[nuv] = ey;
-                                    Zu[nuv] = P.z[dl[lk]];
+                                    b0 += ey * yy;  // Fit2::add(yy, z, ey)
+                                    b1 += ey * yy * P.z[dl[lk]];
+                                    gb |= 1 << (lk - 2);
                                     ++nuv;
                                 }
                             };
@@ -394,14 +441,17 @@ __global__ void __launch_bounds__(W * 32)
                                 if (code != 0xFFFF) attempt(code >> 12, code & 0xFFF);
                             }
                             reached = nhu > 0 && nuv > nhu;
-                            if (reached) {  // K:2368-2379
-                                Fit2 f;
-#pragma unroll 1
-                                for (int k = 0; k < nyh; ++k) f.add(S.Y[k], S.Zy[k], S.eY[k]);
-#pragma unroll 1
-                                for (int k = 0; k < nuv; ++k) f.add(Yu[k], Zu[k], eYu[k]);
-                                f.solve(yc, tyc, eyc, etyc);
-                                pass1 = !(fabsf(yc) > Y0_MAX + 2 * eyc || fabsf(tyc) > TY_MAX + 2 * etyc);
+                            if (reached) {  // K:2368-2379, Fit2::solve with the plane set's inverse
+                                const float *te = S.tab[((gb & 3) - 1) * 3 + (gb >> 2) - 1];
+                                yc = 0.0f;
+                                yc += te[0] * b0;
+                                yc += te[1] * b1;
+                                tyc = 0.0f;
+                                tyc += te[2] * b0;
+                                tyc += te[3] * b1;
+                                eyc = te[6];
+                                etyc = te[7];
+                                pass1 = !(fabsf(yc) > te[4] || fabsf(tyc) > te[5]);
                             }
                         }
                         const int nall = nhx + nuv;
