@@ -1048,7 +1048,10 @@ __device__ __noinline__ void yz_phase2(YzWarp &S, const YzEvent &E, const YzHit 
 // scratch-entry scan.  Survivors (about 6% on the uneven batch) go to the
 // warp's queue in global memory, in order.  Phase 2 (yz_phase2, 32 at a time,
 // when the queue fills or the range ends): sign state, left/right walk, prop
-// and hodoscope gates, chi2 (K:1613-1799).
+// and hodoscope gates, chi2 (K:1613-1799).  This combined walk serves the
+// planning kernel's light tracklets and the units whose survivors do not fit
+// the pool; the first-cut kernel walks listed outer iterations with the
+// inner pairs' records instead (yz_first_kept).
 //
 // Outer iterations (iu3, iv3) whose u3 pair or v3 pair gives no accepted hit
 // are skipped whole: the reference leaves such an iteration before any
@@ -1496,10 +1499,10 @@ __device__ __forceinline__ int yz_scan_queue_off(const YzHit *base, const Stale 
     return qn;
 }
 
-template <bool FIRST_ONLY, bool PRUNE = false>
+template <bool PRUNE = false>
 __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l, long c1l,
                                          Stale st[4], const or_plane_t &P, const YzTab *__restrict__ tab,
-                                         PassEntryStore *Q, int qcap, int *nsurv, const float *__restrict__ osc = nullptr,
+                                         PassEntryStore *Q, int qcap, const float *__restrict__ osc = nullptr,
                                          float t_keep = 0.f) {
     const int lane = lane_id();
     const int nu2 = S.np[0], nu3 = S.np[2];
@@ -1586,12 +1589,6 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
             }
         }
         const bool more = basec < c1;
-        if constexpr (FIRST_ONLY) {
-            if (!more) {
-                *nsurv = qn;
-                return ~0ull;
-            }
-        }
         if (!more && qn == qh) break;
         if (more) {
             const int c = basec + lane;
@@ -1636,14 +1633,7 @@ __device__ unsigned long long yz_range_t(YzWarp &S, const YzEvent &E, const YzHi
             d2 -= cy ? nu3 : 0;
             d3 += s3 + cy;
         }
-        if constexpr (FIRST_ONLY) {
-            // survivors stay queued for the survivor kernel; a queue that
-            // could overflow gives the unit back to the combined path
-            if (qn > qcap - 32) {
-                *nsurv = -1;
-                return ~0ull;
-            }
-        } else if (qn > qcap - 32 || (!more && qn > qh)) {
+        if (qn > qcap - 32 || (!more && qn > qh)) {
             // a full queue (the next chunk could add 32) or the end of the
             // range: evaluate every waiting survivor, 32 at a time, in order
             while (qh < qn) {
@@ -1854,7 +1844,7 @@ template <bool PRUNE>
 __device__ __noinline__ unsigned long long yz_range_ool(YzWarp &S, const YzEvent &E, const YzHit *base, long c0l,
                                                         long c1l, Stale *st, const or_plane_t &P, const YzTab *tab,
                                                         PassEntryStore *Q, int qcap, const float *osc, float t_keep) {
-    return yz_range_t<false, PRUNE>(S, E, base, c0l, c1l, st, P, tab, Q, qcap, nullptr, osc, t_keep);
+    return yz_range_t<PRUNE>(S, E, base, c0l, c1l, st, P, tab, Q, qcap, osc, t_keep);
 }
 
 // write the best combination into the track record (K:1804-1825)
@@ -2141,8 +2131,8 @@ __global__ void __launch_bounds__(W * 32, (OR_YZ_WARPS_SM / W > 0 ? OR_YZ_WARPS_
         const long C2 = (long)S.np[0] * S.np[1];
         const float *osc = PRUNE ? yz_tracklet_scores(prune, hv2) : nullptr;
         const unsigned long long bk =
-            yz_range_t<false, PRUNE>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P,
-                                     sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap, nullptr, osc, prune.t_keep);
+            yz_range_t<PRUNE>(S, E, base, (long)un.g0 * C2, (long)un.g1 * C2, st, P,
+                              sc.tab + YZ_TAB_SETS * (st3 - 3), Q, sc.qcap, osc, prune.t_keep);
         __syncwarp();
         YzBest *dst = sc.best + u;
         if (bk == ~0ull) {
