@@ -75,7 +75,7 @@ constexpr int YZ_MAXPAIR = 100;         // pairs per projection (the reference's
 #define OR_YZ_SPLIT 1
 #endif
 #ifndef OR_YZ_PLAN_WARPS_SM
-#define OR_YZ_PLAN_WARPS_SM 24
+#define OR_YZ_PLAN_WARPS_SM 28
 #endif
 #ifndef OR_YZ_FIRST_WARPS_SM
 #define OR_YZ_FIRST_WARPS_SM 28
