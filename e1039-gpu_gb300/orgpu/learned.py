@@ -4,7 +4,7 @@ A 16-64-64-1 MLP (BF16 weights and activations, FP32 sums, sigmoid) scores
 every XZ tracklet from 16 features (or_tracklet_features); the YZ
 combinatorics of tracklets scoring below a threshold are skipped
 (or_yz_pruned), everything else is the plain path, so every kept tracklet
-gets the plain result bit for bit and the plain method stays the judge:
+gets the plain result bit for bit and the plain method stays the arbiter:
 recall = share of the plain run's global tracks that the learned run
 reproduces exactly (or_track_agreement).
 

@@ -1,6 +1,6 @@
 """The combination scorer (or_yz_scored): pruning of the station-3 (u3, v3)
 outer iterations of queued YZ tracklets, checked by the properties that make
-the plain method its judge, with a seeded untrained network (the properties
+the plain method its arbiter, with a seeded untrained network (the properties
 hold for any scores):
 
   - rows only (no model): the YZ output equals or_yz's bit for bit, and the
