@@ -930,7 +930,20 @@ __device__ __noinline__ void yz_phase2(YzWarp &S, const YzEvent &E, const YzHit 
     const bool carried_f = (g == cs.g) && cs.hasf;
     const int fl = __ffs(vm & seg) - 1;
     const bool is_first = valid && !carried_f && fl == lane;
-    if (is_first) U.sign = walk_uv(nuv, U, base, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
+    // Every survivor walks at once.  A first survivor of its outer iteration
+    // starts from unset signs; the others start with placeholder station-3
+    // signs: the walk only asks whether a sign is set, so it passes over the
+    // station-3 pairs and singles and resolves the station-2 hits and the
+    // cross pair exactly as it does after their real signs, which are put in
+    // below (the first survivor's, or the cross pair's where it resolved).
+    if (valid) {
+        if (!is_first) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (k < n3) uv_set_sign(U, k, 1);
+        }
+        U.sign = walk_uv(nuv, U, base, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
+    }
     short sig[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -958,14 +971,17 @@ __device__ __noinline__ void yz_phase2(YzWarp &S, const YzEvent &E, const YzHit 
     bool pass = false;
     float chi2 = 0.f;
     if (valid && !is_first) {
+        // the station-3 signs this survivor's walk would have started from:
+        // the first survivor's, the last hit's re-set by an earlier survivor's
+        // cross pair; its own cross pair, where resolved, already set the last
+        // station-3 hit in the walk above
 #pragma unroll
         for (int k = 0; k < 4; ++k)
-            if (k < n3) uv_set_sign(U, k, sig[k]);
-        if (n3 > 0) {
+            if (k < n3 && !(xok && k == n3 - 1)) uv_set_sign(U, k, sig[k]);
+        if (n3 > 0 && !xok) {
             if (xs >= 0) uv_set_sign(U, n3 - 1, xprev);
             else if (g == cs.g && cs.hascross) uv_set_sign(U, n3 - 1, cs.cross);
         }
-        U.sign = walk_uv(nuv, U, base, stj, x0, tx, y0, ty, ex0, etx, ey0, ety, P);
     }
     if (valid) {
         pass = yz_gates(E, P, x0, y0, tx, ty, ex0, ey0, etx, ety);
