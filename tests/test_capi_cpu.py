@@ -78,3 +78,18 @@ def test_context_bytes_scale_with_the_largest_batch():
     ctx = C.c_void_p()
     assert lb.or_create_sized(0, -5, C.byref(ctx)) == _lib.OR_ERR_ARG
     assert lb.or_create_sized(0, 10000, None) == _lib.OR_ERR_ARG
+
+
+def test_serving_slot_bytes_use_a_sized_context():
+    """A serving slot of 10,000 events is admitted by its real footprint: its
+    batch buffers plus a context sized for 10,000 events, not the 100,000-
+    event default."""
+    from orgpu import _lib, layout as L
+    from orgpu.serving import Server
+    lb = _lib.lib()
+    cap, rec = 10000, 400
+    base = (lb.or_hits_view_bytes(cap) + lb.or_tracks_view_bytes(cap) + cap * rec * 16 +
+            4 * cap * L.COLLECT_STRIDE * 4)
+    assert Server.slot_bytes(cap, rec, False, 152) == base + lb.or_context_bytes(cap, 152)
+    assert Server.slot_bytes(cap, rec, True, 152) > Server.slot_bytes(cap, rec, False, 152)
+    assert Server.slot_bytes(cap, rec, False, 152) < base + lb.or_context_bytes(0, 152) - 5e9
